@@ -1,0 +1,359 @@
+"""Benchmark of the path-tracer pass on GB300.
+
+Headline workload (one "step"): closest-hit traversal of 8,388,608 incoherent
+rays (origins uniform in the Cornell box, directions uniform on the sphere)
+through the 256,012-triangle Cornell-box scene with 200 level-3 icospheres —
+the incoherent test of the 1920x1080 path-tracing configuration. Metric:
+Mrays/s closest hit.
+
+  value  rays / device time, rays and hits resident in HBM
+  e2e    the same through the C ABI with pinned HOST buffers: every step
+         copies the rays in and the hits out inside the timed region
+  roofline  algorithmic bytes per ray (counted by the CPU oracle on the
+         binary binned-SAH BVH: 32 B ray + 8 B hit + 32 B per node box fetched
+         + 36 B per triangle tested) x rays / average kernel time, against the
+         measured HBM copy bandwidth; an L2 read bandwidth measured here is
+         reported beside it because the 16 MB BVH stays L2-resident
+  cpu_baseline  the CPU oracle (scalar C++, all host threads) on the same
+         workload, timed on this host
+
+Multi-GPU: the pass does not exchange data between GPUs; N ranks trace N
+independent ray batches of the same size (replicas, weak scaling).
+
+--impl reference: the reference renderer has no ray tracer; its arm times
+the CPU restatement of the path (the oracle) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_RAYS = 8_388_608
+METRIC = "Mrays/s closest-hit"
+UNIT = "Mrays/s"
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "trace_closest_cornell_incoherent.txt")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--rays", type=int, default=N_RAYS)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload(rank: int, n_rays: int):
+    from foundation_gb300 import scenes
+    sc = scenes.cornell_scene()
+    rays = scenes.incoherent_rays(n_rays, *sc.bounds, seed=1, stream_base=(1 << 40) + rank * n_rays)
+    return sc, rays
+
+
+def config_block(sc, n_rays, world):
+    return {
+        "workload": "cornell200 incoherent closest-hit",
+        "scene": "Cornell box + 200 level-3 icospheres (seed 1)",
+        "scene_tris": sc.num_tris,
+        "rays_per_step_per_gpu": n_rays,
+        "rays": "origins uniform in the box, directions uniform on S^2",
+        "bvh": "binned SAH 32 bins, <=4 tris/leaf, collapsed to 8-wide compressed nodes",
+        "l2": "inputs larger than L2: 268 MB of rays streamed per step per GPU",
+        "parallelism": f"replicas x{world}",
+    }
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms."""
+
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            self.samples.append((time.perf_counter(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0: float, t1: float):
+        rows = [p for t, p in self.samples if t0 - 0.1 <= t <= t1 + 0.1]
+        mine = [p for p in rows if self.uuid is None or self.uuid.lower() in p[0].lower()]
+        rows = mine or rows
+        if not rows:
+            rows = [p for _, p in self.samples]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+        sm = [num(p[1]) for p in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for p in rows:
+            for name, v in zip(names, p[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.nanmedian(sm)), "sm_max_mhz": num(rows[0][2]), "reasons": sorted(reasons),
+                "power_w_max": float(np.nanmax([num(p[3]) for p in rows])), "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per launch of the traversal kernel from the committed ncu
+    summary (a line 'dram_bytes_per_launch: N'), or None."""
+    if not os.path.exists(PROFILE_SUMMARY):
+        return None
+    for line in open(PROFILE_SUMMARY):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def l2_read_gbs(torch) -> float:
+    x = torch.ones(16 << 20, dtype=torch.float32, device="cuda")  # 64 MB, L2-resident
+    best = float("inf")
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        x.sum()
+    for _ in range(20):
+        s.record()
+        x.sum()
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return x.numel() * 4 / (best * 1e-3) / 1e9
+
+
+def algorithmic_bytes_per_ray(sc, rays, sample=1 << 20):
+    import oracle
+    b = oracle.OracleBVH(sc.verts, sc.idx)
+    _, st = b.closest(rays[:sample], with_stats=True)
+    n = min(sample, len(rays))
+    nodes, tris = st["node_fetches"] / n, st["tri_tests"] / n
+    return 32.0 + 8.0 + 32.0 * nodes + 36.0 * tris, nodes, tris
+
+
+def cpu_baseline(sc, rays):
+    import oracle
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    b = oracle.OracleBVH(sc.verts, sc.idx)
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b.closest(rays, threads=cores)
+    dt = time.perf_counter() - t0
+    n1 = min(len(rays), 1 << 18)
+    t0 = time.perf_counter()
+    b.closest(rays[:n1], threads=1)
+    dt1 = time.perf_counter() - t0
+    return {"value": len(rays) / dt / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"all {len(rays)} rays of one step, scalar C++ oracle on {cores} threads",
+            "single_core_mrays_s": n1 / dt1 / 1e6, "bvh_build_s": build_s}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    sc, rays = workload(0, args.rays)
+    b = oracle.OracleBVH(sc.verts, sc.idx)
+    cores = os.cpu_count() or 1
+    sample = min(len(rays), 1 << 20)
+    for i in range(args.warmup):
+        b.closest(rays[:sample], threads=cores)
+    times = []
+    for i in range(args.steps):
+        off = (i * sample) % max(1, len(rays) - sample + 1)
+        t0 = time.perf_counter()
+        b.closest(rays[off:off + sample], threads=cores)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = sample * args.steps / tot / 1e6
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_block(sc, args.rays, 1), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{sample} rays of the workload per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "mos9527/Foundation has no ray tracer; its arm is the CPU restatement of the path"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    import foundation_gb300 as fg
+    fg.load()  # fails loudly when the native library is missing
+    sc, rays = workload(rank, args.rays)
+    n = len(rays)
+    stream = torch.cuda.Stream()
+    ctx = fg.Context(local, stream=stream.cuda_stream)
+    scene = ctx.upload(sc.verts, sc.idx)
+    info = scene.info()
+    rd = torch.from_numpy(rays).to("cuda")
+    hd = torch.empty(2 * n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    try:
+        uuid = torch.cuda.get_device_properties(local).uuid
+        uuid = str(uuid)
+    except Exception:
+        uuid = None
+    clocks = ClockSampler(uuid)
+    clocks.start()
+    for _ in range(args.warmup):
+        scene.closest(rd, hd)
+    ctx.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            scene.closest(rd, hd)
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.perf_counter()
+    ctx.sync()
+    if world > 1:
+        dist.barrier()
+    per_step = [s.elapsed_time(e) for s, e in ev]
+    total_ms = ev[0][0].elapsed_time(ev[-1][1])
+    clk = clocks.summary(t_wall0, t_wall1)
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    value = n * args.steps * world / (total_ms * 1e-3) / 1e6
+
+    # end to end through the C ABI with pinned host buffers
+    pin_in = fg.PinnedBuffer(n * 32)
+    pin_out = fg.PinnedBuffer(n * 8)
+    hr = pin_in.view(np.float32, (n, 8))
+    hr[:] = rays
+    ho = pin_out.view(fg.HIT_DTYPE, (n,))
+    for _ in range(max(1, args.warmup // 2)):
+        scene.closest(hr, ho)
+    if world > 1:
+        dist.barrier()
+    e2e_steps = max(3, args.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        scene.closest(hr, ho)
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = n * e2e_steps * world / float(te.item()) / 1e6
+    # spot-check the end-to-end result against the device result
+    dev_hits = hd.cpu().numpy().view(np.uint32)
+    e2e_ok = bool(np.array_equal(dev_hits[0::2], ho["prim"]))
+    clocks.stop()
+
+    if rank == 0:
+        peaks, peak_kind = measured_peaks()
+        bpr, nodes, tris = algorithmic_bytes_per_ray(sc, rays)
+        kern_ms = float(np.mean(per_step))
+        achieved = bpr * n / (kern_ms * 1e-3) / 1e9
+        traffic = profile_traffic()
+        l2 = l2_read_gbs(torch)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_block(sc, n, world),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8,
+                    "steps": e2e_steps, "matches_device_result": e2e_ok},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                         "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
+                         "algorithmic_bytes_per_ray": bpr, "oracle_nodes_per_ray": nodes,
+                         "oracle_tris_per_ray": tris, "kernel_ms_avg": kern_ms,
+                         "l2_read_gbs_measured": l2, "frac_of_l2": achieved / l2},
+            "clocks": clk,
+            "scene_info": {k: info[k] for k in ("num_wide_nodes", "wide_depth", "node_bytes", "tri_bytes",
+                                                "build_ms", "collapse_ms")},
+        }
+        if not args.no_cpu_baseline and world == 1:
+            line["cpu_baseline"] = cpu_baseline(sc, rays)
+        print(json.dumps(line), flush=True)
+    scene.close()
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

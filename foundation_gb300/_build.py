@@ -1,0 +1,98 @@
+"""In-tree build of the native library (libfnd_rt.so) with nvcc for sm_103a.
+
+Compiles every translation unit under csrc/ in parallel (one -gencode, no
+cmake) and links one shared library into foundation_gb300/lib/. Objects go
+to foundation_gb300/_build/ and are rebuilt when a source or any header is
+newer than the object.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OBJ_DIR = os.path.join(PKG, "_build")
+LIB_DIR = os.path.join(PKG, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libfnd_rt.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-pthread,-Wall",
+          f"-I{os.path.join(ROOT, 'include')}"]
+# host sources: contraction off so host float code matches its stated
+# expression trees on both x86-64 and aarch64 hosts
+HOST_FLAGS = ["-Xcompiler", "-ffp-contract=off"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found (set NVCC or put the CUDA toolkit on PATH)")
+
+
+def _sources():
+    srcs = sorted(glob.glob(os.path.join(CSRC, "**", "*.cu"), recursive=True))
+    srcs += sorted(glob.glob(os.path.join(CSRC, "**", "*.cpp"), recursive=True))
+    return srcs
+
+
+def _headers():
+    hs = glob.glob(os.path.join(CSRC, "**", "*.h*"), recursive=True)
+    hs += glob.glob(os.path.join(CSRC, "**", "*.cuh"), recursive=True)
+    hs += glob.glob(os.path.join(ROOT, "include", "*.h"))
+    return hs
+
+
+def _obj_for(src: str) -> str:
+    rel = os.path.relpath(src, CSRC).replace(os.sep, "__")
+    return os.path.join(OBJ_DIR, rel + ".o")
+
+
+def _compile(src: str, force: bool, newest_header: float) -> tuple[str, bool]:
+    obj = _obj_for(src)
+    if not force and os.path.exists(obj):
+        t = os.path.getmtime(obj)
+        if t >= os.path.getmtime(src) and t >= newest_header:
+            return obj, False
+    cmd = [nvcc(), *ARCH, *COMMON]
+    if src.endswith(".cpp"):
+        cmd += HOST_FLAGS
+    cmd += ["-c", src, "-o", obj + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(obj + ".tmp", obj)
+    return obj, True
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    srcs = _sources()
+    newest = max((os.path.getmtime(h) for h in _headers()), default=0.0)
+    jobs = min(len(srcs), max(1, os.cpu_count() or 1))
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        results = list(ex.map(lambda s: _compile(s, force, newest), srcs))
+    objs = [o for o, _ in results]
+    rebuilt = any(b for _, b in results)
+    if rebuilt or force or not os.path.exists(LIB_PATH) or \
+            any(os.path.getmtime(o) > os.path.getmtime(LIB_PATH) for o in objs):
+        tmp = LIB_PATH + f".tmp{os.getpid()}"
+        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB_PATH)
+        if verbose:
+            print(f"linked {LIB_PATH}", file=sys.stderr)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)

@@ -1,0 +1,48 @@
+// bvh_build.hpp — binned-SAH binary BVH over triangles (host, multi-threaded).
+//
+// Algorithm (Wald 2007, "On fast Construction of SAH-based Bounding Volume
+// Hierarchies"): per node, bin triangle bounding-box centroids into K bins
+// along each axis with non-zero centroid extent, sweep bin bounds from both
+// ends, split where C_trav + C_isect * (A_L N_L + A_R N_R) / A_node is least
+// (C_trav = C_isect = 1, half surface areas, first minimum wins, axes in
+// x, y, z order); make a leaf when the node holds at most max_leaf triangles
+// and the leaf cost N is not above the split cost; when all centroids of a
+// node coincide, split at the median of the triangle indices. The tree this
+// produces is a function of the triangle set only (not of thread timing).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace Foundation {
+namespace RT {
+
+struct Aabb {
+    float lo[3], hi[3];
+};
+
+struct BinaryNode {
+    float lo[3], hi[3];
+    uint32_t a;      // internal: left child index (right = a + 1); leaf: first slot in prims
+    uint32_t count;  // 0 for internal nodes, triangle count for leaves
+};
+
+struct BinaryBvh {
+    std::vector<BinaryNode> nodes;  // nodes[0] is the root
+    std::vector<uint32_t> prims;    // leaf slots -> original triangle index
+    uint32_t depth = 0;
+    uint32_t leaves = 0;
+    double sah_cost = 0.0;  // normalised by the root half-area
+};
+
+struct BuildParams {
+    uint32_t bins = 32;
+    uint32_t max_leaf = 4;
+    uint32_t threads = 0;  // 0: hardware concurrency
+};
+
+// tri: 9 floats per triangle (v0, v1, v2). nt > 0.
+void BuildBinaryBvh(const float* tri, uint32_t nt, const BuildParams& params, BinaryBvh& out);
+
+}  // namespace RT
+}  // namespace Foundation

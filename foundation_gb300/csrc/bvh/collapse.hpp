@@ -1,0 +1,32 @@
+// collapse.hpp — binary BVH -> compressed 8-wide BVH + triangle vertex planes.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "bvh_build.hpp"
+#include "wide_bvh.hpp"
+
+namespace Foundation {
+namespace RT {
+
+struct WideBvh {
+    std::vector<WideNode> nodes;
+    std::vector<float> v0, v1, v2;  // 4 floats per triangle each (see wide_bvh.hpp)
+    uint32_t depth = 0;             // wide levels on the longest root-to-leaf path
+    uint32_t leaves = 0;
+    float margin = 0.0f;            // absolute outward inflation of every box
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+// Absolute box inflation that keeps the FP32 slab test conservative: 2^-16 of
+// the largest of |coordinate| and extent over the scene bounds. It covers the
+// rounding of (p - o) * inv_dir for ray origins within about 50x that size.
+float SceneMargin(const float lo[3], const float hi[3]);
+
+// Greedy collapse (largest-surface-area internal child expanded first until 8
+// children), octant-ordered slot assignment, 8-bit outward quantisation.
+void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out);
+
+}  // namespace RT
+}  // namespace Foundation

@@ -1,0 +1,408 @@
+// capi_trace.cpp — C ABI: context, scene upload, closest / any-hit traversal.
+//
+// Every entry point runs its body inside Guard(): C++ failures (FndError from
+// CHECK / Fail, std::bad_alloc, CUDA errors) become a negative fnd_status and
+// a message in fnd_rt_last_error; nothing throws across the ABI and nothing
+// terminates the process (the reference's CHECK -> BugCheck -> terminate,
+// src/Core/Core.cpp:7-10, is not acceptable behind a C ABI).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "../bvh/bvh_build.hpp"
+#include "../bvh/collapse.hpp"
+#include "context.hpp"
+
+using namespace Foundation;
+using Foundation::Core::Fail;
+using Foundation::Core::FndError;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+template <typename F>
+int Guard(fnd_rt_ctx* ctx, F&& body) {
+    std::string* err = ctx ? &ctx->last_error : &g_create_error;
+    try {
+        body();
+        err->clear();
+        return FND_OK;
+    } catch (const FndError& e) {
+        *err = e.what();
+        LOG_RUNTIME(FndRt, ERR, "%s", e.what());
+        return e.code();
+    } catch (const std::bad_alloc&) {
+        *err = "host allocation failed";
+        return FND_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        *err = e.what();
+        return FND_ERR_INVALID_ARG;
+    }
+}
+
+double MsSince(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void UseDevice(const fnd_rt_ctx* ctx) { CUDA_CHECK(cudaSetDevice(ctx->device)); }
+
+}  // namespace
+
+namespace Foundation {
+namespace CApi {
+
+void CudaCheck(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return;
+    const int code = e == cudaErrorMemoryAllocation ? FND_ERR_OUT_OF_MEMORY
+                     : (e == cudaErrorNoDevice || e == cudaErrorInvalidDevice) ? FND_ERR_NO_DEVICE
+                                                                                 : FND_ERR_CUDA;
+    Fail(code, "%s failed: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+void EnsureDevice(void*& ptr, size_t& cap, size_t bytes) {
+    if (bytes <= cap) return;
+    if (ptr) CUDA_CHECK(cudaFree(ptr));
+    ptr = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 4;
+    CUDA_CHECK(cudaMalloc(&ptr, want));
+    cap = want;
+}
+
+int ReadStatus(fnd_rt_ctx* ctx) {
+    CUDA_CHECK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    const uint32_t s = *ctx->h_status;
+    if (s == 0) return FND_OK;
+    CUDA_CHECK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
+    CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (s & RT::kStatusStackOverflow) return FND_ERR_STACK_OVERFLOW;
+    if (s & RT::kStatusTimeout) return FND_ERR_TIMEOUT;
+    return FND_ERR_CUDA;
+}
+
+}  // namespace CApi
+}  // namespace Foundation
+
+using namespace Foundation::CApi;
+
+extern "C" {
+
+int fnd_rt_create(const fnd_rt_desc* desc, fnd_rt_ctx** out_ctx) {
+    return Guard(nullptr, [&] {
+        CHECK(desc != nullptr && out_ctx != nullptr);
+        *out_ctx = nullptr;
+        CHECK_CODE(desc->abi_version == FND_RT_ABI_VERSION, FND_ERR_INVALID_ARG, "ABI version %u, library has %u",
+                   desc->abi_version, FND_RT_ABI_VERSION);
+        int count = 0;
+        CUDA_CHECK(cudaGetDeviceCount(&count));
+        CHECK_CODE(desc->device >= 0 && desc->device < count, FND_ERR_NO_DEVICE, "device %d of %d", desc->device,
+                   count);
+        cudaDeviceProp prop;
+        CUDA_CHECK(cudaGetDeviceProperties(&prop, desc->device));
+        CHECK_CODE(prop.major == 10 && prop.minor == 3, FND_ERR_NO_DEVICE,
+                   "device %d is sm_%d%d; this library is built for sm_103a only", desc->device, prop.major,
+                   prop.minor);
+        auto ctx = std::make_unique<fnd_rt_ctx>();
+        ctx->device = desc->device;
+        ctx->sm_count = prop.multiProcessorCount;
+        CUDA_CHECK(cudaSetDevice(ctx->device));
+        auto cleanup = [&](fnd_rt_ctx* c) {
+            if (c->d_counter) cudaFree(c->d_counter);
+            if (c->h_status) cudaFreeHost(c->h_status);
+            if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+        };
+        try {
+            if (desc->stream) {
+                ctx->stream = (cudaStream_t)desc->stream;
+            } else {
+                CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+                ctx->own_stream = true;
+            }
+            // one allocation: counter (256 B slot), status (256 B slot), stats
+            char* scratch = nullptr;
+            CUDA_CHECK(cudaMalloc(&scratch, 1024));
+            ctx->d_counter = reinterpret_cast<uint32_t*>(scratch);
+            ctx->d_status = reinterpret_cast<uint32_t*>(scratch + 256);
+            ctx->d_stats = reinterpret_cast<unsigned long long*>(scratch + 512);
+            CUDA_CHECK(cudaMemsetAsync(scratch, 0, 1024, ctx->stream));
+            CUDA_CHECK(cudaMallocHost(&ctx->h_status, sizeof(uint32_t)));
+            for (int v = 0; v < 4; ++v) CUDA_CHECK(RT::TraceOccupancy(v, &ctx->occupancy[v]));
+            CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        } catch (...) {
+            cleanup(ctx.get());
+            throw;
+        }
+        if (const char* s = std::getenv("FND_RT_REFILL_MIN")) ctx->refill_min = (uint32_t)std::atoi(s);
+        *out_ctx = ctx.release();
+    });
+}
+
+int fnd_rt_destroy(fnd_rt_ctx* ctx) {
+    if (!ctx) return FND_ERR_INVALID_ARG;
+    const int rc = Guard(ctx, [&] {
+        CHECK_CODE(ctx->live_scenes == 0, FND_ERR_INVALID_ARG, "%d scenes still alive", ctx->live_scenes);
+        UseDevice(ctx);
+        CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+    if (rc == FND_ERR_INVALID_ARG) return rc;
+    cudaSetDevice(ctx->device);
+    if (ctx->d_counter) cudaFree(ctx->d_counter);
+    if (ctx->d_in) cudaFree(ctx->d_in);
+    if (ctx->d_out) cudaFree(ctx->d_out);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return rc;
+}
+
+const char* fnd_rt_last_error(const fnd_rt_ctx* ctx) { return ctx ? ctx->last_error.c_str() : g_create_error.c_str(); }
+
+int fnd_rt_sync(fnd_rt_ctx* ctx) {
+    if (!ctx) return FND_ERR_INVALID_ARG;
+    int status = FND_OK;
+    const int rc = Guard(ctx, [&] {
+        UseDevice(ctx);
+        status = ReadStatus(ctx);
+        if (status != FND_OK)
+            Fail(status, "device status: %s",
+                 status == FND_ERR_STACK_OVERFLOW ? "traversal stack overflow" : "bounded wait timed out");
+    });
+    return rc;
+}
+
+void* fnd_rt_stream(const fnd_rt_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                        const fnd_rt_bvh_desc* bvh, fnd_rt_scene** out_scene) {
+    if (!ctx) return FND_ERR_INVALID_ARG;
+    return Guard(ctx, [&] {
+        CHECK(out_scene != nullptr);
+        *out_scene = nullptr;
+        CHECK(nt == 0 || (verts != nullptr && idx != nullptr));
+        CHECK_CODE(nt <= (1u << 30), FND_ERR_INVALID_SCENE, "%u triangles exceed the 2^30 limit", nt);
+        RT::BuildParams bp;
+        if (bvh) {
+            if (bvh->sah_bins) bp.bins = bvh->sah_bins;
+            if (bvh->max_leaf_tris) bp.max_leaf = bvh->max_leaf_tris;
+            bp.threads = bvh->build_threads;
+        }
+        CHECK_CODE(bp.bins >= 2 && bp.bins <= 64, FND_ERR_INVALID_ARG, "sah_bins %u not in [2, 64]", bp.bins);
+        CHECK_CODE(bp.max_leaf >= 1 && bp.max_leaf <= 4, FND_ERR_INVALID_ARG, "max_leaf_tris %u not in [1, 4]",
+                   bp.max_leaf);
+        UseDevice(ctx);
+        auto scene = std::make_unique<fnd_rt_scene>();
+        scene->ctx = ctx;
+        scene->info.num_tris = nt;
+        if (nt == 0) {
+            *out_scene = scene.release();
+            ctx->live_scenes++;
+            return;
+        }
+        // gather + validate (parallel over triangle ranges)
+        std::vector<float> tri(9 * (size_t)nt);
+        {
+            const unsigned threads = bp.threads ? bp.threads : std::max(1u, std::thread::hardware_concurrency());
+            std::vector<std::thread> pool;
+            std::vector<int> bad(threads, 0);
+            const uint32_t chunk = (nt + threads - 1) / threads;
+            for (unsigned w = 0; w < threads; ++w) {
+                pool.emplace_back([&, w] {
+                    const uint32_t s = w * chunk, e = std::min<uint64_t>(nt, (uint64_t)s + chunk);
+                    for (uint32_t t = s; t < e && !bad[w]; ++t)
+                        for (int k = 0; k < 3; ++k) {
+                            const uint32_t vi = idx[3 * (size_t)t + k];
+                            if (vi >= nv) {
+                                bad[w] = 1;
+                                break;
+                            }
+                            for (int c = 0; c < 3; ++c) {
+                                const float x = verts[3 * (size_t)vi + c];
+                                if (!std::isfinite(x)) bad[w] = 2;
+                                tri[9 * (size_t)t + 3 * k + c] = x;
+                            }
+                        }
+                });
+            }
+            for (auto& t : pool) t.join();
+            for (int b : bad) {
+                CHECK_CODE(b != 1, FND_ERR_INVALID_ARG, "vertex index out of range (nv = %u)", nv);
+                CHECK_CODE(b != 2, FND_ERR_INVALID_ARG, "non-finite vertex coordinate");
+            }
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        RT::BinaryBvh bin;
+        RT::BuildBinaryBvh(tri.data(), nt, bp, bin);
+        scene->info.build_ms = MsSince(t0);
+        t0 = std::chrono::steady_clock::now();
+        RT::WideBvh wide;
+        RT::CollapseToWide(bin, tri.data(), nt, wide);
+        scene->info.collapse_ms = MsSince(t0);
+        CHECK_CODE(wide.depth <= (uint32_t)RT::kMaxStack / 2, FND_ERR_INVALID_SCENE,
+                   "wide BVH depth %u exceeds the traversal stack bound %d", wide.depth, RT::kMaxStack / 2);
+        fnd_rt_scene_info& I = scene->info;
+        I.num_binary_nodes = (uint32_t)bin.nodes.size();
+        I.binary_depth = bin.depth;
+        I.num_leaves = bin.leaves;
+        I.sah_cost = bin.sah_cost;
+        I.num_wide_nodes = (uint32_t)wide.nodes.size();
+        I.wide_depth = wide.depth;
+        I.node_bytes = wide.nodes.size() * sizeof(RT::WideNode);
+        I.tri_bytes = 3ull * 16ull * nt;
+        for (int a = 0; a < 3; ++a) {
+            I.bounds_lo[a] = wide.lo[a];
+            I.bounds_hi[a] = wide.hi[a];
+        }
+        I.box_margin = wide.margin;
+        t0 = std::chrono::steady_clock::now();
+        try {
+            CUDA_CHECK(cudaMalloc(&scene->d_nodes, I.node_bytes));
+            CUDA_CHECK(cudaMalloc(&scene->d_tris, I.tri_bytes));
+            char* tris = static_cast<char*>(scene->d_tris);
+            const size_t plane = 16ull * nt;
+            CUDA_CHECK(cudaMemcpy(scene->d_nodes, wide.nodes.data(), I.node_bytes, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(tris, wide.v0.data(), plane, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(tris + plane, wide.v1.data(), plane, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(tris + 2 * plane, wide.v2.data(), plane, cudaMemcpyHostToDevice));
+        } catch (...) {
+            if (scene->d_nodes) cudaFree(scene->d_nodes);
+            if (scene->d_tris) cudaFree(scene->d_tris);
+            throw;
+        }
+        I.upload_ms = MsSince(t0);
+        char* tris = static_cast<char*>(scene->d_tris);
+        const size_t plane = 16ull * nt;
+        scene->view.nodes = static_cast<const uint4*>(scene->d_nodes);
+        scene->view.v0 = reinterpret_cast<const float4*>(tris);
+        scene->view.v1 = reinterpret_cast<const float4*>(tris + plane);
+        scene->view.v2 = reinterpret_cast<const float4*>(tris + 2 * plane);
+        scene->view.num_nodes = I.num_wide_nodes;
+        scene->view.num_tris = nt;
+        *out_scene = scene.release();
+        ctx->live_scenes++;
+    });
+}
+
+int fnd_rt_scene_info_get(const fnd_rt_scene* scene, fnd_rt_scene_info* out_info) {
+    if (!scene || !out_info) return FND_ERR_INVALID_ARG;
+    *out_info = scene->info;
+    return FND_OK;
+}
+
+int fnd_rt_scene_destroy(fnd_rt_scene* scene) {
+    if (!scene) return FND_ERR_INVALID_ARG;
+    fnd_rt_ctx* ctx = scene->ctx;
+    const int rc = Guard(ctx, [&] {
+        UseDevice(ctx);
+        CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        if (scene->d_nodes) CUDA_CHECK(cudaFree(scene->d_nodes));
+        if (scene->d_tris) CUDA_CHECK(cudaFree(scene->d_tris));
+    });
+    ctx->live_scenes--;
+    delete scene;
+    return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n, void* out, int mem,
+              bool any, fnd_rt_trace_stats* stats) {
+    if (!ctx) return FND_ERR_INVALID_ARG;
+    return Guard(ctx, [&] {
+        CHECK(scene != nullptr && scene->ctx == ctx);
+        CHECK(mem == FND_MEM_HOST || mem == FND_MEM_DEVICE);
+        CHECK(n == 0 || (rays != nullptr && out != nullptr));
+        CHECK_CODE(n <= (1u << 31), FND_ERR_INVALID_ARG, "%u rays exceed the 2^31 limit per call", n);
+        UseDevice(ctx);
+        const size_t out_bytes = any ? (size_t)n : sizeof(fnd_hit) * (size_t)n;
+        const size_t in_bytes = sizeof(fnd_ray) * (size_t)n;
+        RT::TraceLaunch L{};
+        L.scene = scene->view;
+        L.n = n;
+        L.counter = ctx->d_counter;
+        L.status = ctx->d_status;
+        L.stats = ctx->d_stats;
+        L.refill_min = ctx->refill_min;
+        if (mem == FND_MEM_DEVICE) {
+            L.rays = reinterpret_cast<const float4*>(rays);
+            if (any)
+                L.occluded = static_cast<uint8_t*>(out);
+            else
+                L.hits = out;
+        } else {
+            EnsureDevice(ctx->d_in, ctx->d_in_cap, in_bytes);
+            EnsureDevice(ctx->d_out, ctx->d_out_cap, out_bytes);
+            if (n) CUDA_CHECK(cudaMemcpyAsync(ctx->d_in, rays, in_bytes, cudaMemcpyHostToDevice, ctx->stream));
+            L.rays = static_cast<const float4*>(ctx->d_in);
+            if (any)
+                L.occluded = static_cast<uint8_t*>(ctx->d_out);
+            else
+                L.hits = ctx->d_out;
+        }
+        if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        const int variant = (any ? 1 : 0) + (stats ? 2 : 0);
+        const int grid = ctx->sm_count * std::max(1, ctx->occupancy[variant]);
+        CUDA_CHECK(RT::LaunchTrace(L, any, stats != nullptr, grid, ctx->stream));
+        if (stats) {
+            unsigned long long h[2] = {0, 0};
+            CUDA_CHECK(cudaMemcpyAsync(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+            CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+            stats->rays = n;
+            stats->node_fetches = h[0];
+            stats->tri_tests = h[1];
+        }
+        if (mem == FND_MEM_HOST) {
+            if (n) CUDA_CHECK(cudaMemcpyAsync(out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+            const int s = ReadStatus(ctx);
+            if (s != FND_OK) Fail(s, "device status: traversal stack overflow");
+        }
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+int fnd_rt_trace_closest(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n, fnd_hit* out,
+                         int mem) {
+    return TraceImpl(ctx, scene, rays, n, out, mem, false, nullptr);
+}
+
+int fnd_rt_trace_any(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n, uint8_t* out,
+                     int mem) {
+    return TraceImpl(ctx, scene, rays, n, out, mem, true, nullptr);
+}
+
+int fnd_rt_trace_closest_stats(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n,
+                               fnd_hit* out, int mem, fnd_rt_trace_stats* stats) {
+    if (!stats) return FND_ERR_INVALID_ARG;
+    return TraceImpl(ctx, scene, rays, n, out, mem, false, stats);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int fnd_rt_host_alloc(size_t bytes, void** out_ptr) {
+    if (!out_ptr) return FND_ERR_INVALID_ARG;
+    *out_ptr = nullptr;
+    const cudaError_t e = cudaMallocHost(out_ptr, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        g_create_error = cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? FND_ERR_OUT_OF_MEMORY : FND_ERR_CUDA;
+    }
+    return FND_OK;
+}
+
+int fnd_rt_host_free(void* ptr) {
+    if (!ptr) return FND_OK;
+    return cudaFreeHost(ptr) == cudaSuccess ? FND_OK : FND_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,55 @@
+// context.hpp — internal definitions of the opaque C-ABI handles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../../include/fnd_rt.h"
+#include "../core/core.hpp"
+#include "../rt/traverse_launch.hpp"
+
+struct fnd_rt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sm_count = 0;
+    int occupancy[4] = {0, 0, 0, 0};  // blocks/SM of the trace kernel variants
+    uint32_t refill_min = 8;
+    // device scratch owned by the context
+    uint32_t* d_counter = nullptr;
+    uint32_t* d_status = nullptr;
+    unsigned long long* d_stats = nullptr;
+    uint32_t* h_status = nullptr;  // pinned
+    // staging buffers for FND_MEM_HOST calls
+    void* d_in = nullptr;
+    size_t d_in_cap = 0;
+    void* d_out = nullptr;
+    size_t d_out_cap = 0;
+    int live_scenes = 0;
+    std::string last_error;
+    Foundation::Core::HeapAllocator allocator;
+};
+
+struct fnd_rt_scene {
+    fnd_rt_ctx* ctx = nullptr;
+    void* d_nodes = nullptr;
+    void* d_tris = nullptr;
+    Foundation::RT::DeviceScene view{};
+    fnd_rt_scene_info info{};
+};
+
+namespace Foundation {
+namespace CApi {
+
+void CudaCheck(cudaError_t e, const char* what);
+#define CUDA_CHECK(expr) ::Foundation::CApi::CudaCheck((expr), #expr)
+
+// Grows a device staging buffer to at least `bytes`.
+void EnsureDevice(void*& ptr, size_t& cap, size_t bytes);
+
+// Reads and clears the latched device status; returns FND_OK or an error code.
+int ReadStatus(fnd_rt_ctx* ctx);
+
+}  // namespace CApi
+}  // namespace Foundation

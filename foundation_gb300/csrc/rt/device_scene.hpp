@@ -1,0 +1,27 @@
+// device_scene.hpp — plain (host-compilable) types shared by the traversal
+// kernels and the host launch code.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace Foundation {
+namespace RT {
+
+// Device status bits (latched, read back by fnd_rt_sync).
+constexpr uint32_t kStatusStackOverflow = 1u;
+constexpr uint32_t kStatusTimeout = 2u;
+
+constexpr int kMaxStack = 64;  // node-group + triangle-group entries per ray
+
+struct DeviceScene {
+    const uint4* nodes;  // 5 uint4 per WideNode
+    const float4* v0;    // (x, y, z, original index bits)
+    const float4* v1;
+    const float4* v2;
+    uint32_t num_nodes;
+    uint32_t num_tris;
+};
+
+}  // namespace RT
+}  // namespace Foundation

@@ -1,0 +1,176 @@
+// traverse.cuh — device-side scene view, ray set-up, watertight triangle test
+// and compressed 8-wide node test shared by every traversal kernel
+// (closest hit, any hit, the batched multi-scene launch and the integrator's
+// extend / shadow stages).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../bvh/wide_bvh.hpp"
+#include "device_scene.hpp"
+
+namespace Foundation {
+namespace RT {
+
+// Per-ray state for the node test (origin, sanitised inverse direction,
+// direction-sign octant) and for the watertight triangle test (shear
+// constants of Woop, Benthin & Wald 2013, dominant axis kz).
+struct RayState {
+    float ox, oy, oz;
+    float ix, iy, iz;
+    float nSx, nSy, Sz;  // -Sx, -Sy, Sz
+    float tmin, tmax;
+    uint32_t oct;
+    int kz;
+};
+
+__device__ __forceinline__ float sanitize_dir(float d) {
+    // keep the sign (also of -0.0); 2^-64 keeps the inverse finite
+    return fabsf(d) < 5.421010862427522e-20f ? copysignf(5.421010862427522e-20f, d) : d;
+}
+
+__device__ __forceinline__ RayState setup_ray(float4 r0, float4 r1) {
+    RayState s;
+    s.ox = r0.x;
+    s.oy = r0.y;
+    s.oz = r0.z;
+    s.tmin = r0.w;
+    s.tmax = r1.w;
+    s.ix = __fdiv_rn(1.0f, sanitize_dir(r1.x));
+    s.iy = __fdiv_rn(1.0f, sanitize_dir(r1.y));
+    s.iz = __fdiv_rn(1.0f, sanitize_dir(r1.z));
+    s.oct = (signbit(r1.x) ? 1u : 0u) | (signbit(r1.y) ? 2u : 0u) | (signbit(r1.z) ? 4u : 0u);
+    const float ax = fabsf(r1.x), ay = fabsf(r1.y), az = fabsf(r1.z);
+    const int kz = (ax >= ay) ? (ax >= az ? 0 : 2) : (ay >= az ? 1 : 2);
+    s.kz = kz;
+    const float dkz = kz == 0 ? r1.x : (kz == 1 ? r1.y : r1.z);
+    const float dkx = kz == 0 ? r1.y : (kz == 1 ? r1.z : r1.x);
+    const float dky = kz == 0 ? r1.z : (kz == 1 ? r1.x : r1.y);
+    s.nSx = -__fdiv_rn(dkx, dkz);
+    s.nSy = -__fdiv_rn(dky, dkz);
+    s.Sz = __fdiv_rn(1.0f, dkz);
+    return s;
+}
+
+// Cyclic permutation (kx, ky, kz) = (kz+1, kz+2, kz) mod 3.
+__device__ __forceinline__ void permute(const RayState& r, float a0, float a1, float a2, float& x, float& y, float& z) {
+    x = r.kz == 0 ? a1 : (r.kz == 1 ? a2 : a0);
+    y = r.kz == 0 ? a2 : (r.kz == 1 ? a0 : a1);
+    z = r.kz == 0 ? a0 : (r.kz == 1 ? a1 : a2);
+}
+
+__device__ __forceinline__ float edge_fallback(float ax, float by, float ay, float bx) {
+    return __double2float_rn(__dsub_rn(__dmul_rn((double)ax, (double)by), __dmul_rn((double)ay, (double)bx)));
+}
+
+// Watertight test, non-culling, same FP32 expression tree as the CPU
+// restatement: every operation is an explicit round-to-nearest intrinsic so
+// the compiler cannot contract or reorder it. Returns t (NaN-free) on a hit
+// with t in [tmin, tmax]; out_u/out_v/out_det for barycentrics on request.
+template <bool kBary = false>
+__device__ __forceinline__ bool intersect_tri(const RayState& r, float4 v0, float4 v1, float4 v2, float tmax,
+                                              float& t_out, float* bary = nullptr) {
+    float Ax, Ay, Az, Bx, By, Bz, Cx, Cy, Cz;
+    permute(r, __fsub_rn(v0.x, r.ox), __fsub_rn(v0.y, r.oy), __fsub_rn(v0.z, r.oz), Ax, Ay, Az);
+    permute(r, __fsub_rn(v1.x, r.ox), __fsub_rn(v1.y, r.oy), __fsub_rn(v1.z, r.oz), Bx, By, Bz);
+    permute(r, __fsub_rn(v2.x, r.ox), __fsub_rn(v2.y, r.oy), __fsub_rn(v2.z, r.oz), Cx, Cy, Cz);
+    const float ax = __fmaf_rn(r.nSx, Az, Ax), ay = __fmaf_rn(r.nSy, Az, Ay);
+    const float bx = __fmaf_rn(r.nSx, Bz, Bx), by = __fmaf_rn(r.nSy, Bz, By);
+    const float cx = __fmaf_rn(r.nSx, Cz, Cx), cy = __fmaf_rn(r.nSy, Cz, Cy);
+    float U = __fsub_rn(__fmul_rn(cx, by), __fmul_rn(cy, bx));
+    float V = __fsub_rn(__fmul_rn(ax, cy), __fmul_rn(ay, cx));
+    float W = __fsub_rn(__fmul_rn(bx, ay), __fmul_rn(by, ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = edge_fallback(cx, by, cy, bx);
+        V = edge_fallback(ax, cy, ay, cx);
+        W = edge_fallback(bx, ay, by, ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float az = __fmul_rn(r.Sz, Az), bz = __fmul_rn(r.Sz, Bz), cz = __fmul_rn(r.Sz, Cz);
+    const float T = __fmaf_rn(W, cz, __fmaf_rn(V, bz, __fmul_rn(U, az)));
+    const float t = __fdiv_rn(T, det);
+    if (!(t >= r.tmin && t <= tmax)) return false;
+    t_out = t;
+    if (kBary) {
+        bary[0] = U;
+        bary[1] = V;
+        bary[2] = W;
+        bary[3] = det;
+    }
+    return true;
+}
+
+// uint8 -> float without I2F: byte into the mantissa of 2^23, subtract 2^23.
+__device__ __forceinline__ float byte_to_float(uint32_t word, uint32_t sel) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | sel)) - 8388608.0f;
+}
+
+// Tests the 8 child boxes of one compressed node against the ray.
+// Returns the hit mask of internal children in traversal order (bit i is
+// slot i ^ oct) in bits 0..7 with the node's imask in bits 8..15, and the
+// triangle mask (bit k: triangle tri_base + k) of the hit leaf children.
+struct NodeHits {
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint32_t group;  // imask << 8 | ordered internal hits
+    uint32_t tris;
+};
+
+__device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint4* __restrict__ nodes, uint32_t idx,
+                                                   float tfar) {
+    const uint4* n = nodes + 5 * (size_t)idx;
+    const uint4 w0 = __ldg(n + 0);
+    const uint4 w1 = __ldg(n + 1);
+    const uint4 w2 = __ldg(n + 2);
+    const uint4 w3 = __ldg(n + 3);
+    const uint4 w4 = __ldg(n + 4);
+    const float sx = __uint_as_float((w0.w & 0xFFu) << 23) * r.ix;
+    const float sy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * r.iy;
+    const float sz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23) * r.iz;
+    const float bx = (__uint_as_float(w0.x) - r.ox) * r.ix;
+    const float by = (__uint_as_float(w0.y) - r.oy) * r.iy;
+    const float bz = (__uint_as_float(w0.z) - r.oz) * r.iz;
+    const uint32_t imask = w0.w >> 24;
+    // near / far plane words per axis, chosen by the direction signs
+    const bool fx = r.oct & 1u, fy = r.oct & 2u, fz = r.oct & 4u;
+    const uint32_t nx0 = fx ? w3.z : w2.x, nx1 = fx ? w3.w : w2.y;
+    const uint32_t gx0 = fx ? w2.x : w3.z, gx1 = fx ? w2.y : w3.w;
+    const uint32_t ny0 = fy ? w4.x : w2.z, ny1 = fy ? w4.y : w2.w;
+    const uint32_t gy0 = fy ? w2.z : w4.x, gy1 = fy ? w2.w : w4.y;
+    const uint32_t nz0 = fz ? w4.z : w3.x, nz1 = fz ? w4.w : w3.y;
+    const uint32_t gz0 = fz ? w3.x : w4.z, gz1 = fz ? w3.y : w4.w;
+    uint32_t hits = 0, tris = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t sel = (uint32_t)(s & 3);
+        const uint32_t meta = __byte_perm(s < 4 ? w1.z : w1.w, 0u, 0x4440u | sel);
+        const float tnx = __fmaf_rn(byte_to_float(s < 4 ? nx0 : nx1, sel), sx, bx);
+        const float tny = __fmaf_rn(byte_to_float(s < 4 ? ny0 : ny1, sel), sy, by);
+        const float tnz = __fmaf_rn(byte_to_float(s < 4 ? nz0 : nz1, sel), sz, bz);
+        const float tfx = __fmaf_rn(byte_to_float(s < 4 ? gx0 : gx1, sel), sx, bx);
+        const float tfy = __fmaf_rn(byte_to_float(s < 4 ? gy0 : gy1, sel), sy, by);
+        const float tfz = __fmaf_rn(byte_to_float(s < 4 ? gz0 : gz1, sel), sz, bz);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tfar));
+        if (meta != 0u && tn <= tf) {
+            if (imask & (1u << s)) {
+                hits |= 1u << ((uint32_t)s ^ r.oct);
+            } else {
+                const uint32_t cnt = ((meta >> 5) & 3u) + 1u;
+                tris |= ((1u << cnt) - 1u) << (meta & 31u);
+            }
+        }
+    }
+    NodeHits out;
+    out.child_base = w1.x;
+    out.tri_base = w1.y;
+    out.group = (imask << 8) | hits;
+    out.tris = tris;
+    return out;
+}
+
+}  // namespace RT
+}  // namespace Foundation

@@ -1,0 +1,256 @@
+"""ctypes binding of the C ABI in include/fnd_rt.h.
+
+This is the Python face of the path-tracer pass: a ``Context`` (one CUDA
+stream on one device, the counterpart of ``Renderer::Renderer(device,
+allocator)`` in src/Renderer/Renderer.hpp:41) owns ``Scene`` objects (BVH +
+triangles in device memory) and traces ray batches. Errors come back as
+``FndError`` carrying the library status code and message; there is no CPU
+fallback: if the native library is missing, importing this module's entry
+points raises.
+
+Buffers: numpy arrays are host memory (the library copies in and out and
+synchronises); objects exposing ``data_ptr()`` and ``is_cuda`` (torch CUDA
+tensors) are passed as device pointers and the call only enqueues work on
+the context stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+LIB_PATH = _build.LIB_PATH
+
+FND_OK = 0
+STATUS_NAMES = {
+    -1: "FND_ERR_INVALID_ARG", -2: "FND_ERR_OUT_OF_MEMORY", -3: "FND_ERR_CUDA", -4: "FND_ERR_NO_DEVICE",
+    -5: "FND_ERR_INVALID_SCENE", -6: "FND_ERR_STACK_OVERFLOW", -7: "FND_ERR_TIMEOUT", -8: "FND_ERR_UNSUPPORTED",
+    -9: "FND_ERR_IO",
+}
+FND_MEM_HOST, FND_MEM_DEVICE = 0, 1
+ABI_VERSION = 1
+INVALID_ID = 0xFFFFFFFF
+
+HIT_DTYPE = np.dtype([("prim", np.uint32), ("t", np.float32)])
+
+
+class FndError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Desc(C.Structure):
+    _fields_ = [("abi_version", C.c_uint32), ("device", C.c_int32), ("stream", C.c_void_p), ("flags", C.c_uint32)]
+
+
+class _BvhDesc(C.Structure):
+    _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("build_threads", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_tris", C.c_uint32), ("num_binary_nodes", C.c_uint32), ("num_wide_nodes", C.c_uint32),
+                ("binary_depth", C.c_uint32), ("wide_depth", C.c_uint32), ("num_leaves", C.c_uint32),
+                ("node_bytes", C.c_uint64), ("tri_bytes", C.c_uint64), ("sah_cost", C.c_double),
+                ("build_ms", C.c_double), ("collapse_ms", C.c_double), ("upload_ms", C.c_double),
+                ("bounds_lo", C.c_float * 3), ("bounds_hi", C.c_float * 3), ("box_margin", C.c_float)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["bounds_lo"] = list(self.bounds_lo)
+        d["bounds_hi"] = list(self.bounds_hi)
+        return d
+
+
+class TraceStats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("node_fetches", C.c_uint64), ("tri_tests", C.c_uint64)]
+
+
+# every symbol include/fnd_rt.h declares, with (restype, argtypes)
+_P, _U32, _I32, _SZ = C.c_void_p, C.c_uint32, C.c_int, C.c_size_t
+SIGNATURES = {
+    "fnd_rt_create": (_I32, [_P, _P]),
+    "fnd_rt_destroy": (_I32, [_P]),
+    "fnd_rt_last_error": (C.c_char_p, [_P]),
+    "fnd_rt_sync": (_I32, [_P]),
+    "fnd_rt_stream": (_P, [_P]),
+    "fnd_rt_host_alloc": (_I32, [_SZ, _P]),
+    "fnd_rt_host_free": (_I32, [_P]),
+    "fnd_rt_scene_upload": (_I32, [_P, _P, _U32, _P, _U32, _P, _P]),
+    "fnd_rt_scene_info_get": (_I32, [_P, _P]),
+    "fnd_rt_scene_destroy": (_I32, [_P]),
+    "fnd_rt_trace_closest": (_I32, [_P, _P, _P, _U32, _P, _I32]),
+    "fnd_rt_trace_any": (_I32, [_P, _P, _P, _U32, _P, _I32]),
+    "fnd_rt_trace_closest_stats": (_I32, [_P, _P, _P, _U32, _P, _I32, _P]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads libfnd_rt.so (built by foundation_gb300._build.build())."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FndError(-8, f"native library not built: {p} (run __graft_entry__.build())")
+    L = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def _check(rc: int, ctx=None):
+    if rc != FND_OK:
+        msg = load().fnd_rt_last_error(ctx)
+        raise FndError(rc, msg.decode() if msg else "")
+
+
+def _is_device(a) -> bool:
+    return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
+
+
+def _ptr(a):
+    if _is_device(a):
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One device + one CUDA stream (``stream``: an int cudaStream_t handle, or
+    None for a private non-blocking stream)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._h = None
+        d = _Desc(ABI_VERSION, device, C.c_void_p(stream) if stream else None, 0)
+        h = C.c_void_p()
+        _check(load().fnd_rt_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return int(load().fnd_rt_stream(self._h) or 0)
+
+    def sync(self):
+        _check(load().fnd_rt_sync(self._h), self._h)
+
+    def close(self):
+        if self._h is not None:
+            _check(load().fnd_rt_destroy(self._h))
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0) -> "Scene":
+        return Scene(self, verts, idx, bins, max_leaf, threads)
+
+
+class Scene:
+    def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0):
+        self._h = None
+        self.ctx = ctx
+        v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+        f = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
+        bd = _BvhDesc(bins, max_leaf, threads, 0)
+        h = C.c_void_p()
+        _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),
+               ctx.handle)
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        out = SceneInfo()
+        _check(load().fnd_rt_scene_info_get(self._h, C.byref(out)))
+        return out.as_dict()
+
+    def close(self):
+        if self._h is not None:
+            _check(load().fnd_rt_scene_destroy(self._h), self.ctx.handle)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _trace(self, rays, out, any_hit: bool, stats: bool = False):
+        dev = _is_device(rays)
+        if dev != _is_device(out):
+            raise FndError(-1, "rays and output must both be host or both be device buffers")
+        n = (rays.numel() * rays.element_size() if dev else rays.nbytes) // 32
+        mem = FND_MEM_DEVICE if dev else FND_MEM_HOST
+        L = load()
+        if stats:
+            st = TraceStats()
+            _check(L.fnd_rt_trace_closest_stats(self.ctx.handle, self._h, _ptr(rays), n, _ptr(out), mem,
+                                                C.byref(st)), self.ctx.handle)
+            return dict(rays=st.rays, node_fetches=st.node_fetches, tri_tests=st.tri_tests)
+        fn = L.fnd_rt_trace_any if any_hit else L.fnd_rt_trace_closest
+        _check(fn(self.ctx.handle, self._h, _ptr(rays), n, _ptr(out), mem), self.ctx.handle)
+        return None
+
+    def closest(self, rays, out=None, stats: bool = False):
+        """Closest hit. Host: rays (n, 8) float32 -> structured (prim, t)
+        array. Device: rays / out are CUDA tensors (out: n*2 int32/float32
+        words); asynchronous on the context stream."""
+        if _is_device(rays):
+            if out is None:
+                raise FndError(-1, "device call needs an output tensor")
+            st = self._trace(rays, out, False, stats)
+            return st if stats else out
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        out = np.empty(len(rays), HIT_DTYPE) if out is None else out
+        st = self._trace(rays, out, False, stats)
+        return (out, st) if stats else out
+
+    def any(self, rays, out=None):
+        if _is_device(rays):
+            if out is None:
+                raise FndError(-1, "device call needs an output tensor")
+            self._trace(rays, out, True)
+            return out
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        out = np.empty(len(rays), np.uint8) if out is None else out
+        self._trace(rays, out, True)
+        return out
+
+
+class PinnedBuffer:
+    """Page-locked host memory from fnd_rt_host_alloc, viewed as numpy."""
+
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        _check(load().fnd_rt_host_alloc(nbytes, C.byref(p)))
+        self._p = p
+        self.nbytes = nbytes
+
+    def view(self, dtype, shape):
+        buf = (C.c_char * self.nbytes).from_address(self._p.value)
+        return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def __del__(self):
+        if getattr(self, "_p", None):
+            load().fnd_rt_host_free(self._p)
+            self._p = None

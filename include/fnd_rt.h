@@ -1,0 +1,188 @@
+/*
+ * fnd_rt.h — C ABI of the Foundation path-tracer pass (GB300 / sm_103a).
+ *
+ * The reference renderer (mos9527/Foundation) exposes one monolithic raster
+ * pass: `Foundation::Renderer::Renderer(device, allocator)` with a per-frame
+ * `Draw()` (src/Renderer/Renderer.hpp:39-43, src/Renderer/Renderer.cpp:367-401),
+ * CHECK/BugCheck error handling (src/Core/Core.hpp:17, src/Core/Core.cpp:7-10)
+ * and owner-scoped RAII handles (src/Platform/RHI/Details/Details.hpp:76-121).
+ * It has no ray-tracing code at all, so every entry point below has no
+ * line-for-line counterpart; each one names the reference interface whose
+ * role it takes over in the new path-tracer pass.
+ *
+ * Conventions (all entry points):
+ *  - return FND_OK (0) on success, a negative fnd_status on failure; no C++
+ *    exception crosses this boundary and nothing terminates the process;
+ *  - fnd_rt_last_error(ctx) gives a human-readable message for the last
+ *    failure on that context;
+ *  - input and output buffers are owned by the caller; device memory that the
+ *    library allocates is owned by the context / scene and freed by destroy;
+ *  - one CUDA stream per context; a context is not thread-safe, separate
+ *    contexts may be used from separate threads;
+ *  - device-side failures (traversal stack overflow, queue timeout) are
+ *    latched in a device status word and returned by the next synchronising
+ *    call (fnd_rt_sync, or any call made with FND_MEM_HOST buffers).
+ */
+#ifndef FND_RT_H
+#define FND_RT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FND_RT_ABI_VERSION 1u
+#define FND_INVALID_ID 0xFFFFFFFFu
+
+typedef enum fnd_status {
+    FND_OK = 0,
+    FND_ERR_INVALID_ARG = -1,    /* null pointer, bad size, bad flag, non-finite vertex */
+    FND_ERR_OUT_OF_MEMORY = -2,  /* host or device allocation failed */
+    FND_ERR_CUDA = -3,           /* a CUDA runtime call failed (message has the CUDA error) */
+    FND_ERR_NO_DEVICE = -4,      /* no CUDA device / bad ordinal / not an sm_103 part */
+    FND_ERR_INVALID_SCENE = -5,  /* scene too large for the node format, or depth over the stack */
+    FND_ERR_STACK_OVERFLOW = -6, /* a ray needed more traversal stack than provisioned */
+    FND_ERR_TIMEOUT = -7,        /* a bounded device wait ran out of iterations */
+    FND_ERR_UNSUPPORTED = -8,    /* feature not available in this build */
+    FND_ERR_IO = -9              /* file read / write failed */
+} fnd_status;
+
+/* Where the ray / hit buffers of a trace call live. */
+enum { FND_MEM_HOST = 0, FND_MEM_DEVICE = 1 };
+
+/* One ray: origin, [tmin, tmax] interval, direction (need not be unit).
+ * 32 bytes, two 16-byte halves so a thread loads it with two vector loads. */
+typedef struct fnd_ray {
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} fnd_ray;
+
+/* Closest-hit result: original triangle index (FND_INVALID_ID on a miss) and
+ * the hit distance in units of |dir| (+inf on a miss). 8 bytes. */
+typedef struct fnd_hit {
+    uint32_t prim;
+    float t;
+} fnd_hit;
+
+typedef struct fnd_rt_ctx fnd_rt_ctx;
+typedef struct fnd_rt_scene fnd_rt_scene;
+
+/* Replaces the (device, allocator) pair handed to Renderer::Renderer
+ * (src/Renderer/Renderer.hpp:41). */
+typedef struct fnd_rt_desc {
+    uint32_t abi_version; /* must be FND_RT_ABI_VERSION */
+    int32_t device;       /* CUDA device ordinal */
+    void* stream;         /* cudaStream_t to launch on; NULL: the context creates its own */
+    uint32_t flags;       /* reserved, 0 */
+} fnd_rt_desc;
+
+/* BVH build parameters. The builder is binned SAH over triangle bounding-box
+ * centroids, then a collapse of the binary tree into 8-wide compressed nodes. */
+typedef struct fnd_rt_bvh_desc {
+    uint32_t sah_bins;      /* 2..64, default 32 */
+    uint32_t max_leaf_tris; /* 1..4, default 4 */
+    uint32_t build_threads; /* 0: all host cores */
+    uint32_t flags;         /* reserved, 0 */
+} fnd_rt_bvh_desc;
+
+typedef struct fnd_rt_scene_info {
+    uint32_t num_tris;
+    uint32_t num_binary_nodes;
+    uint32_t num_wide_nodes;
+    uint32_t binary_depth;
+    uint32_t wide_depth;
+    uint32_t num_leaves;
+    uint64_t node_bytes; /* device bytes of the wide nodes */
+    uint64_t tri_bytes;  /* device bytes of the triangle arrays */
+    double sah_cost;     /* SAH cost of the binary tree (C_trav = C_isect = 1) */
+    double build_ms;     /* binary binned-SAH build, host */
+    double collapse_ms;  /* collapse + compression + triangle re-layout, host */
+    double upload_ms;    /* host -> device copies */
+    float bounds_lo[3];
+    float bounds_hi[3];
+    float box_margin; /* absolute outward inflation applied to every node box */
+} fnd_rt_scene_info;
+
+/* ---- context --------------------------------------------------------- */
+
+/* Creates a context on desc->device. Allocates the device status word and the
+ * work-queue counters. Counterpart of Renderer::Renderer
+ * (src/Renderer/Renderer.cpp:34-311). */
+int fnd_rt_create(const fnd_rt_desc* desc, fnd_rt_ctx** out_ctx);
+
+/* Waits for the context's stream, frees everything it owns (scenes must be
+ * destroyed first). Counterpart of Renderer::~Renderer
+ * (src/Renderer/Renderer.cpp:402-406), which waits for its queue to idle. */
+int fnd_rt_destroy(fnd_rt_ctx* ctx);
+
+/* Message of the last failure on ctx ("" if none); valid until the next call
+ * on ctx. ctx may be NULL for failures of fnd_rt_create. */
+const char* fnd_rt_last_error(const fnd_rt_ctx* ctx);
+
+/* Waits for the context's stream and returns the device status: FND_OK, or
+ * the first latched device error (which is then cleared). */
+int fnd_rt_sync(fnd_rt_ctx* ctx);
+
+/* The cudaStream_t the context launches on. */
+void* fnd_rt_stream(const fnd_rt_ctx* ctx);
+
+/* Page-locked host buffers for FND_MEM_HOST calls (copies from pinned memory
+ * run at full link speed). Counterpart of the host-visible staging buffers
+ * the reference maps with MapSpan (src/Platform/RHI/Resource.hpp:62-68). */
+int fnd_rt_host_alloc(size_t bytes, void** out_ptr);
+int fnd_rt_host_free(void* ptr);
+
+/* ---- scenes ----------------------------------------------------------- */
+
+/* Builds the BVH on the host and uploads nodes and triangles.
+ * verts: nv * 3 floats (x, y, z); idx: nt * 3 vertex indices (host memory).
+ * Non-finite vertex coordinates or out-of-range indices are rejected with
+ * FND_ERR_INVALID_ARG; nt == 0 gives an empty scene every ray misses.
+ * Counterpart of the staging uploads of vertex / index buffers in the
+ * reference renderer (src/Renderer/Renderer.cpp:133-198). */
+int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const uint32_t* idx,
+                        uint32_t nt, const fnd_rt_bvh_desc* bvh, fnd_rt_scene** out_scene);
+
+int fnd_rt_scene_info_get(const fnd_rt_scene* scene, fnd_rt_scene_info* out_info);
+
+int fnd_rt_scene_destroy(fnd_rt_scene* scene);
+
+/* ---- traversal -------------------------------------------------------- */
+
+/* Closest hit for n rays: for each ray the triangle with the smallest hit t
+ * in [tmin, tmax], ties broken by the lowest triangle index; t is computed by
+ * the watertight ray/triangle test in FP32.
+ * mem = FND_MEM_DEVICE: rays / out are device pointers, the call only enqueues
+ * work on the context stream (call fnd_rt_sync to wait and read the status);
+ * mem = FND_MEM_HOST: host pointers (pinned or pageable), the call copies in,
+ * traces, copies out and synchronises. */
+int fnd_rt_trace_closest(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n,
+                         fnd_hit* out, int mem);
+
+/* Any hit (occlusion) for n rays: out[i] = 1 if some triangle is hit with t in
+ * [tmin, tmax], else 0. Same memory rules as fnd_rt_trace_closest. */
+int fnd_rt_trace_any(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n,
+                     uint8_t* out, int mem);
+
+/* Traversal counters of the last trace call (device-side totals), for the
+ * memory-roofline accounting: wide nodes fetched and triangles tested. */
+typedef struct fnd_rt_trace_stats {
+    uint64_t rays;
+    uint64_t node_fetches;
+    uint64_t tri_tests;
+} fnd_rt_trace_stats;
+
+/* Re-runs a closest-hit trace with per-ray counters enabled (slower variant of
+ * the kernel) and returns the totals. Same memory rules as trace_closest. */
+int fnd_rt_trace_closest_stats(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays,
+                               uint32_t n, fnd_hit* out, int mem, fnd_rt_trace_stats* stats);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* FND_RT_H */

@@ -1,0 +1,154 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes front end of the scalar CPU oracle.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg,
+always as the checker or the timed CPU baseline, never as a product path.
+Parity against the reference is unpinned: mos9527/Foundation contains no
+ray-tracing code (its only pass is a raster draw, src/Renderer/Renderer.cpp
+:312-366). The oracle restates published methods (binned SAH, Wald 2007;
+watertight intersection, Woop/Benthin/Wald 2013; PCG32, O'Neill 2014) and is
+pinned by hand-derived known-answer tests and brute-force cross-checks.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "librt_oracle.so")
+SOURCES = ["rt_oracle.cpp"]
+HEADERS = ["rt_oracle.h", "oracle_common.hpp"]
+CXXFLAGS = ["-O3", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared", "-pthread"]
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (portable flags, no FMA contraction)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    deps = srcs + [os.path.join(HERE, h) for h in HEADERS]
+    if not force and os.path.exists(LIB_PATH):
+        t = os.path.getmtime(LIB_PATH)
+        if all(os.path.getmtime(d) <= t for d in deps):
+            return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["g++", *CXXFLAGS, "-o", tmp, *srcs])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        P, U32, U64, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float
+        L.orc_bvh_build.restype = P
+        L.orc_bvh_build.argtypes = [P, U32, P, U32, U32, U32]
+        L.orc_bvh_free.argtypes = [P]
+        L.orc_bvh_stats.argtypes = [P, P, P]
+        L.orc_bvh_validate.argtypes = [P]
+        L.orc_bvh_validate.restype = C.c_int
+        L.orc_bvh_margin.argtypes = [P]
+        L.orc_bvh_margin.restype = F
+        L.orc_trace_closest.argtypes = [P, P, U64, P, U32, P]
+        L.orc_trace_any.argtypes = [P, P, U64, P, U32, P]
+        L.orc_brute_closest.argtypes = [P, U32, P, U32, P, U64, P, U32]
+        L.orc_brute_any.argtypes = [P, U32, P, U32, P, U64, P, U32]
+        L.orc_intersect1.argtypes = [P, P, P]
+        L.orc_intersect1.restype = C.c_int
+        L.orc_pcg32_fill.argtypes = [U64, U64, P, U64]
+        L.orc_time_build_ms.argtypes = [P, U32, P, U32, U32, U32]
+        L.orc_time_build_ms.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+HIT_DTYPE = np.dtype([("prim", np.uint32), ("t", np.float32)])
+
+
+class OracleBVH:
+    """Binary binned-SAH BVH of the oracle (32 bins, <= 4 triangles/leaf)."""
+
+    def __init__(self, verts, idx, bins: int = 32, max_leaf: int = 4):
+        self.verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+        self.idx = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
+        self._h = lib().orc_bvh_build(_ptr(self.verts), len(self.verts), _ptr(self.idx), len(self.idx), bins,
+                                      max_leaf)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_bvh_free(self._h)
+            self._h = None
+
+    def stats(self) -> dict:
+        out = np.zeros(4, np.uint64)
+        sah = C.c_double()
+        lib().orc_bvh_stats(self._h, _ptr(out), C.byref(sah))
+        return dict(nodes=int(out[0]), leaves=int(out[1]), depth=int(out[2]), max_leaf=int(out[3]),
+                    sah=sah.value, margin=float(lib().orc_bvh_margin(self._h)))
+
+    def validate(self) -> int:
+        return int(lib().orc_bvh_validate(self._h))
+
+    def closest(self, rays, threads: int = 0, with_stats: bool = False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        hits = np.empty(len(rays), HIT_DTYPE)
+        st = np.zeros(2, np.uint64)
+        lib().orc_trace_closest(self._h, _ptr(rays), len(rays), _ptr(hits), threads, _ptr(st))
+        return (hits, dict(node_fetches=int(st[0]), tri_tests=int(st[1]))) if with_stats else hits
+
+    def any(self, rays, threads: int = 0, with_stats: bool = False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        out = np.empty(len(rays), np.uint8)
+        st = np.zeros(2, np.uint64)
+        lib().orc_trace_any(self._h, _ptr(rays), len(rays), _ptr(out), threads, _ptr(st))
+        return (out, dict(node_fetches=int(st[0]), tri_tests=int(st[1]))) if with_stats else out
+
+
+def brute_closest(verts, idx, rays, threads: int = 0):
+    verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
+    rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+    hits = np.empty(len(rays), HIT_DTYPE)
+    lib().orc_brute_closest(_ptr(verts), len(verts), _ptr(idx), len(idx), _ptr(rays), len(rays), _ptr(hits),
+                            threads)
+    return hits
+
+
+def brute_any(verts, idx, rays, threads: int = 0):
+    verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
+    rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+    out = np.empty(len(rays), np.uint8)
+    lib().orc_brute_any(_ptr(verts), len(verts), _ptr(idx), len(idx), _ptr(rays), len(rays), _ptr(out), threads)
+    return out
+
+
+def intersect1(ray, tri):
+    """One ray (8 floats) vs one triangle (9 floats) -> (hit, t, U, V, W, det)."""
+    r = np.ascontiguousarray(ray, dtype=np.float32).reshape(8)
+    v = np.ascontiguousarray(tri, dtype=np.float32).reshape(9)
+    out = np.zeros(5, np.float32)
+    h = lib().orc_intersect1(_ptr(r), _ptr(v), _ptr(out))
+    return bool(h), float(out[0]), out[1:].copy()
+
+
+def pcg32(seed: int, seq: int, n: int) -> np.ndarray:
+    out = np.empty(n, np.uint32)
+    lib().orc_pcg32_fill(seed, seq, _ptr(out), n)
+    return out
+
+
+def time_build_ms(verts, idx, bins: int = 32, max_leaf: int = 4) -> float:
+    verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
+    return float(lib().orc_time_build_ms(_ptr(verts), len(verts), _ptr(idx), len(idx), bins, max_leaf))

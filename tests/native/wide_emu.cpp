@@ -1,0 +1,154 @@
+// wide_emu.cpp — TEST HARNESS: host emulation of the per-ray traversal logic
+// of foundation_gb300/csrc/rt/traverse.cu, used by the CPU test suite to
+// validate the product's BVH builder, wide-node collapse / quantisation and
+// node + triangle tests without a GPU. It compiles the product's own
+// traverse.cuh with g++ by supplying host definitions of the CUDA intrinsics
+// it uses (round-to-nearest IEEE ops, byte_perm, bit casts), so the numbers
+// are the ones the device computes. Not part of the product library.
+#include <cuda_runtime.h>
+
+#include <bit>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+static inline float __fsub_rn(float a, float b) { return a - b; }
+static inline float __fadd_rn(float a, float b) { return a + b; }
+static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __fdiv_rn(float a, float b) { return a / b; }
+static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
+static inline double __dmul_rn(double a, double b) { return a * b; }
+static inline double __dsub_rn(double a, double b) { return a - b; }
+static inline float __double2float_rn(double d) { return (float)d; }
+static inline float __uint_as_float(uint32_t u) { return std::bit_cast<float>(u); }
+static inline uint32_t __float_as_uint(float f) { return std::bit_cast<uint32_t>(f); }
+static inline uint32_t __byte_perm(uint32_t x, uint32_t y, uint32_t s) {
+    const uint64_t v = ((uint64_t)y << 32) | x;
+    uint32_t r = 0;
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t sel = (s >> (4 * i)) & 7u;
+        r |= (uint32_t)((v >> (8 * sel)) & 0xFFu) << (8 * i);
+    }
+    return r;
+}
+template <typename T>
+static inline T __ldg(const T* p) {
+    return *p;
+}
+using std::copysignf;
+
+using std::signbit;
+
+#include "../../include/fnd_rt.h"
+#include "../../foundation_gb300/csrc/bvh/bvh_build.hpp"
+#include "../../foundation_gb300/csrc/bvh/collapse.hpp"
+#include "../../foundation_gb300/csrc/rt/traverse.cuh"
+
+using namespace Foundation::RT;
+
+struct emu_bvh {
+    BinaryBvh bin;
+    WideBvh wide;
+    DeviceScene view{};
+};
+
+extern "C" {
+
+emu_bvh* emu_build(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads) {
+    auto* e = new emu_bvh();
+    std::vector<float> tri(9 * (size_t)nt);
+    for (uint32_t t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) tri[9 * (size_t)t + 3 * k + c] = verts[3 * (size_t)idx[3 * (size_t)t + k] + c];
+    BuildParams p;
+    p.threads = threads;
+    BuildBinaryBvh(tri.data(), nt, p, e->bin);
+    CollapseToWide(e->bin, tri.data(), nt, e->wide);
+    e->view.nodes = reinterpret_cast<const uint4*>(e->wide.nodes.data());
+    e->view.v0 = reinterpret_cast<const float4*>(e->wide.v0.data());
+    e->view.v1 = reinterpret_cast<const float4*>(e->wide.v1.data());
+    e->view.v2 = reinterpret_cast<const float4*>(e->wide.v2.data());
+    e->view.num_nodes = (uint32_t)e->wide.nodes.size();
+    e->view.num_tris = nt;
+    (void)nv;
+    return e;
+}
+
+void emu_free(emu_bvh* e) { delete e; }
+
+// out: binary nodes, leaves, binary depth, wide nodes, wide depth, wide leaves
+void emu_stats(const emu_bvh* e, uint64_t* out, double* sah, float* margin) {
+    out[0] = e->bin.nodes.size();
+    out[1] = e->bin.leaves;
+    out[2] = e->bin.depth;
+    out[3] = e->wide.nodes.size();
+    out[4] = e->wide.depth;
+    out[5] = e->wide.leaves;
+    *sah = e->bin.sah_cost;
+    *margin = e->wide.margin;
+}
+
+// Per-ray restatement of trace_kernel's lane logic (same group / stack
+// semantics, same node and triangle tests). max_sp receives the deepest stack.
+void emu_trace(const emu_bvh* e, const float* rays, uint64_t n, uint32_t* hits, int any, uint64_t* stats) {
+    uint64_t nodes = 0, tris = 0, max_sp = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* rp = rays + 8 * i;
+        const float4 r0{rp[0], rp[1], rp[2], rp[3]}, r1{rp[4], rp[5], rp[6], rp[7]};
+        const RayState r = setup_ray(r0, r1);
+        float best_t = r.tmax;
+        uint32_t best_p = FND_INVALID_ID;
+        uint32_t ng_base = 0, ng_group = (1u << 8) | (1u << r.oct), tg_base = 0, tg_mask = 0;
+        std::vector<uint2> stack;
+        for (;;) {
+            if (ng_group & 0xFFu) {
+                const uint32_t b = (uint32_t)__builtin_ctz(ng_group & 0xFFu);
+                ng_group &= ~(1u << b);
+                const uint32_t slot = b ^ r.oct;
+                const uint32_t child = ng_base + (uint32_t)__builtin_popcount((ng_group >> 8) & ((1u << slot) - 1u));
+                if (ng_group & 0xFFu) stack.push_back(uint2{ng_base, ng_group});
+                max_sp = std::max<uint64_t>(max_sp, stack.size());
+                const NodeHits h = intersect_node(r, e->view.nodes, child, best_t);
+                nodes++;
+                ng_base = h.child_base;
+                ng_group = h.group;
+                tg_base = h.tri_base;
+                tg_mask = h.tris;
+            }
+            while (tg_mask) {
+                const uint32_t k = (uint32_t)__builtin_ctz(tg_mask);
+                tg_mask &= tg_mask - 1u;
+                const uint32_t ti = tg_base + k;
+                tris++;
+                float t;
+                if (intersect_tri(r, e->view.v0[ti], e->view.v1[ti], e->view.v2[ti], best_t, t)) {
+                    const uint32_t pid = __float_as_uint(e->view.v0[ti].w);
+                    if (any) {
+                        best_t = t;
+                        best_p = pid;
+                        tg_mask = 0;
+                        ng_group = 0;
+                        stack.clear();
+                    } else if (best_p == FND_INVALID_ID || t < best_t || (t == best_t && pid < best_p)) {
+                        best_t = t;
+                        best_p = pid;
+                    }
+                }
+            }
+            if (ng_group & 0xFFu) continue;
+            if (stack.empty()) break;
+            const uint2 g = stack.back();
+            stack.pop_back();
+            ng_base = g.x;
+            ng_group = g.y;
+        }
+        hits[2 * i] = best_p;
+        hits[2 * i + 1] = best_p == FND_INVALID_ID ? 0x7F800000u : __float_as_uint(best_t);
+    }
+    stats[0] = nodes;
+    stats[1] = tris;
+    stats[2] = max_sp;
+}
+
+}  // extern "C"

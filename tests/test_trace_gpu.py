@@ -1,0 +1,134 @@
+"""GPU parity of closest-hit / any-hit traversal through the C ABI against
+the CPU oracle: triangle ids exact, t bit-identical (the kernel evaluates the
+oracle's FP32 expression tree), occlusion flags exact."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from foundation_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def ctx(built):
+    import foundation_gb300 as fg
+    c = fg.Context(0)
+    yield c
+    c.close()
+
+
+def assert_same(h, ref):
+    bad = np.nonzero(h["prim"] != ref["prim"])[0]
+    assert len(bad) == 0, f"{len(bad)} id mismatches, first {bad[:5]}: {h['prim'][bad[:5]]} vs {ref['prim'][bad[:5]]}"
+    assert np.array_equal(h["t"].view(np.uint32), ref["t"].view(np.uint32))
+
+
+def test_golden_soup(ctx):
+    g = np.load(os.path.join(GOLDEN, "soup1k.npz"))
+    sc = ctx.upload(g["verts"], g["idx"])
+    h = sc.closest(g["rays"])
+    assert np.array_equal(h["prim"], g["prim"])
+    assert np.array_equal(h["t"].view(np.uint32), g["t"].view(np.uint32))
+    assert np.array_equal(sc.any(g["rays"]), g["occluded"])
+    sc.close()
+
+
+def test_config1_full_frame(ctx):
+    """1024x1024 primary rays on the icosphere + random-triangle scene."""
+    c1 = S.config1_scene()
+    rays = S.camera_rays(1024, 1024)
+    sc = ctx.upload(c1.verts, c1.idx)
+    h = sc.closest(rays)
+    b = O.OracleBVH(c1.verts, c1.idx)
+    assert_same(h, b.closest(rays))
+    g = np.load(os.path.join(GOLDEN, "config1_rows.npz"))
+    assert np.array_equal(h["prim"][g["sel"]], g["prim"])
+    assert np.array_equal(sc.any(rays), b.any(rays))
+    sc.close()
+
+
+def test_cornell_incoherent_and_camera(ctx):
+    cs = S.cornell_scene()
+    sc = ctx.upload(cs.verts, cs.idx)
+    b = O.OracleBVH(cs.verts, cs.idx)
+    ir = S.incoherent_rays(1 << 20, *cs.bounds, seed=1)
+    assert_same(sc.closest(ir), b.closest(ir))
+    assert np.array_equal(sc.any(ir), b.any(ir))
+    cr = S.camera_rays(480, 270, **S.CORNELL_CAMERA)
+    assert_same(sc.closest(cr), b.closest(cr))
+    g = np.load(os.path.join(GOLDEN, "cornell_rows.npz"))
+    h = sc.closest(g["rays"])
+    assert np.array_equal(h["prim"], g["prim"])
+    sc.close()
+
+
+def test_soup_1m_tris(ctx):
+    so = S.soup_scene(1 << 20)
+    sc = ctx.upload(so.verts, so.idx)
+    rays = S.incoherent_rays(1 << 19, (0, 0, 0), (1, 1, 1), seed=2)
+    b = O.OracleBVH(so.verts, so.idx)
+    assert_same(sc.closest(rays), b.closest(rays))
+    sc.close()
+
+
+def test_device_pointers_and_stats(ctx):
+    import torch
+    cs = S.cornell_scene(num_spheres=50)
+    sc = ctx.upload(cs.verts, cs.idx)
+    rays = S.incoherent_rays(300000, *cs.bounds, seed=9)
+    rd = torch.from_numpy(rays).cuda()
+    out = torch.empty(2 * len(rays), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    sc.closest(rd, out)
+    ctx.sync()
+    h = out.cpu().numpy().view(np.uint32)
+    ref = O.OracleBVH(cs.verts, cs.idx).closest(rays)
+    assert np.array_equal(h[0::2], ref["prim"])
+    assert np.array_equal(h[1::2], ref["t"].view(np.uint32))
+    hh, st = sc.closest(rays, stats=True)
+    assert_same(hh, ref)
+    assert st["rays"] == len(rays) and st["node_fetches"] >= len(rays)
+    occ = torch.empty(len(rays), dtype=torch.uint8, device="cuda")
+    sc.any(rd, occ)
+    ctx.sync()
+    assert np.array_equal(occ.cpu().numpy(), O.OracleBVH(cs.verts, cs.idx).any(rays))
+    sc.close()
+
+
+def test_edge_cases(ctx):
+    import foundation_gb300 as fg
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [2, 2, 2]], np.float32)
+    f = np.array([[0, 1, 2], [0, 1, 2], [3, 3, 3], [0, 2, 1]], np.uint32)
+    rays = np.array([
+        [0.2, 0.2, 1, 0, 0, 0, -1, np.inf],
+        [0.2, 0.2, -1, 0, 0, 0, 1, np.inf],
+        [0.2, 0.2, 1, 0, 0, 0, -1, 0.5],
+        [0.5, 0.0, 1, 0, 0, 0, -1, np.inf],
+        [0.2, 0.2, 1, 0, 0, 0, 1, np.inf],
+        [50.2, 0.2, 1, 0, -1, 0, -0.02, np.inf],
+        [0.2, 0.2, 0, 0, 0, 0, 0, np.inf],
+    ], np.float32)
+    sc = ctx.upload(v, f)
+    h = sc.closest(rays)
+    assert_same(h, O.brute_closest(v, f, rays))
+    sc.close()
+    # empty scene: every ray misses; zero rays: no-op
+    e = ctx.upload(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+    he = e.closest(rays)
+    assert (he["prim"] == fg.INVALID_ID).all() and np.isinf(he["t"]).all()
+    assert (e.any(rays) == 0).all()
+    assert len(e.closest(np.zeros((0, 8), np.float32))) == 0
+    e.close()
+    # malformed scenes are rejected with a status, the context stays usable
+    with pytest.raises(fg.FndError) as ex:
+        ctx.upload(np.array([[np.nan, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.uint32))
+    assert ex.value.code == -1
+    with pytest.raises(fg.FndError):
+        ctx.upload(v, np.array([[0, 1, 9]], np.uint32))
+    ok = ctx.upload(v, f)
+    assert ok.closest(rays[:1])["prim"][0] == 0
+    ok.close()
