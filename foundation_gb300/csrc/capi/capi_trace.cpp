@@ -82,6 +82,7 @@ int ReadStatus(fnd_rt_ctx* ctx) {
     CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     if (s & RT::kStatusStackOverflow) return FND_ERR_STACK_OVERFLOW;
     if (s & RT::kStatusTimeout) return FND_ERR_TIMEOUT;
+    if (s & RT::kStatusBadIndex) return FND_ERR_INVALID_SCENE;
     return FND_ERR_CUDA;
 }
 
@@ -170,7 +171,9 @@ int fnd_rt_sync(fnd_rt_ctx* ctx) {
         status = ReadStatus(ctx);
         if (status != FND_OK)
             Fail(status, "device status: %s",
-                 status == FND_ERR_STACK_OVERFLOW ? "traversal stack overflow" : "bounded wait timed out");
+                 status == FND_ERR_STACK_OVERFLOW   ? "traversal stack overflow"
+                 : status == FND_ERR_INVALID_SCENE ? "scene index out of range"
+                                                    : "bounded wait timed out");
     });
     return rc;
 }
@@ -330,6 +333,8 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
         L.stats = ctx->d_stats;
         L.refill_min = ctx->refill_min;
         if (mem == FND_MEM_DEVICE) {
+            CHECK_CODE(((uintptr_t)rays & 15u) == 0 && ((uintptr_t)out & (any ? 0u : 7u)) == 0, FND_ERR_INVALID_ARG,
+                       "device rays must be 16-byte aligned and hits 8-byte aligned");
             L.rays = reinterpret_cast<const float4*>(rays);
             if (any)
                 L.occluded = static_cast<uint8_t*>(out);
@@ -360,7 +365,9 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
         if (mem == FND_MEM_HOST) {
             if (n) CUDA_CHECK(cudaMemcpyAsync(out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
             const int s = ReadStatus(ctx);
-            if (s != FND_OK) Fail(s, "device status: traversal stack overflow");
+            if (s != FND_OK)
+                Fail(s, "device status: %s",
+                     s == FND_ERR_STACK_OVERFLOW ? "traversal stack overflow" : "scene index out of range");
         }
     });
 }

@@ -11,6 +11,7 @@ namespace RT {
 // Device status bits (latched, read back by fnd_rt_sync).
 constexpr uint32_t kStatusStackOverflow = 1u;
 constexpr uint32_t kStatusTimeout = 2u;
+constexpr uint32_t kStatusBadIndex = 4u;  // node / triangle index outside the scene arrays
 
 constexpr int kMaxStack = 64;  // node-group + triangle-group entries per ray
 

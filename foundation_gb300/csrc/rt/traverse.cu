@@ -95,12 +95,26 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
                     sp++;
                 }
             }
-            const NodeHits h = intersect_node(r, L.scene.nodes, child, best_t);
-            if (kStats) st_nodes++;
-            ng_base = h.child_base;
-            ng_group = h.group;
-            tg_base = h.tri_base;
-            tg_mask = h.tris;
+            if (child < L.scene.num_nodes) {
+                const NodeHits h = intersect_node(r, L.scene.nodes, child, best_t);
+                if (kStats) st_nodes++;
+                ng_base = h.child_base;
+                ng_group = h.group;
+                tg_base = h.tri_base;
+                tg_mask = h.tris;
+                // a node's triangles must lie inside the triangle arrays
+                if (tg_mask && (uint64_t)tg_base + (uint64_t)(32 - __clz(tg_mask)) > L.scene.num_tris) {
+                    atomicOr(L.status, kStatusBadIndex);
+                    tg_mask = 0;
+                    ng_group = 0;
+                    sp = 0;
+                }
+            } else {
+                atomicOr(L.status, kStatusBadIndex);
+                ng_group = 0;
+                tg_mask = 0;
+                sp = 0;
+            }
         }
         // ---- its triangles ---------------------------------------------------
         while (tg_mask) {
