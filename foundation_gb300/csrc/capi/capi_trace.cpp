@@ -22,28 +22,6 @@ using Foundation::Core::FndError;
 
 namespace {
 
-thread_local std::string g_create_error;
-
-template <typename F>
-int Guard(fnd_rt_ctx* ctx, F&& body) {
-    std::string* err = ctx ? &ctx->last_error : &g_create_error;
-    try {
-        body();
-        err->clear();
-        return FND_OK;
-    } catch (const FndError& e) {
-        *err = e.what();
-        LOG_RUNTIME(FndRt, ERR, "%s", e.what());
-        return e.code();
-    } catch (const std::bad_alloc&) {
-        *err = "host allocation failed";
-        return FND_ERR_OUT_OF_MEMORY;
-    } catch (const std::exception& e) {
-        *err = e.what();
-        return FND_ERR_INVALID_ARG;
-    }
-}
-
 double MsSince(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -54,6 +32,11 @@ void UseDevice(const fnd_rt_ctx* ctx) { CUDA_CHECK(cudaSetDevice(ctx->device)); 
 
 namespace Foundation {
 namespace CApi {
+
+std::string& GlobalError() {
+    thread_local std::string msg;
+    return msg;
+}
 
 void CudaCheck(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return;
@@ -161,7 +144,7 @@ int fnd_rt_destroy(fnd_rt_ctx* ctx) {
     return rc;
 }
 
-const char* fnd_rt_last_error(const fnd_rt_ctx* ctx) { return ctx ? ctx->last_error.c_str() : g_create_error.c_str(); }
+const char* fnd_rt_last_error(const fnd_rt_ctx* ctx) { return ctx ? ctx->last_error.c_str() : GlobalError().c_str(); }
 
 int fnd_rt_sync(fnd_rt_ctx* ctx) {
     if (!ctx) return FND_ERR_INVALID_ARG;
@@ -401,7 +384,7 @@ int fnd_rt_host_alloc(size_t bytes, void** out_ptr) {
     *out_ptr = nullptr;
     const cudaError_t e = cudaMallocHost(out_ptr, bytes ? bytes : 1);
     if (e != cudaSuccess) {
-        g_create_error = cudaGetErrorString(e);
+        GlobalError() = cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? FND_ERR_OUT_OF_MEMORY : FND_ERR_CUDA;
     }
     return FND_OK;

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <new>
+#include <stdexcept>
 #include <string>
 
 #include "../../../include/fnd_rt.h"
@@ -41,6 +43,31 @@ struct fnd_rt_scene {
 
 namespace Foundation {
 namespace CApi {
+
+// Message slot for failures that have no context (fnd_rt_last_error(NULL)).
+std::string& GlobalError();
+
+// Runs an entry point body: C++ failures become a negative fnd_status and a
+// message in the context's (or the global) error slot.
+template <typename F>
+int Guard(fnd_rt_ctx* ctx, F&& body) {
+    std::string* err = ctx ? &ctx->last_error : &GlobalError();
+    try {
+        body();
+        err->clear();
+        return FND_OK;
+    } catch (const Foundation::Core::FndError& e) {
+        *err = e.what();
+        LOG_RUNTIME(FndRt, ERR, "%s", e.what());
+        return e.code();
+    } catch (const std::bad_alloc&) {
+        *err = "host allocation failed";
+        return FND_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        *err = e.what();
+        return FND_ERR_INVALID_ARG;
+    }
+}
 
 void CudaCheck(cudaError_t e, const char* what);
 #define CUDA_CHECK(expr) ::Foundation::CApi::CudaCheck((expr), #expr)
