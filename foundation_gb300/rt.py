@@ -86,6 +86,7 @@ SIGNATURES = {
     "fnd_rt_trace_closest": (_I32, [_P, _P, _P, _U32, _P, _I32]),
     "fnd_rt_trace_any": (_I32, [_P, _P, _P, _U32, _P, _I32]),
     "fnd_rt_trace_closest_stats": (_I32, [_P, _P, _P, _U32, _P, _I32, _P]),
+    "fnd_rt_trace_closest_noalloc": (_I32, [_P, _P, _U32, _P, _P]),
 }
 
 _lib = None

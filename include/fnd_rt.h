@@ -181,6 +181,23 @@ typedef struct fnd_rt_trace_stats {
 int fnd_rt_trace_closest_stats(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays,
                                uint32_t n, fnd_hit* out, int mem, fnd_rt_trace_stats* stats);
 
+/* Closest hit without any device allocation. No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc at trace time
+ * (a plugin inside a host application's frame callback, where the host
+ * forbids device allocations or has handed out all device memory up front,
+ * or code that must not add the device-wide synchronisation of
+ * cudaMalloc / cudaFree). rays / out are HOST buffers; the scene must have
+ * been uploaded beforehand. Results equal fnd_rt_trace_closest's.
+ * The rays and hits are staged through one fixed file-scope device array of
+ * about 2.5 MiB, which every GPU that loads this library holds until the
+ * process exits; a call takes at most 65,536 rays and larger n is rejected
+ * with FND_ERR_INVALID_ARG. The first call on a device resolves the array's
+ * address (set-up), so make it before any stream capture. All calls share
+ * the array: calls that overlap on the GPU race, so serialise them.
+ * stream: cudaStream_t, or NULL for the scene context's stream. Synchronous. */
+int fnd_rt_trace_closest_noalloc(const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n, fnd_hit* out,
+                                 void* stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
