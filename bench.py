@@ -52,6 +52,7 @@ def parse_args():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--rays", type=int, default=N_RAYS)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extra", action="store_true", help="skip the path-tracer and 1M-triangle blocks")
     return p.parse_args()
 
 
@@ -196,6 +197,63 @@ def algorithmic_bytes_per_ray(sc, rays, sample=1 << 20):
     n = min(sample, len(rays))
     nodes, tris = st["node_fetches"] / n, st["tri_tests"] / n
     return 32.0 + 8.0 + 32.0 * nodes + 36.0 * tris, nodes, tris
+
+
+def path_tracer_block(fg, torch, stream, local):
+    """One 1920x1080, 64-spp frame of the Cornell scene (max depth 8, RR from
+    bounce 3, NEE to the area light), timed with CUDA events on the pass's
+    stream after a 4-spp warm-up frame."""
+    from foundation_gb300 import scenes
+    cs = scenes.cornell_scene()
+    ctx = fg.Context(local, stream=stream.cuda_stream)
+    s = ctx.upload(cs.verts, cs.idx)
+    s.set_materials(cs.tri_material, scenes.material_records(cs))
+    s.set_lights(scenes.light_records(cs))
+    out = torch.empty(1920 * 1080 * 3, dtype=torch.float32, device="cuda")
+    ctx.render(s, 1920, 1080, 4, scenes.CORNELL_CAMERA, out=out)
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.render(s, 1920, 1080, 64, scenes.CORNELL_CAMERA, out=out)
+    e1.record(stream)
+    ctx.sync()
+    ms = e0.elapsed_time(e1)
+    st = ctx.render_stats()
+    ctx.close()
+    rays = st["extension_rays"] + st["shadow_rays"]
+    return {"workload": "cornell200 1920x1080 64 spp, max depth 8, RR from bounce 3, NEE", "frame_ms": ms,
+            "paths": st["paths"], "extension_rays": st["extension_rays"], "shadow_rays": st["shadow_rays"],
+            "mrays_s_incl_shading": rays / (ms * 1e-3) / 1e6, "waves": st["waves"]}
+
+
+def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
+    """Spec target workload: a 1,048,576-triangle soup in the unit cube
+    (edge lengths log-uniform in [1e-3, 0.1], seed 2) and 8,388,608 rays with
+    origins uniform in the cube and directions uniform on the sphere."""
+    from foundation_gb300 import scenes
+    so = scenes.soup_scene(1 << 20, seed=2)
+    rays = scenes.incoherent_rays(n_rays, (0, 0, 0), (1, 1, 1), seed=2)
+    ctx = fg.Context(local, stream=stream.cuda_stream)
+    s = ctx.upload(so.verts, so.idx)
+    rd = torch.from_numpy(rays).to("cuda")
+    hd = torch.empty(2 * n_rays, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(3):
+        s.closest(rd, hd)
+    ctx.sync()
+    reps = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        s.closest(rd, hd)
+    e1.record(stream)
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / reps
+    info = s.info()
+    ctx.close()
+    return {"workload": "soup 1,048,576 tris, 8,388,608 incoherent rays", "kernel_ms": ms,
+            "mrays_s": n_rays / (ms * 1e-3) / 1e6, "target_mrays_s": 1500.0,
+            "wide_nodes": info["num_wide_nodes"], "wide_depth": info["wide_depth"], "build_ms": info["build_ms"]}
 
 
 def cpu_baseline(sc, rays):
@@ -357,6 +415,9 @@ def main():
             "scene_info": {k: info[k] for k in ("num_wide_nodes", "wide_depth", "node_bytes", "tri_bytes",
                                                 "build_ms", "collapse_ms")},
         }
+        if not args.no_extra:
+            line["path_tracer"] = path_tracer_block(fg, torch, stream, local)
+            line["incoherent_1m_tris"] = incoherent_1m_block(fg, torch, stream, local)
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, rays)
         print(json.dumps(line), flush=True)

@@ -20,6 +20,8 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ_DIR = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libfnd_rt.so")
+DEMO_PATH = os.path.join(LIB_DIR, "fnd_pass_demo")
+RENDERER = os.path.join(PKG, "renderer")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-pthread,-Wall",
@@ -91,7 +93,28 @@ def build(force: bool = False, verbose: bool = False) -> str:
         os.replace(tmp, LIB_PATH)
         if verbose:
             print(f"linked {LIB_PATH}", file=sys.stderr)
+    _build_demo(force, verbose)
     return LIB_PATH
+
+
+def _build_demo(force: bool, verbose: bool) -> None:
+    """The C++ path-tracer pass (renderer/) and its headless driver, linked
+    against libfnd_rt.so with an $ORIGIN rpath."""
+    srcs = sorted(glob.glob(os.path.join(RENDERER, "*.cpp"))) + [os.path.join(CSRC, "core", "core.cpp")]
+    deps = srcs + glob.glob(os.path.join(RENDERER, "*.hpp")) + _headers() + [LIB_PATH]
+    if not force and os.path.exists(DEMO_PATH) and \
+            all(os.path.getmtime(d) <= os.path.getmtime(DEMO_PATH) for d in deps):
+        return
+    cxx = os.environ.get("CXX", "g++")
+    tmp = DEMO_PATH + f".tmp{os.getpid()}"
+    cmd = [cxx, "-O2", "-std=c++20", "-pthread", f"-I{os.path.join(ROOT, 'include')}", "-I/usr/local/cuda/include",
+           *srcs, "-o", tmp, f"-L{LIB_DIR}", "-lfnd_rt", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"demo build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, DEMO_PATH)
+    if verbose:
+        print(f"linked {DEMO_PATH}", file=sys.stderr)
 
 
 if __name__ == "__main__":

@@ -113,6 +113,7 @@ int fnd_rt_create(const fnd_rt_desc* desc, fnd_rt_ctx** out_ctx) {
             ctx->d_counter = reinterpret_cast<uint32_t*>(scratch);
             ctx->d_status = reinterpret_cast<uint32_t*>(scratch + 256);
             ctx->d_stats = reinterpret_cast<unsigned long long*>(scratch + 512);
+            ctx->d_render_stats = reinterpret_cast<unsigned long long*>(scratch + 768);
             CUDA_CHECK(cudaMemsetAsync(scratch, 0, 1024, ctx->stream));
             CUDA_CHECK(cudaMallocHost(&ctx->h_status, sizeof(uint32_t)));
             for (int v = 0; v < 4; ++v) CUDA_CHECK(RT::TraceOccupancy(v, &ctx->occupancy[v]));
@@ -134,10 +135,15 @@ int fnd_rt_destroy(fnd_rt_ctx* ctx) {
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });
     if (rc == FND_ERR_INVALID_ARG) return rc;
+    // the context is freed below: keep its failure message in the global slot
+    GlobalError() = ctx->last_error;
     cudaSetDevice(ctx->device);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->d_in) cudaFree(ctx->d_in);
     if (ctx->d_out) cudaFree(ctx->d_out);
+    if (ctx->d_paths) cudaFree(ctx->d_paths);
+    if (ctx->d_fb) cudaFree(ctx->d_fb);
+    if (ctx->d_rgb) cudaFree(ctx->d_rgb);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -220,6 +226,29 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
                 CHECK_CODE(b != 2, FND_ERR_INVALID_ARG, "non-finite vertex coordinate");
             }
         }
+        // geometric normals (winding order) for shading; material 0 until set
+        scene->tri_shade.resize(4 * (size_t)nt);
+        for (uint32_t t = 0; t < nt; ++t) {
+            const float* v = &tri[9 * (size_t)t];
+            const float e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+            const float e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+            float nx = e1[1] * e2[2] - e1[2] * e2[1], ny = e1[2] * e2[0] - e1[0] * e2[2],
+                  nz = e1[0] * e2[1] - e1[1] * e2[0];
+            const float l = std::sqrt(nx * nx + ny * ny + nz * nz);
+            if (l > 0.0f) {
+                nx /= l;
+                ny /= l;
+                nz /= l;
+            } else {
+                nx = ny = 0.0f;
+                nz = 1.0f;
+            }
+            float* o = &scene->tri_shade[4 * (size_t)t];
+            o[0] = nx;
+            o[1] = ny;
+            o[2] = nz;
+            o[3] = 0.0f;  // material 0 (bits)
+        }
         auto t0 = std::chrono::steady_clock::now();
         RT::BinaryBvh bin;
         RT::BuildBinaryBvh(tri.data(), nt, bp, bin);
@@ -254,9 +283,21 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             CUDA_CHECK(cudaMemcpy(tris, wide.v0.data(), plane, cudaMemcpyHostToDevice));
             CUDA_CHECK(cudaMemcpy(tris + plane, wide.v1.data(), plane, cudaMemcpyHostToDevice));
             CUDA_CHECK(cudaMemcpy(tris + 2 * plane, wide.v2.data(), plane, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMalloc(&scene->d_tri_shade, 16ull * nt));
+            CUDA_CHECK(cudaMemcpy(scene->d_tri_shade, scene->tri_shade.data(), 16ull * nt, cudaMemcpyHostToDevice));
+            // default material table: one grey Lambertian
+            PT::DevMaterial m{};
+            m.albedo_type = make_float4(0.8f, 0.8f, 0.8f, 0.0f);
+            m.emission_light = make_float4(0.f, 0.f, 0.f, __builtin_bit_cast(float, (int32_t)-1));
+            m.params = make_float4(1.0f, 0.f, 0.f, 0.f);
+            CUDA_CHECK(cudaMalloc(&scene->d_materials, sizeof(m)));
+            CUDA_CHECK(cudaMemcpy(scene->d_materials, &m, sizeof(m), cudaMemcpyHostToDevice));
+            scene->num_materials = 1;
         } catch (...) {
             if (scene->d_nodes) cudaFree(scene->d_nodes);
             if (scene->d_tris) cudaFree(scene->d_tris);
+            if (scene->d_tri_shade) cudaFree(scene->d_tri_shade);
+            if (scene->d_materials) cudaFree(scene->d_materials);
             throw;
         }
         I.upload_ms = MsSince(t0);
@@ -287,6 +328,9 @@ int fnd_rt_scene_destroy(fnd_rt_scene* scene) {
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
         if (scene->d_nodes) CUDA_CHECK(cudaFree(scene->d_nodes));
         if (scene->d_tris) CUDA_CHECK(cudaFree(scene->d_tris));
+        if (scene->d_tri_shade) CUDA_CHECK(cudaFree(scene->d_tri_shade));
+        if (scene->d_materials) CUDA_CHECK(cudaFree(scene->d_materials));
+        if (scene->d_lights) CUDA_CHECK(cudaFree(scene->d_lights));
     });
     ctx->live_scenes--;
     delete scene;

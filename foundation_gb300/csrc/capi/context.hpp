@@ -9,7 +9,10 @@
 
 #include "../../../include/fnd_rt.h"
 #include "../core/core.hpp"
+#include "../pt/integrator.hpp"
 #include "../rt/traverse_launch.hpp"
+
+#include <vector>
 
 struct fnd_rt_ctx {
     int device = 0;
@@ -29,6 +32,17 @@ struct fnd_rt_ctx {
     void* d_out = nullptr;
     size_t d_out_cap = 0;
     int live_scenes = 0;
+    // path-tracing state: path buffers (capacity paths) and the frame buffer
+    Foundation::PT::PathBuffers paths{};
+    void* d_paths = nullptr;
+    size_t paths_bytes = 0;
+    float4* d_fb = nullptr;
+    size_t fb_pixels = 0;
+    uint32_t fb_width = 0, fb_height = 0, fb_samples = 0;
+    float* d_rgb = nullptr;  // finalize target for host outputs
+    size_t rgb_cap = 0;
+    unsigned long long* d_render_stats = nullptr;  // [0] extension rays, [1] shadow rays
+    fnd_render_stats last_render{};
     std::string last_error;
     Foundation::Core::HeapAllocator allocator;
 };
@@ -39,6 +53,13 @@ struct fnd_rt_scene {
     void* d_tris = nullptr;
     Foundation::RT::DeviceScene view{};
     fnd_rt_scene_info info{};
+    // shading data (original triangle order)
+    std::vector<float> tri_shade;  // 4 floats per triangle: unit normal, material id bits
+    void* d_tri_shade = nullptr;
+    void* d_materials = nullptr;
+    uint32_t num_materials = 0;
+    void* d_lights = nullptr;
+    uint32_t num_lights = 0;
 };
 
 namespace Foundation {

@@ -1,0 +1,85 @@
+// integrator.hpp — host-visible interface of the wavefront path tracer.
+//
+// A frame is processed in waves of at most `capacity` paths. Per wave:
+//   generate -> [extend (closest hit) -> shade -> shadow (any hit + resolve)] x max_depth
+// Queues live in device memory and their lengths are device counters, so no
+// stage needs a host round trip; the host only enqueues the fixed sequence.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../rt/device_scene.hpp"
+
+namespace Foundation {
+namespace PT {
+
+constexpr uint32_t kMatLambert = 0;
+constexpr uint32_t kMatGGX = 1;
+constexpr uint32_t kMatEmissive = 2;
+
+struct DevMaterial {
+    float4 albedo_type;     // rgb albedo / specular colour, w = type bits
+    float4 emission_light;  // rgb emission, w = light index bits (int, -1 = none)
+    float4 params;          // x = GGX alpha
+};
+
+struct DevQuadLight {
+    float4 corner_area;  // xyz corner, w = area
+    float4 eu;           // edge u
+    float4 ev;           // edge v
+    float4 normal;       // unit emitting-side normal (cross(eu, ev))
+    float4 radiance;     // rgb
+};
+
+struct ShadeScene {
+    const float4* tri_shade;  // per original triangle: unit geometric normal (winding), w = material id bits
+    const DevMaterial* materials;
+    const DevQuadLight* lights;
+    uint32_t num_lights;
+    uint32_t num_materials;
+};
+
+struct RenderParams {
+    uint32_t width, height;
+    uint32_t spp;            // samples per pixel of this call
+    uint32_t max_depth;      // surface interactions per path
+    uint32_t rr_start;       // first bounce index that applies Russian roulette
+    uint32_t sample_offset;  // sample index of the first sample of this call (accumulation)
+    uint64_t seed;
+    float eye[3], fwd[3], right[3], up[3];
+    float tan_half, aspect;
+    float sky[3];
+    float sun_dir[3];  // unit, towards the sun
+    float sun_E[3];    // irradiance of the directional sun
+    uint32_t has_sun;
+    float eps;         // ray-origin offset along the normal
+};
+
+struct PathBuffers {
+    uint32_t capacity;
+    uint4* rng;          // x,y = PCG state (lo, hi), z = sequence (sample index), w = pixel
+    float4* beta;        // rgb throughput, w = solid-angle pdf of the last BSDF sample (0 at the camera)
+    float4* ext_rays[2]; // 2 float4 per ray (fnd_ray layout), ping-pong by bounce parity
+    uint32_t* ext_path[2];
+    uint2* hits;
+    float4* sh_rays;     // 2 float4 per shadow ray; up to 2 per path per bounce
+    uint32_t* sh_pixel;
+    float4* sh_contrib;
+    uint8_t* sh_occluded;
+    uint32_t* counts;    // [0], [1] extension queues, [2] shadow queue, [3..] statistics
+    float4* fb;          // per-pixel radiance sums
+};
+
+// Statistics counters appended after the queue counts.
+constexpr int kCountExt0 = 0, kCountExt1 = 1, kCountShadow = 2, kStatExt = 4, kStatShadow = 6;  // 64-bit at 4, 6
+
+cudaError_t LaunchGenerate(const PathBuffers& B, const RenderParams& R, uint64_t wave_base, uint32_t wave_n,
+                           cudaStream_t s);
+cudaError_t LaunchShade(const PathBuffers& B, const RenderParams& R, const ShadeScene& S, int cur, uint32_t bounce,
+                        int grid, cudaStream_t s);
+cudaError_t LaunchResolve(const PathBuffers& B, int grid, cudaStream_t s);
+cudaError_t LaunchFinalize(const PathBuffers& B, float* rgb, uint32_t npix, float scale, cudaStream_t s);
+
+}  // namespace PT
+}  // namespace Foundation

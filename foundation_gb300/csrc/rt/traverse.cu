@@ -36,6 +36,8 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
     uint2 l_stack[kMaxStack - kShort];
     const int tid = threadIdx.x;
     const uint32_t lane = tid & 31;
+    const uint32_t n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
+    if (L.ray_total && blockIdx.x == 0 && tid == 0) atomicAdd(L.ray_total, (unsigned long long)n);
 
     bool active = false, exhausted = false;
     uint32_t ray_id = 0;
@@ -54,10 +56,10 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(L.counter, cnt);
             base = __shfl_sync(kFull, base, 0);
-            if (base + cnt >= L.n) exhausted = true;
+            if (base + cnt >= n) exhausted = true;
             if (!active) {
                 const uint32_t id = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                if (id < L.n) {
+                if (id < n) {
                     const float4 r0 = __ldcs(L.rays + 2 * (size_t)id);
                     const float4 r1 = __ldcs(L.rays + 2 * (size_t)id + 1);
                     r = setup_ray(r0, r1);
@@ -182,8 +184,9 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
     }
 }
 
-__global__ void fill_miss_kernel(uint2* hits, uint8_t* occluded, uint32_t n) {
+__global__ void fill_miss_kernel(uint2* hits, uint8_t* occluded, uint32_t cap, const uint32_t* n_dev) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = n_dev ? min(*n_dev, cap) : cap;
     if (i >= n) return;
     if (hits) hits[i] = make_uint2(FND_INVALID_ID, 0x7F800000u);
     if (occluded) occluded[i] = 0;
@@ -218,7 +221,7 @@ cudaError_t LaunchTrace(const TraceLaunch& L, bool any, bool stats, int grid, cu
     if (L.scene.num_nodes == 0) {
         const uint32_t threads = 256;
         fill_miss_kernel<<<(L.n + threads - 1) / threads, threads, 0, stream>>>(
-            any ? nullptr : reinterpret_cast<uint2*>(L.hits), any ? L.occluded : nullptr, L.n);
+            any ? nullptr : reinterpret_cast<uint2*>(L.hits), any ? L.occluded : nullptr, L.n, L.n_dev);
         return cudaGetLastError();
     }
     cudaError_t e = cudaMemsetAsync(L.counter, 0, sizeof(uint32_t), stream);

@@ -16,7 +16,9 @@ constexpr int kTraceShortStack = 8;  // stack entries per thread kept in shared 
 struct TraceLaunch {
     DeviceScene scene;
     const float4* rays;  // 2 float4 per fnd_ray
-    uint32_t n;
+    uint32_t n;              // ray count, or the capacity when n_dev is set
+    const uint32_t* n_dev;   // device-side ray count (a queue length), or null
+    unsigned long long* ray_total;  // if set, the launch adds its ray count here
     void* hits;          // fnd_hit[n] (closest)
     uint8_t* occluded;   // uint8[n]   (any)
     uint32_t* counter;   // work-queue counter (zeroed before each launch)

@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -35,6 +36,11 @@ ABI_VERSION = 1
 INVALID_ID = 0xFFFFFFFF
 
 HIT_DTYPE = np.dtype([("prim", np.uint32), ("t", np.float32)])
+MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("albedo", "<f4", 3), ("roughness", "<f4"), ("emission", "<f4", 3),
+                           ("light", "<i4"), ("reserved", "<f4", 3)])
+LIGHT_DTYPE = np.dtype([("corner", "<f4", 3), ("edge_u", "<f4", 3), ("edge_v", "<f4", 3), ("radiance", "<f4", 3)])
+MAT_LAMBERT, MAT_GGX, MAT_EMISSIVE = 0, 1, 2
+RENDER_ACCUMULATE = 1
 
 
 class FndError(RuntimeError):
@@ -66,6 +72,22 @@ class SceneInfo(C.Structure):
         return d
 
 
+class _Camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3), ("vfov_deg", C.c_float)]
+
+
+class _RenderDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32), ("max_depth", C.c_uint32),
+                ("rr_start", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64), ("camera", _Camera),
+                ("sky", C.c_float * 3), ("sun_dir", C.c_float * 3), ("sun_irradiance", C.c_float * 3),
+                ("wave_paths", C.c_uint32)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("waves", C.c_uint32), ("samples_accumulated", C.c_uint32)]
+
+
 class TraceStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("node_fetches", C.c_uint64), ("tri_tests", C.c_uint64)]
 
@@ -87,6 +109,10 @@ SIGNATURES = {
     "fnd_rt_trace_any": (_I32, [_P, _P, _P, _U32, _P, _I32]),
     "fnd_rt_trace_closest_stats": (_I32, [_P, _P, _P, _U32, _P, _I32, _P]),
     "fnd_rt_trace_closest_noalloc": (_I32, [_P, _P, _U32, _P, _P]),
+    "fnd_rt_scene_set_materials": (_I32, [_P, _P, _U32, _P, _U32]),
+    "fnd_rt_scene_set_lights": (_I32, [_P, _P, _U32]),
+    "fnd_rt_render": (_I32, [_P, _P, _P, _P, _I32]),
+    "fnd_rt_render_stats_get": (_I32, [_P, _P]),
 }
 
 _lib = None
@@ -137,6 +163,7 @@ class Context:
         _check(load().fnd_rt_create(C.byref(d), C.byref(h)))
         self._h = h
         self.device = device
+        self._scenes = weakref.WeakSet()
 
     @property
     def handle(self):
@@ -150,9 +177,15 @@ class Context:
         _check(load().fnd_rt_sync(self._h), self._h)
 
     def close(self):
+        """Destroys the scenes still open on this context, then the context."""
         if self._h is not None:
-            _check(load().fnd_rt_destroy(self._h))
-            self._h = None
+            for sc in list(self._scenes):
+                sc.close()
+            rc = load().fnd_rt_destroy(self._h)
+            if rc == -1:  # refused (scenes still alive): the context is intact
+                _check(rc, self._h)
+            self._h = None  # freed; a failure message is in the global slot
+            _check(rc, None)
 
     def __enter__(self):
         return self
@@ -162,6 +195,29 @@ class Context:
 
     def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0) -> "Scene":
         return Scene(self, verts, idx, bins, max_leaf, threads)
+
+    def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
+               rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
+               sun_irradiance=(0.0, 0.0, 0.0), accumulate: bool = False, wave_paths: int = 0, out=None):
+        """Path-traces spp samples per pixel. Host: returns (height, width, 3)
+        float32 mean radiance. Device: out is a CUDA tensor of
+        width*height*3 floats, filled asynchronously."""
+        cam = _Camera((C.c_float * 3)(*camera["eye"]), (C.c_float * 3)(*camera["target"]),
+                      (C.c_float * 3)(*camera.get("up", (0.0, 1.0, 0.0))), camera.get("vfov_deg", 45.0))
+        d = _RenderDesc(width, height, spp, max_depth, rr_start, RENDER_ACCUMULATE if accumulate else 0, seed, cam,
+                        (C.c_float * 3)(*sky), (C.c_float * 3)(*sun_dir), (C.c_float * 3)(*sun_irradiance),
+                        wave_paths)
+        if out is not None and _is_device(out):
+            _check(load().fnd_rt_render(self._h, scene.handle, C.byref(d), _ptr(out), FND_MEM_DEVICE), self._h)
+            return out
+        img = np.empty((height, width, 3), np.float32) if out is None else out
+        _check(load().fnd_rt_render(self._h, scene.handle, C.byref(d), _ptr(img), FND_MEM_HOST), self._h)
+        return img
+
+    def render_stats(self) -> dict:
+        st = RenderStats()
+        _check(load().fnd_rt_render_stats_get(self._h, C.byref(st)), self._h)
+        return {k: getattr(st, k) for k, _ in st._fields_}
 
 
 class Scene:
@@ -175,10 +231,20 @@ class Scene:
         _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),
                ctx.handle)
         self._h = h
+        ctx._scenes.add(self)
 
     @property
     def handle(self):
         return self._h
+
+    def set_materials(self, tri_material, materials):
+        tm = np.ascontiguousarray(tri_material, dtype=np.uint32)
+        mats = np.ascontiguousarray(materials, dtype=MATERIAL_DTYPE)
+        _check(load().fnd_rt_scene_set_materials(self._h, _ptr(tm), len(tm), _ptr(mats), len(mats)), self.ctx.handle)
+
+    def set_lights(self, lights):
+        ls = np.ascontiguousarray(lights, dtype=LIGHT_DTYPE)
+        _check(load().fnd_rt_scene_set_lights(self._h, _ptr(ls) if len(ls) else None, len(ls)), self.ctx.handle)
 
     def info(self) -> dict:
         out = SceneInfo()

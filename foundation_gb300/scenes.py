@@ -306,3 +306,73 @@ def soup_scene(n: int, seed: int = 2, stream_base: int = 0) -> Scene:
     v = np.stack([p, p + d1 * l1[:, None], p + d2 * l2[:, None]], 1).astype(np.float32)
     f = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
     return Scene(v.reshape(-1, 3), f, bounds=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), name=f"soup{n}")
+
+
+def material_records(scene: Scene) -> np.ndarray:
+    """fnd_material records of a scene's material table; the k-th emissive
+    material is tied to the k-th quad light."""
+    from .rt import MATERIAL_DTYPE
+    rows = scene.materials if scene.materials is not None else np.array([[0, 0.8, 0.8, 0.8, 1, 0, 0, 0]], np.float32)
+    out = np.zeros(len(rows), MATERIAL_DTYPE)
+    k = 0
+    for i, r in enumerate(rows):
+        out[i]["type"] = int(r[0])
+        out[i]["albedo"] = r[1:4]
+        out[i]["roughness"] = r[4]
+        out[i]["emission"] = r[5:8]
+        out[i]["light"] = -1
+        if int(r[0]) == int(MAT_LIGHT):
+            out[i]["light"] = k
+            k += 1
+    return out
+
+
+def light_records(scene: Scene) -> np.ndarray:
+    from .rt import LIGHT_DTYPE
+    out = np.zeros(len(scene.lights), LIGHT_DTYPE)
+    for i, L in enumerate(scene.lights):
+        out[i]["corner"] = L["corner"]
+        out[i]["edge_u"] = L["edge_u"]
+        out[i]["edge_v"] = L["edge_v"]
+        out[i]["radiance"] = L["radiance"]
+    return out
+
+
+def sphere_scene(level: int = 4, radius: float = 1.0, material=(0, 0.5, 0.5, 0.5, 1.0, 0, 0, 0)) -> Scene:
+    """One icosphere at the origin with one material (furnace tests)."""
+    v, f = icosphere(level)
+    return Scene((v * radius).astype(np.float32), f, tri_material=np.zeros(len(f), np.uint32),
+                 materials=np.asarray([material], np.float32), bounds=((-radius,) * 3, (radius,) * 3),
+                 name=f"sphere{level}")
+
+
+def write_obj(scene: Scene, path: str) -> None:
+    """Writes the scene as OBJ + MTL (+ "#fnd quad_light" lines), the format
+    the C++ pass's ObjLoader reads."""
+    import os
+    mtl = os.path.splitext(path)[0] + ".mtl"
+    rows = scene.materials if scene.materials is not None else np.array([[0, 0.8, 0.8, 0.8, 1, 0, 0, 0]])
+    with open(mtl, "w") as f:
+        for i, r in enumerate(rows):
+            f.write(f"newmtl m{i}\n")
+            t = int(r[0])
+            if t == int(MAT_GGX):
+                f.write(f"Pm 1\nKs {r[1]:.9g} {r[2]:.9g} {r[3]:.9g}\nPr {r[4]:.9g}\n")
+            elif t == int(MAT_LIGHT):
+                f.write(f"Kd 0 0 0\nKe {r[5]:.9g} {r[6]:.9g} {r[7]:.9g}\n")
+            else:
+                f.write(f"Kd {r[1]:.9g} {r[2]:.9g} {r[3]:.9g}\n")
+    tm = scene.tri_material if scene.tri_material is not None else np.zeros(scene.num_tris, np.uint32)
+    with open(path, "w") as f:
+        f.write(f"mtllib {os.path.basename(mtl)}\n")
+        for L in scene.lights:
+            vals = [*L["corner"], *L["edge_u"], *L["edge_v"], *L["radiance"]]
+            f.write("#fnd quad_light " + " ".join(f"{float(x):.9g}" for x in vals) + "\n")
+        f.write("".join(f"v {x:.9g} {y:.9g} {z:.9g}\n" for x, y, z in scene.verts.astype(np.float64)))
+        cur = None
+        for t in range(scene.num_tris):
+            if tm[t] != cur:
+                cur = tm[t]
+                f.write(f"usemtl m{cur}\n")
+            a, b, c = scene.idx[t] + 1
+            f.write(f"f {a} {b} {c}\n")

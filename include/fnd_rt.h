@@ -120,7 +120,8 @@ int fnd_rt_create(const fnd_rt_desc* desc, fnd_rt_ctx** out_ctx);
 int fnd_rt_destroy(fnd_rt_ctx* ctx);
 
 /* Message of the last failure on ctx ("" if none); valid until the next call
- * on ctx. ctx may be NULL for failures of fnd_rt_create. */
+ * on ctx. With ctx = NULL: the message of the calling thread's last failed
+ * fnd_rt_create / fnd_rt_destroy or call made without a valid context. */
 const char* fnd_rt_last_error(const fnd_rt_ctx* ctx);
 
 /* Waits for the context's stream and returns the device status: FND_OK, or
@@ -180,6 +181,85 @@ typedef struct fnd_rt_trace_stats {
  * the kernel) and returns the totals. Same memory rules as trace_closest. */
 int fnd_rt_trace_closest_stats(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays,
                                uint32_t n, fnd_hit* out, int mem, fnd_rt_trace_stats* stats);
+
+/* ---- path tracing ------------------------------------------------------
+ * The reference's per-frame entry is Renderer::Draw
+ * (src/Renderer/Renderer.cpp:367-401): update the camera, record, submit,
+ * present. fnd_rt_render is the path-tracer pass's counterpart: one call
+ * renders `spp` samples per pixel of the scene into a linear-radiance RGB
+ * buffer (no swapchain: the caller owns the output). */
+
+enum { FND_MAT_LAMBERT = 0, FND_MAT_GGX = 1, FND_MAT_EMISSIVE = 2 };
+
+/* 48 bytes. Lambert: albedo. GGX: albedo is the specular colour F0 (Schlick),
+ * roughness is the GGX alpha. Emissive: one-sided black emitter with
+ * radiance `emission` on the side its triangle winding faces; `light` is the
+ * index of the quad light (fnd_rt_scene_set_lights) with the same geometry,
+ * used to weight BSDF-sampled hits against light sampling (-1: none). */
+typedef struct fnd_material {
+    uint32_t type;
+    float albedo[3];
+    float roughness;
+    float emission[3];
+    int32_t light;
+    float reserved[3];
+} fnd_material;
+
+/* Parallelogram light corner + u*edge_u + v*edge_v, emitting `radiance` on
+ * the side of cross(edge_u, edge_v). 48 bytes. */
+typedef struct fnd_quad_light {
+    float corner[3];
+    float edge_u[3];
+    float edge_v[3];
+    float radiance[3];
+} fnd_quad_light;
+
+/* Pinhole camera in the glm::lookAt convention of the reference
+ * (src/Renderer/Renderer.cpp:374-380): right-handed, looking from eye to target. */
+typedef struct fnd_camera {
+    float eye[3];
+    float target[3];
+    float up[3];
+    float vfov_deg;
+} fnd_camera;
+
+enum { FND_RENDER_ACCUMULATE = 1u };
+
+typedef struct fnd_render_desc {
+    uint32_t width, height;
+    uint32_t spp;        /* samples per pixel in this call */
+    uint32_t max_depth;  /* surface interactions per path, 1..64 (8) */
+    uint32_t rr_start;   /* first bounce index with Russian roulette (3) */
+    uint32_t flags;      /* FND_RENDER_ACCUMULATE: add to the previous calls' samples */
+    uint64_t seed;       /* PCG32 seed; each pixel gets its own stream */
+    fnd_camera camera;
+    float sky[3];          /* constant radiance of escaping rays */
+    float sun_dir[3];      /* towards the sun; zero vector: no sun */
+    float sun_irradiance[3];
+    uint32_t wave_paths;   /* paths in flight per wave, 0: automatic */
+} fnd_render_desc;
+
+typedef struct fnd_render_stats {
+    uint64_t paths;
+    uint64_t extension_rays;
+    uint64_t shadow_rays;
+    uint32_t waves;
+    uint32_t samples_accumulated;
+} fnd_render_stats;
+
+/* Material per triangle (original index order) and the material table. */
+int fnd_rt_scene_set_materials(fnd_rt_scene* scene, const uint32_t* tri_material, uint32_t nt,
+                               const fnd_material* materials, uint32_t nm);
+/* Quad lights sampled by next-event estimation. */
+int fnd_rt_scene_set_lights(fnd_rt_scene* scene, const fnd_quad_light* lights, uint32_t nl);
+
+/* Renders desc->spp samples per pixel. rgb: width*height*3 floats, row-major
+ * from the top row, receiving the mean radiance over all accumulated samples;
+ * host or device memory per `mem` (FND_MEM_DEVICE: asynchronous). */
+int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_desc* desc, float* rgb, int mem);
+
+/* Counters of the last fnd_rt_render call (synchronises the stream). */
+int fnd_rt_render_stats_get(fnd_rt_ctx* ctx, fnd_render_stats* out);
 
 /* Closest hit without any device allocation. No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc at trace time

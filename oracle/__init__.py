@@ -19,8 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "librt_oracle.so")
-SOURCES = ["rt_oracle.cpp"]
-HEADERS = ["rt_oracle.h", "oracle_common.hpp"]
+SOURCES = ["rt_oracle.cpp", "pt_oracle.cpp"]
+HEADERS = ["rt_oracle.h", "oracle_common.hpp", "rt_oracle_internal.hpp"]
 CXXFLAGS = ["-O3", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared", "-pthread"]
 
 _lib = None
@@ -64,6 +64,8 @@ def lib():
         L.orc_pcg32_fill.argtypes = [U64, U64, P, U64]
         L.orc_time_build_ms.argtypes = [P, U32, P, U32, U32, U32]
         L.orc_time_build_ms.restype = C.c_double
+        L.orc_pt_render.argtypes = [P, P, P, U32, P, U32, P, U32, U32, U32, U32, U32, U64, P, U32, U32, U32, U32,
+                                    U32, P]
         _lib = L
     return _lib
 
@@ -152,3 +154,23 @@ def time_build_ms(verts, idx, bins: int = 32, max_leaf: int = 4) -> float:
     verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
     idx = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
     return float(lib().orc_time_build_ms(_ptr(verts), len(verts), _ptr(idx), len(idx), bins, max_leaf))
+
+
+def pt_render(bvh: OracleBVH, tri_material, materials, lights, camera: dict, width: int, height: int, spp: int, *,
+              max_depth: int = 8, rr_start: int = 3, seed: int = 1, sky=(0, 0, 0), sun_dir=(0, 0, 0),
+              sun_irradiance=(0, 0, 0), crop=None, threads: int = 0) -> np.ndarray:
+    """FP64 path-traced crop (x0, y0, w, h) of a width x height image:
+    (h, w, 3) float64 mean radiance. materials / lights: fnd_material /
+    fnd_quad_light records (numpy structured arrays)."""
+    x0, y0, cw, ch = crop if crop else (0, 0, width, height)
+    tm = np.ascontiguousarray(tri_material, dtype=np.uint32) if tri_material is not None else None
+    mats = np.ascontiguousarray(materials)
+    ls = np.ascontiguousarray(lights)
+    cam = np.array([*camera["eye"], *camera["target"], *camera.get("up", (0, 1, 0)), camera.get("vfov_deg", 45.0)],
+                   np.float64)
+    env = np.array([*sky, *sun_dir, *sun_irradiance], np.float64)
+    out = np.zeros((ch, cw, 3), np.float64)
+    lib().orc_pt_render(bvh._h, _ptr(tm) if tm is not None else None, _ptr(mats), len(mats),
+                        _ptr(ls) if len(ls) else None, len(ls), _ptr(cam), width, height, spp, max_depth, rr_start,
+                        seed, _ptr(env), x0, y0, cw, ch, threads, _ptr(out))
+    return out

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "oracle_common.hpp"
+#include "rt_oracle_internal.hpp"
 
 using namespace oracle;
 
@@ -48,26 +49,6 @@ struct Aabb {
     }
 };
 
-struct BNode {
-    float lo[3], hi[3];
-    uint32_t a;      // internal: left child (right = a + 1); leaf: first prim slot
-    uint32_t count;  // 0: internal, else number of triangles
-};
-
-}  // namespace
-
-struct orc_bvh {
-    std::vector<BNode> nodes;
-    std::vector<uint32_t> prims;  // leaf slots -> original triangle index
-    std::vector<float> tri;       // 9 floats per original triangle
-    uint32_t nt = 0;
-    uint32_t depth = 0;
-    uint32_t max_leaf = 4;
-    double sah = 0.0;
-    float margin = 0.0f;
-};
-
-namespace {
 
 void tri_bounds(const orc_bvh& b, uint32_t t, Aabb& box) {
     box = Aabb();

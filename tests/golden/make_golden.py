@@ -56,6 +56,12 @@ def main():
     hc = bc.closest(ir)
     np.savez_compressed(os.path.join(OUT, "cornell_rows.npz"), rays=ir, prim=hc["prim"], t=hc["t"],
                         scene_sha256=np.array(digest(cs.verts, cs.idx, cs.tri_material, cs.materials)))
+    # 4) FP64 oracle render of the Cornell box at 96x54, 4096 spp
+    cam = scenes.CORNELL_CAMERA
+    img = oracle.pt_render(bc, cs.tri_material, scenes.material_records(cs), scenes.light_records(cs), cam, 96, 54,
+                           4096, max_depth=8, rr_start=3, seed=7)
+    np.savez_compressed(os.path.join(OUT, "cornell_fp64_96x54.npz"), image=img.astype(np.float32), spp=4096,
+                        max_depth=8, rr_start=3)
     print("written to", OUT)
 
 

@@ -1,0 +1,108 @@
+"""GPU wavefront path tracer against the FP64 oracle: exact furnace values,
+GGX furnace means, and the Cornell box against the committed 4096-spp FP64
+render (relMSE = mean((I - R)^2 / (R^2 + 1e-2)))."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from foundation_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FURNACE_CAM = dict(eye=(0.0, 0.0, 4.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), vfov_deg=45.0)
+
+
+def relmse(img, ref, eps=1e-2):
+    img = np.asarray(img, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
+
+
+@pytest.fixture(scope="module")
+def ctx(built):
+    import foundation_gb300 as fg
+    c = fg.Context(0)
+    yield c
+    c.close()
+
+
+def upload(ctx, sc):
+    s = ctx.upload(sc.verts, sc.idx)
+    s.set_materials(sc.tri_material, S.material_records(sc))
+    s.set_lights(S.light_records(sc))
+    return s
+
+
+def test_lambert_furnace_exact(ctx):
+    sc = S.sphere_scene(4, 1.0)
+    s = upload(ctx, sc)
+    img = ctx.render(s, 64, 64, 16, FURNACE_CAM, sky=(1, 1, 1))
+    assert np.all(img[24:40, 24:40] == 0.5)
+    assert img.min() >= 0.5 - 1e-6 and img.max() <= 1.0 + 1e-6
+    assert np.all(img[0, 0] == 1.0)
+    s.close()
+
+
+def test_ggx_furnace_matches_oracle(ctx):
+    sc = S.sphere_scene(4, 1.0, material=(1, 1.0, 1.0, 1.0, 0.5, 0, 0, 0))
+    s = upload(ctx, sc)
+    img = ctx.render(s, 48, 48, 2048, FURNACE_CAM, sky=(1, 1, 1))
+    b = O.OracleBVH(sc.verts, sc.idx)
+    ref = O.pt_render(b, sc.tri_material, S.material_records(sc), S.light_records(sc), FURNACE_CAM, 48, 48, 1024,
+                      sky=(1, 1, 1))
+    m = slice(16, 32)
+    g, r = img[m, m].mean(), ref[m, m].mean()
+    assert 0.5 < r < 1.0
+    assert abs(g / r - 1.0) < 5e-3, (g, r)
+    s.close()
+
+
+def test_cornell_matches_fp64_oracle(ctx):
+    g = np.load(os.path.join(GOLDEN, "cornell_fp64_96x54.npz"))
+    ref = g["image"]
+    cs = S.cornell_scene()
+    s = upload(ctx, cs)
+    a = ctx.render(s, 96, 54, 4096, S.CORNELL_CAMERA, seed=1)
+    b = ctx.render(s, 96, 54, 4096, S.CORNELL_CAMERA, seed=2)
+    r_ab = relmse(a, b)
+    r = relmse(a, ref)
+    # both sides carry sampling noise only: without bias relMSE(a, ref) ~ r_ab
+    assert r < 1.5 * r_ab + 1e-5, (r, r_ab)
+    assert abs(a.mean() / ref.mean() - 1.0) < 0.01
+    st = ctx.render_stats()
+    assert st["paths"] == 96 * 54 * 4096
+    assert st["extension_rays"] >= st["paths"] and st["shadow_rays"] > 0
+    s.close()
+
+
+def test_accumulate(ctx):
+    cs = S.cornell_scene(num_spheres=20, level=2)
+    s = upload(ctx, cs)
+    one = ctx.render(s, 64, 36, 8, S.CORNELL_CAMERA, seed=3)
+    two = ctx.render(s, 64, 36, 8, S.CORNELL_CAMERA, seed=3, accumulate=True)
+    assert ctx.render_stats()["samples_accumulated"] == 16
+    assert not np.array_equal(one, two)
+    full = ctx.render(s, 64, 36, 1024, S.CORNELL_CAMERA, seed=9)
+    assert relmse(two, full) < relmse(one, full) * 1.2
+    s.close()
+
+
+def test_render_argument_errors(ctx):
+    import foundation_gb300 as fg
+    cs = S.cornell_scene(num_spheres=2, level=1)
+    s = upload(ctx, cs)
+    with pytest.raises(fg.FndError):
+        ctx.render(s, 0, 10, 1, S.CORNELL_CAMERA)
+    with pytest.raises(fg.FndError):
+        ctx.render(s, 8, 8, 1, dict(eye=(0, 0, 0), target=(0, 0, 0)))
+    with pytest.raises(fg.FndError):
+        s.set_materials(np.zeros(3, np.uint32), S.material_records(cs))
+    bad = S.material_records(cs)
+    bad[0]["type"] = 7
+    with pytest.raises(fg.FndError):
+        s.set_materials(cs.tri_material, bad)
+    img = ctx.render(s, 8, 8, 1, S.CORNELL_CAMERA)  # context still usable
+    assert np.isfinite(img).all()
+    s.close()
