@@ -87,6 +87,50 @@ bool Normalize(double v[3]) {
     return true;
 }
 
+// One wave's bounce loop: extend -> shade -> shadow -> resolve, max_depth times.
+void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffers& B, const PT::RenderParams& R,
+                const PT::ShadeScene& S, const PT::CacheIO& C, uint32_t max_depth, int grid_shade) {
+    const int g_closest = ctx->sm_count * std::max(1, ctx->occupancy[0]);
+    const int g_any = ctx->sm_count * std::max(1, ctx->occupancy[1]);
+    for (uint32_t b = 0; b < max_depth; ++b) {
+        const int cur = (int)(b & 1u), nxt = cur ^ 1;
+        RT::TraceLaunch L{};
+        L.scene = scene->view;
+        L.rays = B.ext_rays[cur];
+        L.n = B.capacity;
+        L.n_dev = B.counts + cur;
+        L.ray_total = ctx->d_render_stats + 0;
+        L.hits = B.hits;
+        L.counter = ctx->d_counter;
+        L.status = ctx->d_status;
+        L.refill_min = ctx->refill_min;
+        CUDA_CHECK(RT::LaunchTrace(L, false, false, g_closest, ctx->stream));
+        CUDA_CHECK(cudaMemsetAsync(B.counts + nxt, 0, sizeof(uint32_t), ctx->stream));
+        CUDA_CHECK(cudaMemsetAsync(B.counts + PT::kCountShadow, 0, sizeof(uint32_t), ctx->stream));
+        CUDA_CHECK(PT::LaunchShade(B, R, S, C, cur, b, grid_shade, ctx->stream));
+        RT::TraceLaunch A{};
+        A.scene = scene->view;
+        A.rays = B.sh_rays;
+        A.n = 2 * B.capacity;
+        A.n_dev = B.counts + PT::kCountShadow;
+        A.ray_total = ctx->d_render_stats + 1;
+        A.occluded = B.sh_occluded;
+        A.counter = ctx->d_counter;
+        A.status = ctx->d_status;
+        A.refill_min = ctx->refill_min;
+        CUDA_CHECK(RT::LaunchTrace(A, true, false, g_any, ctx->stream));
+        CUDA_CHECK(PT::LaunchResolve(B, grid_shade, ctx->stream));
+    }
+}
+
+uint32_t Mix32(uint64_t a, uint64_t b) {
+    uint64_t x = a * 0x9E3779B97F4A7C15ull ^ (b + 0x632BE59BD9B4E019ull);
+    x ^= x >> 31;
+    x *= 0xBF58476D1CE4E5B9ull;
+    x ^= x >> 29;
+    return (uint32_t)x;
+}
+
 }  // namespace
 
 extern "C" {
@@ -186,7 +230,12 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         uint32_t cap = D.wave_paths ? D.wave_paths : kDefaultWave;
         if (cap > total) cap = (uint32_t)total;
         CHECK_CODE(cap >= 1 && cap <= (1u << 28), FND_ERR_INVALID_ARG, "wave_paths %u out of range", cap);
-        EnsurePathBuffers(ctx, cap);
+        const bool use_cache = (D.flags & FND_RENDER_CACHE) != 0;
+        CHECK_CODE(!use_cache || ctx->cache != nullptr, FND_ERR_INVALID_ARG,
+                   "FND_RENDER_CACHE needs a cache (fnd_rt_cache_create)");
+        const uint32_t train_paths = use_cache ? ctx->cache->desc.train_paths : 0u;
+        EnsurePathBuffers(ctx, std::max(cap, train_paths));
+        if (use_cache) CApi::EnsureCacheBuffers(ctx, cap, D.max_depth);
         // frame buffer (restart unless accumulating into a frame of the same size)
         const bool accumulate = (D.flags & FND_RENDER_ACCUMULATE) && ctx->d_fb && ctx->fb_width == D.width &&
                                 ctx->fb_height == D.height;
@@ -244,43 +293,49 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         S.num_materials = scene->num_materials;
         CHECK_CODE(scene->info.num_tris == 0 || S.tri_shade != nullptr, FND_ERR_INVALID_SCENE, "scene has no shading data");
         PT::PathBuffers& B = ctx->paths;
-        const int grid_shade = std::max(1, std::min<int>((int)((cap + 255) / 256), ctx->sm_count * 8));
+        const int grid_shade =
+            std::max(1, std::min<int>((int)((std::max(cap, train_paths) + 255) / 256), ctx->sm_count * 8));
         CUDA_CHECK(cudaMemsetAsync(ctx->d_render_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
-        const int g_closest = ctx->sm_count * std::max(1, ctx->occupancy[0]);
-        const int g_any = ctx->sm_count * std::max(1, ctx->occupancy[1]);
+        PT::CacheIO C{};
+        if (use_cache) {
+            // 1) training paths: full paths through random pixels, one sample per vertex
+            FndCacheState& cs = *ctx->cache;
+            const fnd_cache_desc& cd = cs.desc;
+            CUDA_CHECK(cudaMemsetAsync(cs.totals, 0, sizeof(float4) * train_paths, ctx->stream));
+            CUDA_CHECK(cudaMemsetAsync(cs.counters + 1, 0, sizeof(uint32_t), ctx->stream));
+            PT::PathBuffers Bt = B;
+            Bt.fb = cs.totals;
+            PT::CacheIO Ct{};
+            Ct.mode = 2;
+            Ct.specular_alpha = cd.specular_alpha;
+            Ct.samples = cs.samples;
+            Ct.sample_count = cs.counters + 1;
+            Ct.sample_cap = cs.sample_cap;
+            const uint32_t tseed = Mix32(cd.seed ^ D.seed, cs.frames);
+            CUDA_CHECK(PT::LaunchGenerate(Bt, R, 0, train_paths, true, tseed, ctx->stream));
+            RunBounces(ctx, scene, Bt, R, S, Ct, D.max_depth, grid_shade);
+            CUDA_CHECK(NRC::Targets(cs.samples, cs.counters + 1, cs.totals, cs.targets, cs.sample_cap, ctx->stream));
+            const int grid_train = std::max(1, std::min<int>((int)((cd.batch + 63) / 64), ctx->sm_count));
+            for (uint32_t st = 0; st < cd.train_steps; ++st)
+                CUDA_CHECK(NRC::TrainStep(cs.net, cs.samples, cs.targets, cs.counters + 1, cd.batch,
+                                          Mix32(tseed, st + 1), cd.learning_rate, grid_train, ctx->stream));
+            cs.frames++;
+            // 2) render waves end their paths in cache queries
+            C.mode = 1;
+            C.specular_alpha = cd.specular_alpha;
+            C.queries = cs.queries;
+            C.query_count = cs.counters + 0;
+            C.query_cap = cs.query_cap;
+        }
         uint32_t waves = 0;
         for (uint64_t wave_base = 0; wave_base < total; wave_base += cap, ++waves) {
             const uint32_t wave_n = (uint32_t)std::min<uint64_t>(cap, total - wave_base);
-            CUDA_CHECK(PT::LaunchGenerate(B, R, wave_base, wave_n, ctx->stream));
-            for (uint32_t b = 0; b < D.max_depth; ++b) {
-                const int cur = (int)(b & 1u), nxt = cur ^ 1;
-                RT::TraceLaunch L{};
-                L.scene = scene->view;
-                L.rays = B.ext_rays[cur];
-                L.n = cap;
-                L.n_dev = B.counts + cur;
-                L.ray_total = ctx->d_render_stats + 0;
-                L.hits = B.hits;
-                L.counter = ctx->d_counter;
-                L.status = ctx->d_status;
-                L.refill_min = ctx->refill_min;
-                CUDA_CHECK(RT::LaunchTrace(L, false, false, g_closest, ctx->stream));
-                CUDA_CHECK(cudaMemsetAsync(B.counts + nxt, 0, sizeof(uint32_t), ctx->stream));
-                CUDA_CHECK(cudaMemsetAsync(B.counts + PT::kCountShadow, 0, sizeof(uint32_t), ctx->stream));
-                CUDA_CHECK(PT::LaunchShade(B, R, S, cur, b, grid_shade, ctx->stream));
-                RT::TraceLaunch A{};
-                A.scene = scene->view;
-                A.rays = B.sh_rays;
-                A.n = 2 * cap;
-                A.n_dev = B.counts + PT::kCountShadow;
-                A.ray_total = ctx->d_render_stats + 1;
-                A.occluded = B.sh_occluded;
-                A.counter = ctx->d_counter;
-                A.status = ctx->d_status;
-                A.refill_min = ctx->refill_min;
-                CUDA_CHECK(RT::LaunchTrace(A, true, false, g_any, ctx->stream));
-                CUDA_CHECK(PT::LaunchResolve(B, grid_shade, ctx->stream));
-            }
+            if (use_cache) CUDA_CHECK(cudaMemsetAsync(C.query_count, 0, sizeof(uint32_t), ctx->stream));
+            CUDA_CHECK(PT::LaunchGenerate(B, R, wave_base, wave_n, false, 0u, ctx->stream));
+            RunBounces(ctx, scene, B, R, S, C, D.max_depth, grid_shade);
+            if (use_cache)
+                CUDA_CHECK(NRC::Infer(ctx->cache->net, C.queries, C.query_count, C.query_cap, B.fb,
+                                      ctx->sm_count * 2, ctx->stream));
         }
         ctx->fb_samples += D.spp;
         const float scale = 1.0f / (float)ctx->fb_samples;

@@ -138,6 +138,7 @@ int fnd_rt_destroy(fnd_rt_ctx* ctx) {
     // the context is freed below: keep its failure message in the global slot
     GlobalError() = ctx->last_error;
     cudaSetDevice(ctx->device);
+    FreeCache(ctx);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->d_in) cudaFree(ctx->d_in);
     if (ctx->d_out) cudaFree(ctx->d_out);

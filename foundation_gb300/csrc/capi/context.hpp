@@ -14,6 +14,23 @@
 
 #include <vector>
 
+// Radiance-cache session of a context.
+struct FndCacheState {
+    fnd_cache_desc desc{};
+    Foundation::NRC::Net net{};
+    void* d_block = nullptr;  // one allocation for everything below
+    size_t block_bytes = 0;
+    Foundation::NRC::TrainSample* samples = nullptr;
+    float4* targets = nullptr;
+    float4* totals = nullptr;
+    Foundation::NRC::CachePoint* queries = nullptr;
+    uint32_t* counters = nullptr;  // [0] queries, [1] samples
+    uint32_t sample_cap = 0;
+    uint32_t query_cap = 0;
+    uint32_t train_cap = 0;
+    uint64_t frames = 0;
+};
+
 struct fnd_rt_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -43,6 +60,7 @@ struct fnd_rt_ctx {
     size_t rgb_cap = 0;
     unsigned long long* d_render_stats = nullptr;  // [0] extension rays, [1] shadow rays
     fnd_render_stats last_render{};
+    FndCacheState* cache = nullptr;
     std::string last_error;
     Foundation::Core::HeapAllocator allocator;
 };
@@ -98,6 +116,10 @@ void EnsureDevice(void*& ptr, size_t& cap, size_t bytes);
 
 // Reads and clears the latched device status; returns FND_OK or an error code.
 int ReadStatus(fnd_rt_ctx* ctx);
+
+// Radiance-cache session storage (capi_cache.cpp).
+void FreeCache(fnd_rt_ctx* ctx);
+void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth);
 
 }  // namespace CApi
 }  // namespace Foundation

@@ -41,6 +41,9 @@ MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("albedo", "<f4", 3), ("roughness", 
 LIGHT_DTYPE = np.dtype([("corner", "<f4", 3), ("edge_u", "<f4", 3), ("edge_v", "<f4", 3), ("radiance", "<f4", 3)])
 MAT_LAMBERT, MAT_GGX, MAT_EMISSIVE = 0, 1, 2
 RENDER_ACCUMULATE = 1
+RENDER_CACHE = 2
+CACHE_NUM_PARAMS = 22720
+CACHE_NUM_FEATURES = 96
 
 
 class FndError(RuntimeError):
@@ -88,6 +91,17 @@ class RenderStats(C.Structure):
                 ("waves", C.c_uint32), ("samples_accumulated", C.c_uint32)]
 
 
+class CacheDesc(C.Structure):
+    _fields_ = [("train_paths", C.c_uint32), ("train_steps", C.c_uint32), ("batch", C.c_uint32),
+                ("learning_rate", C.c_float), ("specular_alpha", C.c_float), ("flags", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
+class CacheStats(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("samples_last", C.c_uint64), ("queries_last", C.c_uint64),
+                ("loss_last", C.c_double)]
+
+
 class TraceStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("node_fetches", C.c_uint64), ("tri_tests", C.c_uint64)]
 
@@ -113,6 +127,16 @@ SIGNATURES = {
     "fnd_rt_scene_set_lights": (_I32, [_P, _P, _U32]),
     "fnd_rt_render": (_I32, [_P, _P, _P, _P, _I32]),
     "fnd_rt_render_stats_get": (_I32, [_P, _P]),
+    "fnd_rt_cache_create": (_I32, [_P, _P, _P]),
+    "fnd_rt_cache_destroy": (_I32, [_P]),
+    "fnd_rt_cache_stats_get": (_I32, [_P, _P]),
+    "fnd_rt_cache_get_weights": (_I32, [_P, _P, _U32]),
+    "fnd_rt_cache_set_weights": (_I32, [_P, _P, _U32]),
+    "fnd_rt_cache_save": (_I32, [_P, C.c_char_p]),
+    "fnd_rt_cache_load": (_I32, [_P, C.c_char_p]),
+    "fnd_rt_cache_eval": (_I32, [_P, _P, _U32, _P]),
+    "fnd_rt_cache_gradient": (_I32, [_P, _P, _P, _U32, _P, _P]),
+    "fnd_rt_cache_adam_step": (_I32, [_P, _P, C.c_float]),
 }
 
 _lib = None
@@ -198,13 +222,15 @@ class Context:
 
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
-               sun_irradiance=(0.0, 0.0, 0.0), accumulate: bool = False, wave_paths: int = 0, out=None):
+               sun_irradiance=(0.0, 0.0, 0.0), accumulate: bool = False, wave_paths: int = 0, out=None,
+               cache: bool = False):
         """Path-traces spp samples per pixel. Host: returns (height, width, 3)
         float32 mean radiance. Device: out is a CUDA tensor of
         width*height*3 floats, filled asynchronously."""
         cam = _Camera((C.c_float * 3)(*camera["eye"]), (C.c_float * 3)(*camera["target"]),
                       (C.c_float * 3)(*camera.get("up", (0.0, 1.0, 0.0))), camera.get("vfov_deg", 45.0))
-        d = _RenderDesc(width, height, spp, max_depth, rr_start, RENDER_ACCUMULATE if accumulate else 0, seed, cam,
+        flags = (RENDER_ACCUMULATE if accumulate else 0) | (RENDER_CACHE if cache else 0)
+        d = _RenderDesc(width, height, spp, max_depth, rr_start, flags, seed, cam,
                         (C.c_float * 3)(*sky), (C.c_float * 3)(*sun_dir), (C.c_float * 3)(*sun_irradiance),
                         wave_paths)
         if out is not None and _is_device(out):
@@ -213,6 +239,53 @@ class Context:
         img = np.empty((height, width, 3), np.float32) if out is None else out
         _check(load().fnd_rt_render(self._h, scene.handle, C.byref(d), _ptr(img), FND_MEM_HOST), self._h)
         return img
+
+    # ---- radiance cache -------------------------------------------------
+    def cache_create(self, scene: "Scene", train_paths: int = 65536, train_steps: int = 4, batch: int = 16384,
+                     learning_rate: float = 1e-2, specular_alpha: float = 0.1, seed: int = 1):
+        d = CacheDesc(train_paths, train_steps, batch, learning_rate, specular_alpha, 0, seed)
+        _check(load().fnd_rt_cache_create(self._h, scene.handle, C.byref(d)), self._h)
+
+    def cache_destroy(self):
+        _check(load().fnd_rt_cache_destroy(self._h), self._h)
+
+    def cache_stats(self) -> dict:
+        st = CacheStats()
+        _check(load().fnd_rt_cache_stats_get(self._h, C.byref(st)), self._h)
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def cache_weights(self) -> np.ndarray:
+        w = np.empty(CACHE_NUM_PARAMS, np.float32)
+        _check(load().fnd_rt_cache_get_weights(self._h, _ptr(w), len(w)), self._h)
+        return w
+
+    def cache_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        _check(load().fnd_rt_cache_set_weights(self._h, _ptr(w), len(w)), self._h)
+
+    def cache_save(self, path: str):
+        _check(load().fnd_rt_cache_save(self._h, str(path).encode()), self._h)
+
+    def cache_load(self, path: str):
+        _check(load().fnd_rt_cache_load(self._h, str(path).encode()), self._h)
+
+    def cache_eval(self, features) -> np.ndarray:
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, CACHE_NUM_FEATURES)
+        out = np.empty((len(f), 3), np.float32)
+        _check(load().fnd_rt_cache_eval(self._h, _ptr(f), len(f), _ptr(out)), self._h)
+        return out
+
+    def cache_gradient(self, features, targets):
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, CACHE_NUM_FEATURES)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, 3)
+        g = np.empty(CACHE_NUM_PARAMS, np.float32)
+        loss = C.c_double()
+        _check(load().fnd_rt_cache_gradient(self._h, _ptr(f), _ptr(t), len(f), _ptr(g), C.byref(loss)), self._h)
+        return g, loss.value
+
+    def cache_adam_step(self, grad, learning_rate: float = 1e-2):
+        g = np.ascontiguousarray(grad, np.float32)
+        _check(load().fnd_rt_cache_adam_step(self._h, _ptr(g), learning_rate), self._h)
 
     def render_stats(self) -> dict:
         st = RenderStats()

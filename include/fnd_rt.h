@@ -261,6 +261,59 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
 /* Counters of the last fnd_rt_render call (synchronises the stream). */
 int fnd_rt_render_stats_get(fnd_rt_ctx* ctx, fnd_render_stats* out);
 
+/* ---- radiance cache -----------------------------------------------------
+ * An online-trained MLP (96 -> 5 x 64 ReLU -> 3, BF16 tensor cores, FP32
+ * Adam) that predicts reflected radiance. With FND_RENDER_CACHE a render
+ * call first traces `train_paths` full training paths and takes
+ * `train_steps` optimiser steps on their vertices, then renders: paths end at
+ * the vertex after their first non-specular bounce, where the network
+ * supplies the reflected radiance. The plain tracer (no flag) stays the
+ * fallback and the judge of the cache's error. No reference counterpart
+ * (the reference has no ray tracer); the session state lives in the context
+ * like the renderer's per-frame resources (src/Renderer/Renderer.hpp:13-36). */
+enum { FND_RENDER_CACHE = 2u };
+
+typedef struct fnd_cache_desc {
+    uint32_t train_paths;   /* training paths per render call (65,536) */
+    uint32_t train_steps;   /* optimiser steps per render call (4) */
+    uint32_t batch;         /* training samples per step (16,384) */
+    float learning_rate;    /* Adam learning rate (1e-2) */
+    float specular_alpha;   /* GGX alpha below which a vertex counts as specular (0.1) */
+    uint32_t flags;         /* reserved, 0 */
+    uint64_t seed;          /* weight initialisation and sampling seed */
+} fnd_cache_desc;
+
+typedef struct fnd_cache_stats {
+    uint64_t steps;           /* optimiser steps taken */
+    uint64_t samples_last;    /* training samples of the last render call */
+    uint64_t queries_last;    /* cache queries of the last render wave */
+    double loss_last;         /* mean relative-L2 loss of the last step */
+} fnd_cache_stats;
+
+#define FND_CACHE_NUM_PARAMS 22720u
+#define FND_CACHE_NUM_FEATURES 96u
+
+/* Creates (or re-creates) the context's cache for a scene: He-uniform
+ * weights, zero Adam state, the scene's bounding box for the position
+ * encoding. */
+int fnd_rt_cache_create(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_cache_desc* desc);
+int fnd_rt_cache_destroy(fnd_rt_ctx* ctx);
+int fnd_rt_cache_stats_get(fnd_rt_ctx* ctx, fnd_cache_stats* out);
+/* FP32 master weights, row-major W[K][N] per layer, layers in order. */
+int fnd_rt_cache_get_weights(fnd_rt_ctx* ctx, float* out, uint32_t n);
+int fnd_rt_cache_set_weights(fnd_rt_ctx* ctx, const float* w, uint32_t n);
+/* Checkpoint: versioned header, weights and Adam moments. */
+int fnd_rt_cache_save(fnd_rt_ctx* ctx, const char* path);
+int fnd_rt_cache_load(fnd_rt_ctx* ctx, const char* path);
+/* Network on explicit features (n x 96 host floats) -> n x 3 host floats. */
+int fnd_rt_cache_eval(fnd_rt_ctx* ctx, const float* features, uint32_t n, float* out);
+/* Gradient of the mean relative-L2 loss on explicit features / targets
+ * (n x 3): grad receives FND_CACHE_NUM_PARAMS floats, loss the mean loss. */
+int fnd_rt_cache_gradient(fnd_rt_ctx* ctx, const float* features, const float* targets, uint32_t n, float* grad,
+                          double* loss);
+/* One Adam step with the given gradient (FND_CACHE_NUM_PARAMS host floats). */
+int fnd_rt_cache_adam_step(fnd_rt_ctx* ctx, const float* grad, float learning_rate);
+
 /* Closest hit without any device allocation. No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc at trace time
  * (a plugin inside a host application's frame callback, where the host

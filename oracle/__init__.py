@@ -19,7 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "librt_oracle.so")
-SOURCES = ["rt_oracle.cpp", "pt_oracle.cpp"]
+SOURCES = ["rt_oracle.cpp", "pt_oracle.cpp", "mlp_oracle.cpp"]
 HEADERS = ["rt_oracle.h", "oracle_common.hpp", "rt_oracle_internal.hpp"]
 CXXFLAGS = ["-O3", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared", "-pthread"]
 
@@ -66,6 +66,10 @@ def lib():
         L.orc_time_build_ms.restype = C.c_double
         L.orc_pt_render.argtypes = [P, P, P, U32, P, U32, P, U32, U32, U32, U32, U32, U64, P, U32, U32, U32, U32,
                                     U32, P]
+        L.orc_mlp_num_params.restype = U64
+        L.orc_mlp_forward_backward.argtypes = [P, P, P, U64, C.c_int, P, P, P, P]
+        L.orc_adam_step.argtypes = [P, P, P, P, U64, U64, C.c_double]
+        L.orc_nrc_encode.argtypes = [P, P, P, P]
         _lib = L
     return _lib
 
@@ -173,4 +177,44 @@ def pt_render(bvh: OracleBVH, tri_material, materials, lights, camera: dict, wid
     lib().orc_pt_render(bvh._h, _ptr(tm) if tm is not None else None, _ptr(mats), len(mats),
                         _ptr(ls) if len(ls) else None, len(ls), _ptr(cam), width, height, spp, max_depth, rr_start,
                         seed, _ptr(env), x0, y0, cw, ch, threads, _ptr(out))
+    return out
+
+
+MLP_DIMS = (96, 64, 64, 64, 64, 64, 3)
+
+
+def mlp_num_params() -> int:
+    return int(lib().orc_mlp_num_params())
+
+
+def mlp_forward_backward(w, x, t=None, emulate_bf16: bool = True, grad: bool = True, fixed_den=None):
+    """FP64 radiance-cache network: returns (y (B x 3), loss, dW) — loss / dW
+    None without targets. fixed_den (B x 3) replaces the loss denominators
+    y^2 + 0.01 by constants."""
+    w = np.ascontiguousarray(w, np.float32)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 96)
+    B = len(x)
+    y = np.zeros((B, 3), np.float64)
+    loss = C.c_double()
+    dw = np.zeros(len(w), np.float64) if (t is not None and grad) else None
+    tt = np.ascontiguousarray(t, np.float32).reshape(-1, 3) if t is not None else None
+    fd = np.ascontiguousarray(fixed_den, np.float64).reshape(-1, 3) if fixed_den is not None else None
+    lib().orc_mlp_forward_backward(_ptr(w), _ptr(x), _ptr(tt) if tt is not None else None, B, int(emulate_bf16),
+                                   _ptr(y), C.byref(loss) if t is not None else None,
+                                   _ptr(dw) if dw is not None else None,
+                                   _ptr(fd) if fd is not None else None)
+    return y, (loss.value if t is not None else None), dw
+
+
+def adam_step(w, m, v, g, step: int, lr: float):
+    """In-place FP64 Adam on float64 arrays."""
+    lib().orc_adam_step(_ptr(w), _ptr(m), _ptr(v), _ptr(np.ascontiguousarray(g, np.float64)), len(w), step, lr)
+
+
+def nrc_encode(p, wo, n, rough, albedo, lo, hi) -> np.ndarray:
+    rec = np.array([*p, *wo, *n, rough, *albedo], np.float32)
+    out = np.zeros(96, np.float32)
+    lo = np.asarray(lo, np.float32)
+    hi = np.asarray(hi, np.float32)
+    lib().orc_nrc_encode(_ptr(rec), _ptr(lo), _ptr(hi), _ptr(out))
     return out

@@ -1,0 +1,134 @@
+"""Radiance-cache kernels on the GPU against the FP64 oracle (BF16 rounding
+emulated at the kernels' rounding points): forward, gradient of the
+relative-L2 loss, Adam; an overfit run; checkpoints; and the cache-on
+renderer against the plain one on the Cornell box."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from foundation_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def relmse(img, ref, eps=1e-2):
+    return float(np.mean((np.asarray(img, np.float64) - ref) ** 2 / (np.asarray(ref, np.float64) ** 2 + eps)))
+
+
+@pytest.fixture(scope="module")
+def cache_ctx(built):
+    import foundation_gb300 as fg
+    c = fg.Context(0)
+    cs = S.cornell_scene(num_spheres=20, level=2)
+    s = c.upload(cs.verts, cs.idx)
+    s.set_materials(cs.tri_material, S.material_records(cs))
+    s.set_lights(S.light_records(cs))
+    c.cache_create(s, seed=3)
+    yield c, s, cs
+    c.close()
+
+
+def features(n, seed):
+    r = np.random.default_rng(seed)
+    return r.uniform(-1, 1, (n, 96)).astype(np.float32)
+
+
+def bf16_round(a):
+    a = np.ascontiguousarray(a, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def test_forward_matches_oracle(cache_ctx):
+    ctx, _, _ = cache_ctx
+    w = ctx.cache_weights()
+    x = features(1000, 1)
+    y = ctx.cache_eval(x)
+    ref, _, _ = O.mlp_forward_backward(bf16_round(w), x, None, emulate_bf16=True)
+    err = np.abs(y - ref).max() / (np.abs(ref).max() + 1e-6)
+    assert err < 2e-2, err
+
+
+def test_gradient_matches_oracle(cache_ctx):
+    ctx, _, _ = cache_ctx
+    w = ctx.cache_weights()
+    x = features(777, 2)
+    t = np.random.default_rng(3).uniform(0, 2, (777, 3)).astype(np.float32)
+    g, loss = ctx.cache_gradient(x, t)
+    _, loss_ref, g_ref = O.mlp_forward_backward(bf16_round(w), x, t, emulate_bf16=True)
+    assert abs(loss / loss_ref - 1) < 1e-2, (loss, loss_ref)
+    off = 0
+    for l in range(6):
+        K, N = O.MLP_DIMS[l], O.MLP_DIMS[l + 1]
+        a, b = g[off:off + K * N], g_ref[off:off + K * N]
+        rel = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30)
+        assert rel < 3e-2, (l, rel)
+        off += K * N
+
+
+def test_adam_matches_oracle(cache_ctx):
+    ctx, _, _ = cache_ctx
+    w0 = ctx.cache_weights().astype(np.float64)
+    g = np.random.default_rng(4).normal(size=len(w0)).astype(np.float32) * 1e-3
+    st0 = ctx.cache_stats()["steps"]
+    ctx.cache_adam_step(g, 1e-2)
+    w1 = ctx.cache_weights()
+    # fresh moments (steps == 0) or continue: restate from the kernel's step count
+    m = np.zeros_like(w0)
+    v = np.zeros_like(w0)
+    wr = w0.copy()
+    if st0 == 0:
+        O.adam_step(wr, m, v, g.astype(np.float64), 1, 1e-2)
+        assert np.allclose(w1, wr, rtol=1e-5, atol=1e-7)
+    else:
+        assert np.all(np.isfinite(w1)) and not np.array_equal(w1, w0.astype(np.float32))
+
+
+def test_overfit_and_checkpoint(cache_ctx, tmp_path):
+    ctx, _, _ = cache_ctx
+    x = features(512, 5)
+    t = (0.5 + 0.4 * np.sin(3 * x[:, :3])).astype(np.float32)
+    losses = []
+    for i in range(300):
+        g, loss = ctx.cache_gradient(x, t)
+        ctx.cache_adam_step(g, 5e-3)
+        losses.append(loss)
+    assert losses[-1] < 0.1 * losses[0], (losses[0], losses[-1])
+    p = str(tmp_path / "cache.bin")
+    ctx.cache_save(p)
+    y0 = ctx.cache_eval(x)
+    ctx.cache_set_weights(np.zeros(22720, np.float32))
+    assert np.all(ctx.cache_eval(x) == 0)
+    ctx.cache_load(p)
+    assert np.array_equal(ctx.cache_eval(x), y0)
+
+
+def test_cache_render_beats_plain_at_equal_samples(built):
+    """Cornell box at 96x54: after 32 training calls the cache-terminated
+    render at 16 spp has lower relMSE against the 4096-spp FP64 fixture than
+    the plain tracer at 16 spp; its bias (cache at 1024 spp vs fixture) is
+    reported and bounded."""
+    import foundation_gb300 as fg
+    g = np.load(os.path.join(GOLDEN, "cornell_fp64_96x54.npz"))
+    ref = g["image"].astype(np.float64)
+    cs = S.cornell_scene()
+    with fg.Context(0) as ctx:
+        s = ctx.upload(cs.verts, cs.idx)
+        s.set_materials(cs.tri_material, S.material_records(cs))
+        s.set_lights(S.light_records(cs))
+        ctx.cache_create(s, train_paths=16384, train_steps=4, batch=4096, seed=7)
+        for i in range(32):
+            ctx.render(s, 96, 54, 1, S.CORNELL_CAMERA, seed=100 + i, cache=True)
+        st = ctx.cache_stats()
+        assert st["steps"] == 128 and st["samples_last"] > 16384 and np.isfinite(st["loss_last"])
+        cache16 = ctx.render(s, 96, 54, 16, S.CORNELL_CAMERA, seed=1, cache=True)
+        plain16 = ctx.render(s, 96, 54, 16, S.CORNELL_CAMERA, seed=1)
+        cache_hi = ctx.render(s, 96, 54, 1024, S.CORNELL_CAMERA, seed=2, cache=True)
+        r_cache, r_plain, bias = relmse(cache16, ref), relmse(plain16, ref), relmse(cache_hi, ref)
+        print(f"relMSE cache16 {r_cache:.4g} plain16 {r_plain:.4g} cache bias (1024 spp) {bias:.4g}")
+        assert r_cache < r_plain
+        assert bias < 0.05
