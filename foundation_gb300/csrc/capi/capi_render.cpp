@@ -90,8 +90,8 @@ bool Normalize(double v[3]) {
 // One wave's bounce loop: extend -> shade -> shadow -> resolve, max_depth times.
 void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffers& B, const PT::RenderParams& R,
                 const PT::ShadeScene& S, const PT::CacheIO& C, uint32_t max_depth, int grid_shade) {
-    const int g_closest = ctx->sm_count * std::max(1, ctx->occupancy[0]);
-    const int g_any = ctx->sm_count * std::max(1, ctx->occupancy[1]);
+    const int g_closest = CApi::TraceGrid(ctx, ctx->trace_cfg, 0);
+    const int g_any = CApi::TraceGrid(ctx, ctx->trace_cfg, 1);
     for (uint32_t b = 0; b < max_depth; ++b) {
         const int cur = (int)(b & 1u), nxt = cur ^ 1;
         RT::TraceLaunch L{};
@@ -104,7 +104,7 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
         L.counter = ctx->d_counter;
         L.status = ctx->d_status;
         L.refill_min = ctx->refill_min;
-        CUDA_CHECK(RT::LaunchTrace(L, false, false, g_closest, ctx->stream));
+        CUDA_CHECK(RT::LaunchTraceConfigured(L, false, false, ctx->trace_cfg, g_closest, ctx->stream));
         CUDA_CHECK(cudaMemsetAsync(B.counts + nxt, 0, sizeof(uint32_t), ctx->stream));
         CUDA_CHECK(cudaMemsetAsync(B.counts + PT::kCountShadow, 0, sizeof(uint32_t), ctx->stream));
         CUDA_CHECK(PT::LaunchShade(B, R, S, C, cur, b, grid_shade, ctx->stream));
@@ -118,7 +118,7 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
         A.counter = ctx->d_counter;
         A.status = ctx->d_status;
         A.refill_min = ctx->refill_min;
-        CUDA_CHECK(RT::LaunchTrace(A, true, false, g_any, ctx->stream));
+        CUDA_CHECK(RT::LaunchTraceConfigured(A, true, false, ctx->trace_cfg, g_any, ctx->stream));
         CUDA_CHECK(PT::LaunchResolve(B, grid_shade, ctx->stream));
     }
 }

@@ -380,8 +380,8 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
         }
         if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
         const int variant = (any ? 1 : 0) + (stats ? 2 : 0);
-        const int grid = ctx->sm_count * std::max(1, ctx->occupancy[variant]);
-        CUDA_CHECK(RT::LaunchTrace(L, any, stats != nullptr, grid, ctx->stream));
+        const int grid = TraceGrid(ctx, ctx->trace_cfg, variant);
+        CUDA_CHECK(RT::LaunchTraceConfigured(L, any, stats != nullptr, ctx->trace_cfg, grid, ctx->stream));
         if (stats) {
             unsigned long long h[2] = {0, 0};
             CUDA_CHECK(cudaMemcpyAsync(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));

@@ -49,6 +49,7 @@ struct fnd_rt_ctx {
     void* d_out = nullptr;
     size_t d_out_cap = 0;
     int live_scenes = 0;
+    Foundation::RT::TraceConfig trace_cfg{};  // launch shape of the traversal kernels
     // path-tracing state: path buffers (capacity paths) and the frame buffer
     Foundation::PT::PathBuffers paths{};
     void* d_paths = nullptr;
@@ -116,6 +117,10 @@ void EnsureDevice(void*& ptr, size_t& cap, size_t bytes);
 
 // Reads and clears the latched device status; returns FND_OK or an error code.
 int ReadStatus(fnd_rt_ctx* ctx);
+
+// Persistent grid (SMs x resident blocks) of a traversal variant under a
+// launch shape (variant as in RT::TraceOccupancyFor).
+int TraceGrid(fnd_rt_ctx* ctx, const Foundation::RT::TraceConfig& cfg, int variant);
 
 // Radiance-cache session storage (capi_cache.cpp).
 void FreeCache(fnd_rt_ctx* ctx);

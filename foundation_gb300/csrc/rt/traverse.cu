@@ -1,5 +1,6 @@
 // traverse.cu — persistent closest-hit / any-hit traversal of the compressed
-// 8-wide BVH (sm_103a).
+// 8-wide BVH (sm_103a), for one scene (trace_kernel) or for a table of
+// (scene, ray batch, query kind) jobs in one launch (batch_kernel).
 //
 // Structure (after Aila & Laine, "Understanding the Efficiency of Ray
 // Traversal on GPUs", HPG 2009, and Ylitie, Karras & Laine, HPG 2017):
@@ -16,10 +17,13 @@
 //    to a thread-local array; the depth bound kMaxStack is checked on the
 //    host at scene upload and again on every push (a failed push latches
 //    kStatusStackOverflow and ends the ray instead of writing out of bounds).
-#include "traverse_launch.hpp"
-#include "traverse.cuh"
-
+// Block size, short-stack depth and the refill threshold are launch
+// parameters chosen by the autotuner (tune.cpp); every combination below is
+// compiled.
 #include <cfloat>
+
+#include "traverse.cuh"
+#include "traverse_launch.hpp"
 
 namespace Foundation {
 namespace RT {
@@ -29,18 +33,94 @@ namespace {
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr uint32_t kTriGroupFlag = 0x80000000u;
 
-template <bool kAny, bool kStats, int kShort>
-__global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L) {
+struct Common {
+    uint32_t* counter;
+    uint32_t* status;
+    unsigned long long* stats;
+    uint32_t refill_min;
+};
+
+// ---- work sources -----------------------------------------------------------
+// One scene, one ray array, one query kind for the whole launch.
+struct SingleSource {
+    DeviceScene scene;
+    const float4* rays;
+    void* hits;
+    uint8_t* occluded;
+    uint32_t n;
+    struct Lane {};
+    __device__ __forceinline__ void load(uint32_t id, float4& r0, float4& r1, Lane&) const {
+        r0 = __ldcs(rays + 2 * (size_t)id);
+        r1 = __ldcs(rays + 2 * (size_t)id + 1);
+    }
+    __device__ __forceinline__ const DeviceScene& scene_of(const Lane&) const { return scene; }
+    __device__ __forceinline__ bool any_of(const Lane&, bool dflt) const { return dflt; }
+    __device__ __forceinline__ void store(uint32_t id, const Lane&, bool any, uint32_t prim, float t) const {
+        if (any) {
+            __stcs(occluded + id, (uint8_t)(prim != FND_INVALID_ID ? 1 : 0));
+        } else {
+            const uint2 o = make_uint2(prim, prim == FND_INVALID_ID ? 0x7F800000u : __float_as_uint(t));
+            __stcs(reinterpret_cast<uint2*>(hits) + id, o);
+        }
+    }
+};
+
+// A job table; a global ray id is mapped to its job by binary search over
+// the prefix of ray counts (kept in shared memory when it fits).
+struct BatchSource {
+    const BatchJob* jobs;
+    const uint32_t* prefix;  // njobs + 1 entries
+    uint32_t njobs;
+    uint32_t n;
+    struct Lane {
+        uint32_t job;
+        uint32_t local;
+        DeviceScene scene;
+        bool any;
+    };
+    __device__ __forceinline__ void load(uint32_t id, float4& r0, float4& r1, Lane& ln) const {
+        uint32_t lo = 0, hi = njobs;  // prefix[lo] <= id < prefix[hi]
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (prefix[mid] <= id)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        ln.job = lo;
+        ln.local = id - prefix[lo];
+        const BatchJob& j = jobs[lo];
+        ln.scene = j.scene;
+        ln.any = j.any != 0;
+        r0 = __ldcs(j.rays + 2 * (size_t)ln.local);
+        r1 = __ldcs(j.rays + 2 * (size_t)ln.local + 1);
+    }
+    __device__ __forceinline__ const DeviceScene& scene_of(const Lane& ln) const { return ln.scene; }
+    __device__ __forceinline__ bool any_of(const Lane& ln, bool) const { return ln.any; }
+    __device__ __forceinline__ void store(uint32_t, const Lane& ln, bool any, uint32_t prim, float t) const {
+        const BatchJob& j = jobs[ln.job];
+        if (any) {
+            __stcs(static_cast<uint8_t*>(j.out) + ln.local, (uint8_t)(prim != FND_INVALID_ID ? 1 : 0));
+        } else {
+            const uint2 o = make_uint2(prim, prim == FND_INVALID_ID ? 0x7F800000u : __float_as_uint(t));
+            __stcs(reinterpret_cast<uint2*>(j.out) + ln.local, o);
+        }
+    }
+};
+
+// ---- the persistent traversal loop ----------------------------------------
+// kKind: 0 closest, 1 any, 2 per-lane (from the source).
+template <class Src, int kKind, bool kStats, int kShort, int kBlock>
+__device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack) {
     static_assert((kShort & (kShort - 1)) == 0, "short stack size must be a power of two");
-    __shared__ uint2 s_stack[kShort * kTraceBlock];
     uint2 l_stack[kMaxStack - kShort];
     const int tid = threadIdx.x;
     const uint32_t lane = tid & 31;
-    const uint32_t n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
-    if (L.ray_total && blockIdx.x == 0 && tid == 0) atomicAdd(L.ray_total, (unsigned long long)n);
+    const uint32_t n = src.n;
 
-    bool active = false, exhausted = false;
+    bool active = false, exhausted = false, any_hit = kKind == 1;
     uint32_t ray_id = 0;
+    typename Src::Lane ln{};
     RayState r;
     float best_t = 0.0f;
     uint32_t best_p = FND_INVALID_ID;
@@ -51,23 +131,25 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
     for (;;) {
         // ---- dynamic fetch -------------------------------------------------
         const uint32_t idle = __ballot_sync(kFull, !active);
-        if (!exhausted && idle != 0u && (__popc(idle) >= (int)L.refill_min || idle == kFull)) {
+        if (!exhausted && idle != 0u && (__popc(idle) >= (int)C.refill_min || idle == kFull)) {
             const uint32_t cnt = (uint32_t)__popc(idle);
             uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(L.counter, cnt);
+            if (lane == 0) base = atomicAdd(C.counter, cnt);
             base = __shfl_sync(kFull, base, 0);
             if (base + cnt >= n) exhausted = true;
             if (!active) {
                 const uint32_t id = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (id < n) {
-                    const float4 r0 = __ldcs(L.rays + 2 * (size_t)id);
-                    const float4 r1 = __ldcs(L.rays + 2 * (size_t)id + 1);
+                    float4 r0, r1;
+                    src.load(id, r0, r1, ln);
+                    if (kKind == 2) any_hit = src.any_of(ln, false);
                     r = setup_ray(r0, r1);
                     ray_id = id;
                     best_t = r.tmax;
                     best_p = FND_INVALID_ID;
                     ng_base = 0;
                     ng_group = (1u << 8) | (1u << r.oct);  // pseudo group holding the root in slot 0
+                    if (src.scene_of(ln).num_nodes == 0) ng_group = 0;  // empty scene: a miss
                     tg_mask = 0;
                     sp = 0;
                     active = true;
@@ -80,6 +162,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
         }
         if (!active) continue;
 
+        const DeviceScene& sc = src.scene_of(ln);
         bool overflow = false;
         // ---- one node --------------------------------------------------------
         if (ng_group & 0xFFu) {
@@ -91,28 +174,28 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
                 if (sp >= kMaxStack) {
                     overflow = true;
                 } else {
-                    const int s = (sp & (kShort - 1)) * kTraceBlock + tid;
+                    const int s = (sp & (kShort - 1)) * kBlock + tid;
                     if (sp >= kShort) l_stack[sp - kShort] = s_stack[s];
                     s_stack[s] = make_uint2(ng_base, ng_group);
                     sp++;
                 }
             }
-            if (child < L.scene.num_nodes) {
-                const NodeHits h = intersect_node(r, L.scene.nodes, child, best_t);
+            if (child < sc.num_nodes) {
+                const NodeHits h = intersect_node(r, sc.nodes, child, best_t);
                 if (kStats) st_nodes++;
                 ng_base = h.child_base;
                 ng_group = h.group;
                 tg_base = h.tri_base;
                 tg_mask = h.tris;
                 // a node's triangles must lie inside the triangle arrays
-                if (tg_mask && (uint64_t)tg_base + (uint64_t)(32 - __clz(tg_mask)) > L.scene.num_tris) {
-                    atomicOr(L.status, kStatusBadIndex);
+                if (tg_mask && (uint64_t)tg_base + (uint64_t)(32 - __clz(tg_mask)) > sc.num_tris) {
+                    atomicOr(C.status, kStatusBadIndex);
                     tg_mask = 0;
                     ng_group = 0;
                     sp = 0;
                 }
             } else {
-                atomicOr(L.status, kStatusBadIndex);
+                atomicOr(C.status, kStatusBadIndex);
                 ng_group = 0;
                 tg_mask = 0;
                 sp = 0;
@@ -123,14 +206,14 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
             const uint32_t k = (uint32_t)__ffs(tg_mask) - 1u;
             tg_mask &= tg_mask - 1u;
             const uint32_t ti = tg_base + k;
-            const float4 v0 = __ldg(L.scene.v0 + ti);
-            const float4 v1 = __ldg(L.scene.v1 + ti);
-            const float4 v2 = __ldg(L.scene.v2 + ti);
+            const float4 v0 = __ldg(sc.v0 + ti);
+            const float4 v1 = __ldg(sc.v1 + ti);
+            const float4 v2 = __ldg(sc.v2 + ti);
             if (kStats) st_tris++;
             float t;
             if (intersect_tri(r, v0, v1, v2, best_t, t)) {
                 const uint32_t pid = __float_as_uint(v0.w);
-                if (kAny) {
+                if (any_hit) {
                     best_t = t;
                     best_p = pid;
                     tg_mask = 0;
@@ -146,7 +229,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
         if ((ng_group & 0xFFu) == 0u && !overflow) {
             if (sp > 0) {
                 sp--;
-                const int s = (sp & (kShort - 1)) * kTraceBlock + tid;
+                const int s = (sp & (kShort - 1)) * kBlock + tid;
                 const uint2 e = s_stack[s];
                 if (sp >= kShort) s_stack[s] = l_stack[sp - kShort];
                 if (e.x & kTriGroupFlag) {
@@ -163,13 +246,8 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
             continue;
         }
         // ray finished (or aborted on overflow)
-        if (overflow) atomicOr(L.status, kStatusStackOverflow);
-        if (kAny) {
-            __stcs(L.occluded + ray_id, (uint8_t)(best_p != FND_INVALID_ID ? 1 : 0));
-        } else {
-            const uint2 o = make_uint2(best_p, best_p == FND_INVALID_ID ? 0x7F800000u : __float_as_uint(best_t));
-            __stcs(reinterpret_cast<uint2*>(L.hits) + ray_id, o);
-        }
+        if (overflow) atomicOr(C.status, kStatusStackOverflow);
+        src.store(ray_id, ln, any_hit, best_p, best_t);
         active = false;
     }
     if (kStats) {
@@ -178,10 +256,40 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceLaunch L)
             st_tris += __shfl_down_sync(kFull, st_tris, o);
         }
         if (lane == 0) {
-            atomicAdd(L.stats + 0, st_nodes);
-            atomicAdd(L.stats + 1, st_tris);
+            atomicAdd(C.stats + 0, st_nodes);
+            atomicAdd(C.stats + 1, st_tris);
         }
     }
+}
+
+// 36 resident warps per SM (9 blocks of 128 threads: at most 56 registers)
+// unless the block is 256 threads wide.
+constexpr int MinBlocks(int block) { return block == 256 ? 4 : 1152 / block; }
+
+template <bool kAny, bool kStats, int kShort, int kBlock>
+__global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const TraceLaunch L) {
+    __shared__ uint2 s_stack[kShort * kBlock];
+    SingleSource src;
+    src.scene = L.scene;
+    src.rays = L.rays;
+    src.hits = L.hits;
+    src.occluded = L.occluded;
+    src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
+    if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
+    const Common C{L.counter, L.status, L.stats, L.refill_min};
+    persistent_trace<SingleSource, kAny ? 1 : 0, kStats, kShort, kBlock>(src, C, s_stack);
+}
+
+template <int kShort, int kBlock>
+__global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) batch_kernel(const BatchLaunch B) {
+    __shared__ uint2 s_stack[kShort * kBlock];
+    BatchSource src;
+    src.jobs = B.jobs;
+    src.prefix = B.prefix;
+    src.njobs = B.njobs;
+    src.n = B.total;
+    const Common C{B.counter, B.status, nullptr, B.refill_min};
+    persistent_trace<BatchSource, 2, false, kShort, kBlock>(src, C, s_stack);
 }
 
 __global__ void fill_miss_kernel(uint2* hits, uint8_t* occluded, uint32_t cap, const uint32_t* n_dev) {
@@ -192,31 +300,59 @@ __global__ void fill_miss_kernel(uint2* hits, uint8_t* occluded, uint32_t cap, c
     if (occluded) occluded[i] = 0;
 }
 
-template <bool kAny, bool kStats>
-const void* kernel_ptr() {
-    return reinterpret_cast<const void*>(&trace_kernel<kAny, kStats, kTraceShortStack>);
+// ---- variant tables ---------------------------------------------------------
+template <bool kAny, bool kStats, int kShort, int kBlock>
+const void* trace_ptr() {
+    return reinterpret_cast<const void*>(&trace_kernel<kAny, kStats, kShort, kBlock>);
 }
 
-template <bool kAny, bool kStats>
-cudaError_t launch(const TraceLaunch& L, int grid, cudaStream_t stream) {
-    trace_kernel<kAny, kStats, kTraceShortStack><<<grid, kTraceBlock, 0, stream>>>(L);
-    return cudaGetLastError();
+int block_index(int block) { return block == 64 ? 0 : (block == 256 ? 2 : 1); }
+int short_index(int s) { return s == 4 ? 0 : (s == 16 ? 2 : 1); }
+
+template <bool kAny>
+const void* select_trace(const TraceConfig& c, bool stats) {
+    if (stats) return kAny ? trace_ptr<true, true, 8, 128>() : trace_ptr<false, true, 8, 128>();
+    static const void* table[3][3] = {
+        {trace_ptr<kAny, false, 4, 64>(), trace_ptr<kAny, false, 8, 64>(), trace_ptr<kAny, false, 16, 64>()},
+        {trace_ptr<kAny, false, 4, 128>(), trace_ptr<kAny, false, 8, 128>(), trace_ptr<kAny, false, 16, 128>()},
+        {trace_ptr<kAny, false, 4, 256>(), trace_ptr<kAny, false, 8, 256>(), trace_ptr<kAny, false, 16, 256>()},
+    };
+    return table[block_index(c.block)][short_index(c.short_stack)];
 }
+
+const void* select_batch(const TraceConfig& c) {
+    static const void* table[3][3] = {
+        {(const void*)&batch_kernel<4, 64>, (const void*)&batch_kernel<8, 64>, (const void*)&batch_kernel<16, 64>},
+        {(const void*)&batch_kernel<4, 128>, (const void*)&batch_kernel<8, 128>, (const void*)&batch_kernel<16, 128>},
+        {(const void*)&batch_kernel<4, 256>, (const void*)&batch_kernel<8, 256>, (const void*)&batch_kernel<16, 256>},
+    };
+    return table[block_index(c.block)][short_index(c.short_stack)];
+}
+
+int normalized_block(int b) { return b == 64 || b == 256 ? b : 128; }
 
 }  // namespace
 
-cudaError_t TraceOccupancy(int variant, int* blocks_per_sm) {
-    const void* fn = nullptr;
-    switch (variant) {
-        case 0: fn = kernel_ptr<false, false>(); break;
-        case 1: fn = kernel_ptr<true, false>(); break;
-        case 2: fn = kernel_ptr<false, true>(); break;
-        default: fn = kernel_ptr<true, true>(); break;
-    }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kTraceBlock, 0);
+bool ValidTraceConfig(const TraceConfig& c) {
+    return (c.block == 64 || c.block == 128 || c.block == 256) &&
+           (c.short_stack == 4 || c.short_stack == 8 || c.short_stack == 16) && c.refill_min >= 1 &&
+           c.refill_min <= 32 && c.blocks_per_sm >= 0 && c.blocks_per_sm <= 32;
 }
 
-cudaError_t LaunchTrace(const TraceLaunch& L, bool any, bool stats, int grid, cudaStream_t stream) {
+cudaError_t TraceOccupancy(int variant, int* blocks_per_sm) {
+    TraceConfig c{};
+    return TraceOccupancyFor(c, variant, blocks_per_sm);
+}
+
+cudaError_t TraceOccupancyFor(const TraceConfig& c, int variant, int* blocks_per_sm) {
+    const bool any = variant == 1 || variant == 3, stats = variant >= 2;
+    const void* fn = variant == 4 ? select_batch(c) : (any ? select_trace<true>(c, stats) : select_trace<false>(c, stats));
+    const int block = stats ? 128 : normalized_block(c.block);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, 0);
+}
+
+cudaError_t LaunchTraceConfigured(const TraceLaunch& L, bool any, bool stats, const TraceConfig& c, int grid,
+                                  cudaStream_t stream) {
     if (L.n == 0) return cudaSuccess;
     if (L.scene.num_nodes == 0) {
         const uint32_t threads = 256;
@@ -226,8 +362,28 @@ cudaError_t LaunchTrace(const TraceLaunch& L, bool any, bool stats, int grid, cu
     }
     cudaError_t e = cudaMemsetAsync(L.counter, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
-    if (any) return stats ? launch<true, true>(L, grid, stream) : launch<true, false>(L, grid, stream);
-    return stats ? launch<false, true>(L, grid, stream) : launch<false, false>(L, grid, stream);
+    const void* fn = any ? select_trace<true>(c, stats) : select_trace<false>(c, stats);
+    const int block = stats ? 128 : normalized_block(c.block);
+    TraceLaunch arg = L;
+    arg.refill_min = c.refill_min ? c.refill_min : L.refill_min;
+    void* params[] = {&arg};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), params, 0, stream);
+}
+
+cudaError_t LaunchTrace(const TraceLaunch& L, bool any, bool stats, int grid, cudaStream_t stream) {
+    TraceConfig c{};
+    c.refill_min = L.refill_min;
+    return LaunchTraceConfigured(L, any, stats, c, grid, stream);
+}
+
+cudaError_t LaunchBatch(const BatchLaunch& B, const TraceConfig& c, int grid, cudaStream_t stream) {
+    if (B.total == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+    BatchLaunch arg = B;
+    arg.refill_min = c.refill_min ? c.refill_min : B.refill_min;
+    void* params[] = {&arg};
+    return cudaLaunchKernel(select_batch(c), dim3(grid), dim3(normalized_block(c.block)), params, 0, stream);
 }
 
 }  // namespace RT

@@ -10,8 +10,8 @@
 namespace Foundation {
 namespace RT {
 
-constexpr int kTraceBlock = 128;     // threads per block (4 warps)
-constexpr int kTraceShortStack = 8;  // stack entries per thread kept in shared memory
+constexpr int kTraceBlock = 128;     // default threads per block (4 warps)
+constexpr int kTraceShortStack = 8;  // default stack entries per thread kept in shared memory
 
 struct TraceLaunch {
     DeviceScene scene;
@@ -27,9 +27,41 @@ struct TraceLaunch {
     uint32_t refill_min;        // refill a warp once this many lanes are idle
 };
 
-// variant: 0 closest, 1 any, 2 closest+stats, 3 any+stats
+// Launch shape of a traversal kernel (the autotuner's search space).
+struct TraceConfig {
+    int block = kTraceBlock;             // 64, 128 or 256 threads
+    int short_stack = kTraceShortStack;  // 4, 8 or 16 shared-memory stack entries per thread
+    uint32_t refill_min = 8;             // 1..32 idle lanes before a warp refills
+    int blocks_per_sm = 0;               // 0: as many as fit
+};
+bool ValidTraceConfig(const TraceConfig& c);
+
+// One job of a batched launch: a ray batch against one scene.
+struct BatchJob {
+    DeviceScene scene;
+    const float4* rays;
+    void* out;       // fnd_hit* (closest) or uint8_t* (any)
+    uint32_t n;
+    uint32_t any;    // 0 closest, 1 any
+};
+
+struct BatchLaunch {
+    const BatchJob* jobs;     // device job table
+    const uint32_t* prefix;   // device prefix sums of ray counts (njobs + 1)
+    uint32_t njobs;
+    uint32_t total;           // sum of ray counts
+    uint32_t* counter;
+    uint32_t* status;
+    uint32_t refill_min;
+};
+
+// variant: 0 closest, 1 any, 2 closest+stats, 3 any+stats, 4 batch
 cudaError_t TraceOccupancy(int variant, int* blocks_per_sm);
+cudaError_t TraceOccupancyFor(const TraceConfig& c, int variant, int* blocks_per_sm);
 cudaError_t LaunchTrace(const TraceLaunch& L, bool any, bool stats, int grid, cudaStream_t stream);
+cudaError_t LaunchTraceConfigured(const TraceLaunch& L, bool any, bool stats, const TraceConfig& c, int grid,
+                                  cudaStream_t stream);
+cudaError_t LaunchBatch(const BatchLaunch& B, const TraceConfig& c, int grid, cudaStream_t stream);
 
 }  // namespace RT
 }  // namespace Foundation

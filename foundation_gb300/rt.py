@@ -91,6 +91,27 @@ class RenderStats(C.Structure):
                 ("waves", C.c_uint32), ("samples_accumulated", C.c_uint32)]
 
 
+class TraceConfig(C.Structure):
+    _fields_ = [("block", C.c_uint32), ("short_stack", C.c_uint32), ("refill_min", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+    def as_dict(self):
+        return dict(block=self.block, short_stack=self.short_stack, refill_min=self.refill_min)
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("config", TraceConfig), ("ms", C.c_float)]
+
+
+class BatchJobDesc(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("rays", C.c_void_p), ("out", C.c_void_p), ("n", C.c_uint32),
+                ("kind", C.c_uint32)]
+
+
+QUERY_CLOSEST, QUERY_ANY = 0, 1
+BATCH_NO_GRAPH = 1
+
+
 class CacheDesc(C.Structure):
     _fields_ = [("train_paths", C.c_uint32), ("train_steps", C.c_uint32), ("batch", C.c_uint32),
                 ("learning_rate", C.c_float), ("specular_alpha", C.c_float), ("flags", C.c_uint32),
@@ -127,6 +148,13 @@ SIGNATURES = {
     "fnd_rt_scene_set_lights": (_I32, [_P, _P, _U32]),
     "fnd_rt_render": (_I32, [_P, _P, _P, _P, _I32]),
     "fnd_rt_render_stats_get": (_I32, [_P, _P]),
+    "fnd_rt_set_trace_config": (_I32, [_P, _P]),
+    "fnd_rt_get_trace_config": (_I32, [_P, _P]),
+    "fnd_rt_tune": (_I32, [_P, _P, _P, _U32, _U32, _U32, _P, _U32, _P, _P]),
+    "fnd_rt_batch_create": (_I32, [_P, _P, _U32, _U32, _P]),
+    "fnd_rt_batch_launch": (_I32, [_P]),
+    "fnd_rt_batch_tune": (_I32, [_P, _U32, _P, _U32, _P, _P]),
+    "fnd_rt_batch_destroy": (_I32, [_P]),
     "fnd_rt_cache_create": (_I32, [_P, _P, _P]),
     "fnd_rt_cache_destroy": (_I32, [_P]),
     "fnd_rt_cache_stats_get": (_I32, [_P, _P]),
@@ -239,6 +267,26 @@ class Context:
         img = np.empty((height, width, 3), np.float32) if out is None else out
         _check(load().fnd_rt_render(self._h, scene.handle, C.byref(d), _ptr(img), FND_MEM_HOST), self._h)
         return img
+
+    # ---- launch shape -------------------------------------------------
+    def set_trace_config(self, block: int = 128, short_stack: int = 8, refill_min: int = 8):
+        c = TraceConfig(block, short_stack, refill_min, 0)
+        _check(load().fnd_rt_set_trace_config(self._h, C.byref(c)), self._h)
+
+    def trace_config(self) -> dict:
+        c = TraceConfig()
+        _check(load().fnd_rt_get_trace_config(self._h, C.byref(c)), self._h)
+        return c.as_dict()
+
+    def tune(self, scene: "Scene", rays, kind: int = QUERY_CLOSEST, reps: int = 3):
+        """Times every launch shape on device rays; returns (best, table)."""
+        n = rays.numel() * rays.element_size() // 32
+        table = (TuneEntry * 64)()
+        tn = C.c_uint32()
+        best = TraceConfig()
+        _check(load().fnd_rt_tune(self._h, scene.handle, _ptr(rays), n, kind, reps, table, 64, C.byref(tn),
+                                  C.byref(best)), self._h)
+        return best.as_dict(), [dict(table[i].config.as_dict(), ms=table[i].ms) for i in range(tn.value)]
 
     # ---- radiance cache -------------------------------------------------
     def cache_create(self, scene: "Scene", train_paths: int = 65536, train_steps: int = 4, batch: int = 16384,
@@ -394,3 +442,43 @@ class PinnedBuffer:
         if getattr(self, "_p", None):
             load().fnd_rt_host_free(self._p)
             self._p = None
+
+
+class Batch:
+    """Batched traversal: jobs = [(scene, rays, out, kind)] with CUDA tensors
+    (rays: n x 8 float32; out: 2n int32 words for closest, n uint8 for any).
+    One persistent launch over all jobs, captured in a CUDA graph."""
+
+    def __init__(self, ctx: Context, jobs, graph: bool = True):
+        self.ctx = ctx
+        self._keep = jobs  # keeps the tensors alive
+        arr = (BatchJobDesc * len(jobs))()
+        for i, (scene, rays, out, kind) in enumerate(jobs):
+            n = rays.numel() * rays.element_size() // 32
+            arr[i] = BatchJobDesc(scene.handle.value, rays.data_ptr(), out.data_ptr(), n, kind)
+        h = C.c_void_p()
+        _check(load().fnd_rt_batch_create(ctx.handle, arr, len(jobs), 0 if graph else BATCH_NO_GRAPH, C.byref(h)),
+               ctx.handle)
+        self._h = h
+        self.total_rays = sum(r.numel() * r.element_size() // 32 for _, r, _, _ in jobs)
+
+    def launch(self):
+        _check(load().fnd_rt_batch_launch(self._h), self.ctx.handle)
+
+    def tune(self, reps: int = 2):
+        table = (TuneEntry * 64)()
+        tn = C.c_uint32()
+        best = TraceConfig()
+        _check(load().fnd_rt_batch_tune(self._h, reps, table, 64, C.byref(tn), C.byref(best)), self.ctx.handle)
+        return best.as_dict(), [dict(table[i].config.as_dict(), ms=table[i].ms) for i in range(tn.value)]
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            _check(load().fnd_rt_batch_destroy(self._h), self.ctx.handle)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -376,3 +376,54 @@ def write_obj(scene: Scene, path: str) -> None:
                 f.write(f"usemtl m{cur}\n")
             a, b, c = scene.idx[t] + 1
             f.write(f"f {a} {b} {c}\n")
+
+
+def log_uniform_ints(n: int, lo: int, hi: int, seed: int, stream_base: int) -> np.ndarray:
+    g = Pcg32Streams(seed, np.arange(stream_base, stream_base + n, dtype=np.uint64))
+    u = g.next_f64()
+    return np.round(_exp2_det(math.log2(lo) + u * (math.log2(hi) - math.log2(lo)))).astype(np.int64)
+
+
+def cube_camera_rays(n: int) -> np.ndarray:
+    """n coherent primary rays looking at the unit cube from (0.5, 0.5, 2.5)."""
+    w = max(1, int(math.ceil(math.sqrt(n))))
+    h = max(1, int(math.ceil(n / w)))
+    return camera_rays(w, h, eye=(0.5, 0.5, 2.5), target=(0.5, 0.5, 0.5), vfov_deg=40.0)[:n]
+
+
+def shadow_segments(n: int, seed: int, stream_base: int) -> np.ndarray:
+    """n any-hit queries: segments between two uniform points of the unit
+    cube (unnormalised direction p1 - p0, t in [0, 1])."""
+    g = Pcg32Streams(seed, np.arange(stream_base, stream_base + n, dtype=np.uint64))
+    p0 = np.stack([g.next_f64() for _ in range(3)], 1)
+    p1 = np.stack([g.next_f64() for _ in range(3)], 1)
+    rays = np.empty((n, 8), np.float32)
+    rays[:, 0:3] = p0
+    rays[:, 3] = 0.0
+    rays[:, 4:7] = p1 - p0
+    rays[:, 7] = 1.0
+    return rays
+
+
+def batch_workload(num_scenes: int = 256, seed: int = 2, tris=(1000, 500000), rays=(4096, 1 << 20)):
+    """The batched-traversal workload: `num_scenes` triangle soups in the unit
+    cube (log-uniform triangle counts, edge lengths log-uniform in [1e-3,
+    0.1]), each with a ray batch of log-uniform size: half coherent camera
+    rays, half uniform-random rays (closest hit), plus as many any-hit
+    shadow segments. Returns a list of dicts (scene, closest_rays, any_rays)."""
+    nt = log_uniform_ints(num_scenes, tris[0], tris[1], seed, 1 << 50)
+    nr = log_uniform_ints(num_scenes, rays[0], rays[1], seed, (1 << 50) + 4096)
+    out = []
+    tri_base = 0
+    ray_base = 1 << 44
+    for i in range(num_scenes):
+        sc = soup_scene(int(nt[i]), seed=seed, stream_base=tri_base)
+        tri_base += int(nt[i])
+        n = int(nr[i])
+        cam = cube_camera_rays(n // 2)
+        rnd = incoherent_rays(n - n // 2, (0, 0, 0), (1, 1, 1), seed=seed, stream_base=ray_base)
+        ray_base += n
+        sh = shadow_segments(n, seed, ray_base)
+        ray_base += n
+        out.append(dict(scene=sc, closest=np.concatenate([cam, rnd], 0), any=sh))
+    return out

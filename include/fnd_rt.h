@@ -182,6 +182,63 @@ typedef struct fnd_rt_trace_stats {
 int fnd_rt_trace_closest_stats(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays,
                                uint32_t n, fnd_hit* out, int mem, fnd_rt_trace_stats* stats);
 
+/* ---- launch shape and autotuning ----------------------------------------
+ * Block size, shared-memory short-stack depth and the refill threshold of
+ * the persistent traversal kernels. A context starts with the defaults
+ * (128, 8, 8); fnd_rt_tune times every combination on a caller's ray batch
+ * and reports the table and the fastest. No reference counterpart: the
+ * reference has no compute dispatch to tune (src/Platform/RHI/Command.hpp:32-116). */
+typedef struct fnd_rt_trace_config {
+    uint32_t block;        /* 64, 128 or 256 threads */
+    uint32_t short_stack;  /* 4, 8 or 16 entries per thread */
+    uint32_t refill_min;   /* 1..32 idle lanes before a warp refills */
+    uint32_t reserved;
+} fnd_rt_trace_config;
+
+typedef struct fnd_rt_tune_entry {
+    fnd_rt_trace_config config;
+    float ms;              /* best-of-reps kernel time (CUDA events) */
+} fnd_rt_tune_entry;
+
+enum { FND_QUERY_CLOSEST = 0, FND_QUERY_ANY = 1 };
+
+int fnd_rt_set_trace_config(fnd_rt_ctx* ctx, const fnd_rt_trace_config* config);
+int fnd_rt_get_trace_config(const fnd_rt_ctx* ctx, fnd_rt_trace_config* out);
+/* Times every launch shape on n device rays (FND_QUERY_CLOSEST / _ANY) with
+ * `reps` timed runs each; fills up to table_cap entries, *table_n, *best
+ * (the context keeps its own config; apply *best with fnd_rt_set_trace_config). */
+int fnd_rt_tune(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n, uint32_t kind,
+                uint32_t reps, fnd_rt_tune_entry* table, uint32_t table_cap, uint32_t* table_n,
+                fnd_rt_trace_config* best);
+
+/* ---- batched traversal --------------------------------------------------
+ * Many scenes and ray batches of uneven sizes in ONE persistent launch: every
+ * job is (scene, device rays, device output, query kind); a global work
+ * counter hands rays of all jobs to the warps. The launch (counter reset +
+ * kernel) is captured once in a CUDA graph and replayed by
+ * fnd_rt_batch_launch. */
+typedef struct fnd_rt_batch fnd_rt_batch;
+
+typedef struct fnd_rt_batch_job {
+    const fnd_rt_scene* scene;
+    const fnd_ray* rays;  /* device, 16-byte aligned */
+    void* out;            /* device: fnd_hit[n] (closest) or uint8_t[n] (any) */
+    uint32_t n;
+    uint32_t kind;        /* FND_QUERY_CLOSEST or FND_QUERY_ANY */
+} fnd_rt_batch_job;
+
+enum { FND_BATCH_NO_GRAPH = 1u };
+
+int fnd_rt_batch_create(fnd_rt_ctx* ctx, const fnd_rt_batch_job* jobs, uint32_t njobs, uint32_t flags,
+                        fnd_rt_batch** out_batch);
+/* Enqueues the batch on the context stream (asynchronous; fnd_rt_sync waits). */
+int fnd_rt_batch_launch(fnd_rt_batch* batch);
+/* Times every launch shape on the batch, re-captures its graph with the
+ * fastest and returns it (table as in fnd_rt_tune). */
+int fnd_rt_batch_tune(fnd_rt_batch* batch, uint32_t reps, fnd_rt_tune_entry* table, uint32_t table_cap,
+                      uint32_t* table_n, fnd_rt_trace_config* best);
+int fnd_rt_batch_destroy(fnd_rt_batch* batch);
+
 /* ---- path tracing ------------------------------------------------------
  * The reference's per-frame entry is Renderer::Draw
  * (src/Renderer/Renderer.cpp:367-401): update the camera, record, submit,
