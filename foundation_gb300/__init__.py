@@ -1,6 +1,8 @@
 """Foundation path-tracer pass for GB300 (sm_103a): BVH traversal, wavefront
 path tracing and an online-trained radiance cache behind the C ABI of
 include/fnd_rt.h. See ``foundation_gb300.rt`` for the binding."""
-from .rt import (Context, FndError, HIT_DTYPE, INVALID_ID, PinnedBuffer, Scene, load)  # noqa: F401
+from .rt import (Batch, Context, FndError, HIT_DTYPE, INVALID_ID, LIGHT_DTYPE, MATERIAL_DTYPE, PinnedBuffer,  # noqa
+                 QUERY_ANY, QUERY_CLOSEST, Scene, load)
 
-__all__ = ["Context", "Scene", "FndError", "HIT_DTYPE", "INVALID_ID", "PinnedBuffer", "load"]
+__all__ = ["Batch", "Context", "Scene", "FndError", "HIT_DTYPE", "INVALID_ID", "LIGHT_DTYPE", "MATERIAL_DTYPE",
+           "PinnedBuffer", "QUERY_ANY", "QUERY_CLOSEST", "load"]

@@ -28,7 +28,7 @@ void FreeCache(fnd_rt_ctx* ctx) {
 void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth) {
     FndCacheState& c = *ctx->cache;
     const uint32_t train = c.desc.train_paths;
-    const uint32_t samples = train * max_depth;
+    const uint32_t samples = train * std::min(max_depth, 16u);
     if (c.d_block && c.query_cap >= query_cap && c.sample_cap >= samples && c.train_cap >= train) return;
     const uint32_t qcap = std::max(query_cap, c.query_cap), scap = std::max(samples, c.sample_cap);
     const size_t P = NRC::kNumParams;
@@ -36,8 +36,7 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
         sizeof(uint16_t) * NRC::kFwdElems, sizeof(uint16_t) * NRC::kBwdElems,
         4 * P, 4 * P, 4 * P, 4 * P,            // master, m, v, grad
         sizeof(double) * 4,                    // loss
-        sizeof(NRC::TrainSample) * scap, sizeof(float4) * scap, sizeof(float4) * train,
-        sizeof(NRC::CachePoint) * qcap, 256,
+        sizeof(NRC::TrainSample) * scap, sizeof(float4) * scap, sizeof(NRC::CachePoint) * qcap, 256,
     };
     size_t total = 0;
     for (size_t sz : sizes) total += Align256(sz);
@@ -71,9 +70,8 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
     c.net = net;
     c.samples = reinterpret_cast<NRC::TrainSample*>(take(sizes[7]));
     c.targets = reinterpret_cast<float4*>(take(sizes[8]));
-    c.totals = reinterpret_cast<float4*>(take(sizes[9]));
-    c.queries = reinterpret_cast<NRC::CachePoint*>(take(sizes[10]));
-    c.counters = reinterpret_cast<uint32_t*>(take(sizes[11]));
+    c.queries = reinterpret_cast<NRC::CachePoint*>(take(sizes[9]));
+    c.counters = reinterpret_cast<uint32_t*>(take(sizes[10]));
     c.d_block = base;
     c.block_bytes = total;
     c.query_cap = qcap;
@@ -275,6 +273,33 @@ int fnd_rt_cache_gradient(fnd_rt_ctx* ctx, const float* features, const float* t
         CUDA_CHECK(cudaMemcpyAsync(&l, c.net.loss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
         if (loss) *loss = l / (3.0 * n);
+    });
+}
+
+int fnd_rt_cache_encode(fnd_rt_ctx* ctx, const float* points, uint32_t n, float* out) {
+    if (!ctx) return FND_ERR_INVALID_ARG;
+    return Guard(ctx, [&] {
+        FndCacheState& c = NeedCache(ctx);
+        CHECK(n == 0 || (points && out));
+        if (!n) return;
+        std::vector<NRC::CachePoint> pts(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            const float* r = points + 13 * (size_t)i;
+            pts[i].p_rough = make_float4(r[0], r[1], r[2], r[9]);
+            pts[i].wo_aux = make_float4(r[3], r[4], r[5], 0.f);
+            pts[i].n_pad = make_float4(r[6], r[7], r[8], 0.f);
+            pts[i].albedo = make_float4(r[10], r[11], r[12], 0.f);
+            pts[i].beta = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        CUDA_CHECK(cudaSetDevice(ctx->device));
+        const size_t pb = sizeof(NRC::CachePoint) * n, ob = 4ull * n * NRC::kIn;
+        EnsureDevice(ctx->d_in, ctx->d_in_cap, pb);
+        EnsureDevice(ctx->d_out, ctx->d_out_cap, ob);
+        CUDA_CHECK(cudaMemcpyAsync(ctx->d_in, pts.data(), pb, cudaMemcpyHostToDevice, ctx->stream));
+        CUDA_CHECK(NRC::EncodeRaw(c.net, static_cast<const NRC::CachePoint*>(ctx->d_in), n,
+                                  static_cast<float*>(ctx->d_out), ctx->stream));
+        CUDA_CHECK(cudaMemcpyAsync(out, ctx->d_out, ob, cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });
 }
 

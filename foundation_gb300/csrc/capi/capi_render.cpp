@@ -234,7 +234,7 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         CHECK_CODE(!use_cache || ctx->cache != nullptr, FND_ERR_INVALID_ARG,
                    "FND_RENDER_CACHE needs a cache (fnd_rt_cache_create)");
         const uint32_t train_paths = use_cache ? ctx->cache->desc.train_paths : 0u;
-        EnsurePathBuffers(ctx, std::max(cap, train_paths));
+        EnsurePathBuffers(ctx, cap);
         if (use_cache) CApi::EnsureCacheBuffers(ctx, cap, D.max_depth);
         // frame buffer (restart unless accumulating into a frame of the same size)
         const bool accumulate = (D.flags & FND_RENDER_ACCUMULATE) && ctx->d_fb && ctx->fb_width == D.width &&
@@ -293,28 +293,28 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         S.num_materials = scene->num_materials;
         CHECK_CODE(scene->info.num_tris == 0 || S.tri_shade != nullptr, FND_ERR_INVALID_SCENE, "scene has no shading data");
         PT::PathBuffers& B = ctx->paths;
-        const int grid_shade =
-            std::max(1, std::min<int>((int)((std::max(cap, train_paths) + 255) / 256), ctx->sm_count * 8));
+        const int grid_shade = std::max(1, std::min<int>((int)((cap + 255) / 256), ctx->sm_count * 8));
         CUDA_CHECK(cudaMemsetAsync(ctx->d_render_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
         PT::CacheIO C{};
         if (use_cache) {
-            // 1) training paths: full paths through random pixels, one sample per vertex
+            // 1) training paths: full paths through random pixels, one thread
+            //    each, one training sample (with its target) per vertex
             FndCacheState& cs = *ctx->cache;
             const fnd_cache_desc& cd = cs.desc;
-            CUDA_CHECK(cudaMemsetAsync(cs.totals, 0, sizeof(float4) * train_paths, ctx->stream));
             CUDA_CHECK(cudaMemsetAsync(cs.counters + 1, 0, sizeof(uint32_t), ctx->stream));
-            PT::PathBuffers Bt = B;
-            Bt.fb = cs.totals;
-            PT::CacheIO Ct{};
-            Ct.mode = 2;
-            Ct.specular_alpha = cd.specular_alpha;
-            Ct.samples = cs.samples;
-            Ct.sample_count = cs.counters + 1;
-            Ct.sample_cap = cs.sample_cap;
+            PT::TrainPathsArgs T{};
+            T.scene = scene->view;
+            T.R = R;
+            T.S = S;
+            T.n = train_paths;
             const uint32_t tseed = Mix32(cd.seed ^ D.seed, cs.frames);
-            CUDA_CHECK(PT::LaunchGenerate(Bt, R, 0, train_paths, true, tseed, ctx->stream));
-            RunBounces(ctx, scene, Bt, R, S, Ct, D.max_depth, grid_shade);
-            CUDA_CHECK(NRC::Targets(cs.samples, cs.counters + 1, cs.totals, cs.targets, cs.sample_cap, ctx->stream));
+            T.seed = tseed;
+            T.samples = cs.samples;
+            T.targets = cs.targets;
+            T.sample_count = cs.counters + 1;
+            T.sample_cap = cs.sample_cap;
+            T.status = ctx->d_status;
+            CUDA_CHECK(PT::LaunchTrainingPaths(T, ctx->stream));
             const int grid_train = std::max(1, std::min<int>((int)((cd.batch + 63) / 64), ctx->sm_count));
             for (uint32_t st = 0; st < cd.train_steps; ++st)
                 CUDA_CHECK(NRC::TrainStep(cs.net, cs.samples, cs.targets, cs.counters + 1, cd.batch,
@@ -331,7 +331,7 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         for (uint64_t wave_base = 0; wave_base < total; wave_base += cap, ++waves) {
             const uint32_t wave_n = (uint32_t)std::min<uint64_t>(cap, total - wave_base);
             if (use_cache) CUDA_CHECK(cudaMemsetAsync(C.query_count, 0, sizeof(uint32_t), ctx->stream));
-            CUDA_CHECK(PT::LaunchGenerate(B, R, wave_base, wave_n, false, 0u, ctx->stream));
+            CUDA_CHECK(PT::LaunchGenerate(B, R, wave_base, wave_n, ctx->stream));
             RunBounces(ctx, scene, B, R, S, C, D.max_depth, grid_shade);
             if (use_cache)
                 CUDA_CHECK(NRC::Infer(ctx->cache->net, C.queries, C.query_count, C.query_cap, B.fb,

@@ -22,7 +22,6 @@ struct FndCacheState {
     size_t block_bytes = 0;
     Foundation::NRC::TrainSample* samples = nullptr;
     float4* targets = nullptr;
-    float4* totals = nullptr;
     Foundation::NRC::CachePoint* queries = nullptr;
     uint32_t* counters = nullptr;  // [0] queries, [1] samples
     uint32_t sample_cap = 0;

@@ -83,29 +83,36 @@ __device__ __forceinline__ uint32_t b_addr(const uint16_t* m, int stride, int n0
 // 12 sine/cosine bands per normalised position axis (sin / cos of 2^k pi p),
 // then outgoing direction, normal, roughness, albedo, zero padding to 96.
 // `half` 0 writes features 0..47, `half` 1 features 48..95.
+__device__ __forceinline__ void encode_axis(float u, uint16_t* out) {
+    // bands k = 0..11: sin / cos of 2^k pi u. Bands 0, 4, 8 come from
+    // sincospif; the three after each from the double-angle identities
+    // (at most three doublings: error below 1e-6, far under a bf16 step).
+#pragma unroll
+    for (int k0 = 0; k0 < 12; k0 += 4) {
+        float s, c;
+        sincospif(ldexpf(u, k0), &s, &c);
+#pragma unroll
+        for (int k = k0; k < k0 + 4; ++k) {
+            out[2 * k] = bf16_bits(s);
+            out[2 * k + 1] = bf16_bits(c);
+            const float s2 = 2.0f * s * c, c2 = (c - s) * (c + s);
+            s = s2;
+            c = c2;
+        }
+    }
+}
+
 __device__ __forceinline__ void encode_half(const CachePoint& c, const float lo[3], const float hi[3], int half,
                                             uint16_t* row) {
     const float p[3] = {c.p_rough.x, c.p_rough.y, c.p_rough.z};
     if (half == 0) {
         for (int a = 0; a < 2; ++a) {
             const float ext = hi[a] - lo[a];
-            const float u = ext > 0.0f ? (p[a] - lo[a]) / ext : 0.0f;
-            for (int k = 0; k < 12; ++k) {
-                float s, co;
-                sincospif(ldexpf(u, k), &s, &co);
-                row[24 * a + 2 * k] = bf16_bits(s);
-                row[24 * a + 2 * k + 1] = bf16_bits(co);
-            }
+            encode_axis(ext > 0.0f ? (p[a] - lo[a]) / ext : 0.0f, row + 24 * a);
         }
     } else {
         const float ext = hi[2] - lo[2];
-        const float u = ext > 0.0f ? (p[2] - lo[2]) / ext : 0.0f;
-        for (int k = 0; k < 12; ++k) {
-            float s, co;
-            sincospif(ldexpf(u, k), &s, &co);
-            row[48 + 2 * k] = bf16_bits(s);
-            row[48 + 2 * k + 1] = bf16_bits(co);
-        }
+        encode_axis(ext > 0.0f ? (p[2] - lo[2]) / ext : 0.0f, row + 48);
         const float rest[10] = {c.wo_aux.x, c.wo_aux.y, c.wo_aux.z, c.n_pad.x, c.n_pad.y, c.n_pad.z,
                                 c.p_rough.w, c.albedo.x, c.albedo.y, c.albedo.z};
         for (int i = 0; i < 10; ++i) row[72 + i] = bf16_bits(rest[i]);
@@ -159,6 +166,65 @@ __device__ __forceinline__ void forward16(const uint16_t* fwd, uint16_t* const* 
             }
         }
         __syncwarp();
+    }
+}
+
+// Inference forward of one warp's 16 rows with the activations kept in
+// registers: the FP32 accumulator fragment of one layer, after ReLU and
+// BF16 rounding, is exactly the A fragment of the next (same values as the
+// shared-memory round trip of forward16). x: input rows (stride 104).
+__device__ __forceinline__ void forward16_reg(const uint16_t* fwd, const uint16_t* x, int lane, float* y) {
+    uint32_t a[4][4];
+    float acc[8][4];
+    // layer 0 from shared memory
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.0f;
+    {
+        const uint16_t* W = fwd + FwdOffset(0);
+#pragma unroll
+        for (int kk = 0; kk < kIn / 16; ++kk) {
+            uint32_t af[4];
+            ldsm4(af, a_addr(x, kStrideX, 0, 16 * kk, lane));
+#pragma unroll
+            for (int np = 0; np < 4; ++np) {
+                uint32_t b[4];
+                ldsm4(b, b_addr(W, kIn + kPad, 16 * np, 16 * kk, lane));
+                mma(acc[2 * np], af, b[0], b[1]);
+                mma(acc[2 * np + 1], af, b[2], b[3]);
+            }
+        }
+    }
+#pragma unroll 1
+    for (int l = 1; l < kLayers; ++l) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            a[kk][0] = pack2(fmaxf(acc[2 * kk][0], 0.f), fmaxf(acc[2 * kk][1], 0.f));
+            a[kk][1] = pack2(fmaxf(acc[2 * kk][2], 0.f), fmaxf(acc[2 * kk][3], 0.f));
+            a[kk][2] = pack2(fmaxf(acc[2 * kk + 1][0], 0.f), fmaxf(acc[2 * kk + 1][1], 0.f));
+            a[kk][3] = pack2(fmaxf(acc[2 * kk + 1][2], 0.f), fmaxf(acc[2 * kk + 1][3], 0.f));
+        }
+        const uint16_t* W = fwd + FwdOffset(l);
+        if (l + 1 < kLayers) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.0f;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+                for (int np = 0; np < 4; ++np) {
+                    uint32_t b[4];
+                    ldsm4(b, b_addr(W, kWidth + kPad, 16 * np, 16 * kk, lane));
+                    mma(acc[2 * np], a[kk], b[0], b[1]);
+                    mma(acc[2 * np + 1], a[kk], b[2], b[3]);
+                }
+        } else {
+            y[0] = y[1] = y[2] = y[3] = 0.0f;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                uint32_t b[2];
+                ldsm2(b, b_addr(W, kWidth + kPad, 0, 16 * kk, lane & 15));
+                mma(y, a[kk], b[0], b[1]);
+            }
+        }
     }
 }
 
@@ -342,30 +408,30 @@ __global__ void __launch_bounds__(kThreads) train_kernel(const TrainArgs A) {
 }
 
 // ---- inference ----------------------------------------------------------
+constexpr int kInferWarps = 8;
+
 template <bool kRaw>
-__global__ void __launch_bounds__(kThreads) infer_kernel(const Net net, const CachePoint* pts, const uint32_t* count,
-                                                         uint32_t capacity, float4* fb, const float* raw_feats,
-                                                         uint32_t raw_n, float* raw_out) {
+__global__ void __launch_bounds__(32 * kInferWarps) infer_kernel(const Net net, const CachePoint* pts,
+                                                                 const uint32_t* count, uint32_t capacity,
+                                                                 float4* fb, const float* raw_feats, uint32_t raw_n,
+                                                                 float* raw_out) {
     extern __shared__ __align__(16) uint16_t smem[];
     uint16_t* s_fwd = smem;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3;
-    uint16_t* wbuf = s_fwd + kFwdElems + warp * (16 * kStrideX + 16 * kStrideH * 2);
-    uint16_t* act[kLayers];
-    act[0] = wbuf;
-    for (int l = 1; l < kLayers; ++l) act[l] = wbuf + 16 * kStrideX + ((l - 1) & 1) * 16 * kStrideH;
+    uint16_t* xbuf = s_fwd + kFwdElems + warp * (16 * kStrideX);
     {
         const int4* src = reinterpret_cast<const int4*>(net.fwd);
         int4* dst = reinterpret_cast<int4*>(s_fwd);
-        for (int i = tid; i < kFwdElems / 8; i += kThreads) dst[i] = src[i];
+        for (int i = tid; i < kFwdElems / 8; i += 32 * kInferWarps) dst[i] = src[i];
     }
     __syncthreads();
     const uint32_t n = kRaw ? raw_n : min(*count, capacity);
     const uint32_t tiles = (n + 15) / 16;
-    for (uint32_t tile = blockIdx.x * kWarps + warp; tile < tiles; tile += gridDim.x * kWarps) {
+    for (uint32_t tile = blockIdx.x * kInferWarps + warp; tile < tiles; tile += gridDim.x * kInferWarps) {
         const int row = lane >> 1, half = lane & 1;
         const uint32_t q = tile * 16 + row;
-        uint16_t* xr = act[0] + row * kStrideX;
+        uint16_t* xr = xbuf + row * kStrideX;
         if (q >= n) {
             for (int i = half * 48; i < half * 48 + 48; ++i) xr[i] = 0;
         } else if (kRaw) {
@@ -375,7 +441,7 @@ __global__ void __launch_bounds__(kThreads) infer_kernel(const Net net, const Ca
         }
         __syncwarp();
         float y[4];
-        forward16(s_fwd, act, 0, lane, y);
+        forward16_reg(s_fwd, xbuf, lane, y);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const uint32_t qr = tile * 16 + g + 8 * h;
@@ -401,22 +467,16 @@ __global__ void __launch_bounds__(kThreads) infer_kernel(const Net net, const Ca
     }
 }
 
-__global__ void targets_kernel(const TrainSample* smp, const uint32_t* count, uint32_t capacity, const float4* totals,
-                               float4* targets) {
-    const uint32_t n = min(*count, capacity);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const TrainSample s = smp[i];
-        const uint32_t slot = __float_as_uint(s.pt.wo_aux.w);
-        const float4 tot = totals[slot];
-        const float b[3] = {s.pt.beta.x, s.pt.beta.y, s.pt.beta.z};
-        const float d[3] = {tot.x - s.before.x, tot.y - s.before.y, tot.z - s.before.z};
-        float o[3];
-        bool ok = true;
-        for (int c = 0; c < 3; ++c) {
-            ok = ok && b[c] > 1e-8f;
-            o[c] = b[c] > 1e-8f ? fmaxf(d[c], 0.0f) / b[c] : 0.0f;
-        }
-        targets[i] = make_float4(o[0], o[1], o[2], ok ? 1.0f : 0.0f);
+// Encoding hook: the 96 features of n cache points (tests).
+__global__ void encode_kernel(const Net net, const CachePoint* pts, uint32_t n, float* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint16_t row[kIn];
+    encode_half(pts[i], net.lo, net.hi, 0, row);
+    encode_half(pts[i], net.lo, net.hi, 1, row);
+    for (int k = 0; k < kIn; ++k) {
+        const uint32_t u = (uint32_t)row[k] << 16;
+        out[(size_t)i * kIn + k] = __uint_as_float(u);
     }
 }
 
@@ -471,9 +531,7 @@ size_t train_smem() {
                                6 * (size_t)kTileRows * kStrideH) +
            sizeof(float) * 4 * kTileRows;
 }
-size_t infer_smem() {
-    return sizeof(uint16_t) * ((size_t)kFwdElems + (size_t)kWarps * (16 * kStrideX + 2 * 16 * kStrideH));
-}
+size_t infer_smem() { return sizeof(uint16_t) * ((size_t)kFwdElems + (size_t)kInferWarps * 16 * kStrideX); }
 
 template <typename K>
 cudaError_t allow_smem(K kernel, size_t bytes) {
@@ -502,7 +560,8 @@ cudaError_t Infer(const Net& net, const CachePoint* pts, const uint32_t* count, 
                   int grid, cudaStream_t s) {
     cudaError_t e = allow_smem(infer_kernel<false>, infer_smem());
     if (e != cudaSuccess) return e;
-    infer_kernel<false><<<grid, kThreads, infer_smem(), s>>>(net, pts, count, capacity, fb, nullptr, 0, nullptr);
+    infer_kernel<false><<<grid, 32 * kInferWarps, infer_smem(), s>>>(net, pts, count, capacity, fb, nullptr, 0,
+                                                                      nullptr);
     return cudaGetLastError();
 }
 
@@ -510,16 +569,9 @@ cudaError_t InferRaw(const Net& net, const float* feats, uint32_t n, float* out,
     cudaError_t e = allow_smem(infer_kernel<true>, infer_smem());
     if (e != cudaSuccess) return e;
     const uint32_t tiles = (n + 15) / 16;
-    const int grid = (int)((tiles + kWarps - 1) / kWarps);
-    infer_kernel<true><<<grid > 0 ? grid : 1, kThreads, infer_smem(), s>>>(net, nullptr, nullptr, 0, nullptr, feats,
-                                                                           n, out);
-    return cudaGetLastError();
-}
-
-cudaError_t Targets(const TrainSample* smp, const uint32_t* count, const float4* totals, float4* targets,
-                    uint32_t capacity, cudaStream_t s) {
-    const int blocks = (int)std::min<uint32_t>(1024u, (capacity + 255) / 256);
-    targets_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(smp, count, capacity, totals, targets);
+    const int grid = (int)((tiles + kInferWarps - 1) / kInferWarps);
+    infer_kernel<true><<<grid > 0 ? grid : 1, 32 * kInferWarps, infer_smem(), s>>>(net, nullptr, nullptr, 0, nullptr,
+                                                                                   feats, n, out);
     return cudaGetLastError();
 }
 
@@ -568,6 +620,12 @@ cudaError_t GradRaw(const Net& net, const float* feats, const float* targets, ui
 }
 
 cudaError_t AdamRaw(Net& net, float lr, cudaStream_t s) { return launch_adam(net, lr, s); }
+
+cudaError_t EncodeRaw(const Net& net, const CachePoint* pts, uint32_t n, float* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    encode_kernel<<<(n + 127) / 128, 128, 0, s>>>(net, pts, n, out);
+    return cudaGetLastError();
+}
 
 }  // namespace NRC
 }  // namespace Foundation

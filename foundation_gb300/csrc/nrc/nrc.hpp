@@ -80,8 +80,6 @@ cudaError_t InitNet(const Net& net, uint64_t seed, cudaStream_t s);        // He
 cudaError_t Infer(const Net& net, const CachePoint* pts, const uint32_t* count, uint32_t capacity,
                   float4* fb, int grid, cudaStream_t s);                     // fb[pixel] += beta * max(0, f(x))
 cudaError_t InferRaw(const Net& net, const float* feats, uint32_t n, float* out, cudaStream_t s);  // test hook
-cudaError_t Targets(const TrainSample* smp, const uint32_t* count, const float4* totals, float4* targets,
-                    uint32_t capacity, cudaStream_t s);
 // One training step on `batch` samples drawn (with replacement, PCG32) from
 // the first *count samples; accumulates the gradient, then Adam.
 cudaError_t TrainStep(Net& net, const TrainSample* smp, const float4* targets, const uint32_t* count,
@@ -90,6 +88,8 @@ cudaError_t TrainStep(Net& net, const TrainSample* smp, const float4* targets, c
 cudaError_t GradRaw(const Net& net, const float* feats, const float* targets, uint32_t n, cudaStream_t s);
 cudaError_t AdamRaw(Net& net, float lr, cudaStream_t s);
 cudaError_t RewriteImages(const Net& net, cudaStream_t s);  // bf16 images from the fp32 master weights
+// Test hook: the bf16 input features (widened to float) of n cache points.
+cudaError_t EncodeRaw(const Net& net, const CachePoint* pts, uint32_t n, float* out, cudaStream_t s);
 size_t TrainSmemBytes();
 size_t InferSmemBytes();
 

@@ -51,15 +51,8 @@ __device__ __forceinline__ uint32_t append_slot(uint32_t* counter, bool pred, ui
     return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
 }
 
-__device__ __forceinline__ uint32_t hash32(uint32_t v) {
-    const uint32_t s = v * 747796405u + 2891336453u;
-    const uint32_t w = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
-    return (w >> 22u) ^ w;
-}
-
 __global__ void __launch_bounds__(kBlock) generate_kernel(const PathBuffers B, const RenderParams R,
-                                                          uint64_t wave_base, uint32_t wave_n, bool training,
-                                                          uint32_t train_seed) {
+                                                          uint64_t wave_base, uint32_t wave_n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         B.counts[kCountExt0] = wave_n;
@@ -69,15 +62,10 @@ __global__ void __launch_bounds__(kBlock) generate_kernel(const PathBuffers B, c
     if (i >= wave_n) return;
     const uint64_t npix = (uint64_t)R.width * R.height;
     const uint64_t g = wave_base + i;
-    uint32_t pixel = (uint32_t)(g % npix);
-    uint32_t sample = (uint32_t)(g / npix) + R.sample_offset;
-    if (training) {
-        // a training path through a random pixel, on its own PCG32 stream
-        pixel = hash32(train_seed ^ hash32(i)) % (uint32_t)npix;
-        sample = 0x40000000u + (train_seed & 0x3FFFFFFFu);
-    }
+    const uint32_t pixel = (uint32_t)(g % npix);
+    const uint32_t sample = (uint32_t)(g / npix) + R.sample_offset;
     Pcg32 rng;
-    rng.seed(R.seed * 0x9E3779B97F4A7C15ull + pixel + (training ? 0x5851F42D4C957F2Dull * (i + 1) : 0ull), sample);
+    rng.seed(R.seed * 0x9E3779B97F4A7C15ull + pixel, sample);
     const float a = rng.uniform(), b = rng.uniform();
     const uint32_t px = pixel % R.width, py = pixel / R.width;
     const float sx = (2.0f * ((float)px + a) / (float)R.width - 1.0f) * R.tan_half * R.aspect;
@@ -86,8 +74,7 @@ __global__ void __launch_bounds__(kBlock) generate_kernel(const PathBuffers B, c
     B.ext_rays[0][2 * (size_t)i] = make_float4(R.eye[0], R.eye[1], R.eye[2], 0.0f);
     B.ext_rays[0][2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7F800000));
     B.ext_path[0][i] = i;
-    // accumulation index: the pixel, or the path slot of a training path
-    B.rng[i] = make_uint4((uint32_t)rng.state, (uint32_t)(rng.state >> 32), sample, training ? i : pixel);
+    B.rng[i] = make_uint4((uint32_t)rng.state, (uint32_t)(rng.state >> 32), sample, pixel);
     B.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
 }
 
@@ -116,9 +103,8 @@ __global__ void __launch_bounds__(kBlock) shade_kernel(const PathBuffers B, cons
         float3 beta = xyz(beta4);
         const float3 o = xyz(r0), d = xyz(r1);
 
-        bool want_shadow = false, want_sun = false, want_next = false, want_query = false, want_sample = false;
+        bool want_shadow = false, want_sun = false, want_next = false, want_query = false;
         NRC::CachePoint cp;
-        float4 before_rad = make_float4(0.f, 0.f, 0.f, 0.f);
         float3 sh_o, sh_d, sh_c, sun_c, next_d, surf_o = f3(0.f, 0.f, 0.f);
         float sh_tmax = 0.0f;
         if (hit.x == FND_INVALID_ID) {
@@ -162,17 +148,6 @@ __global__ void __launch_bounds__(kBlock) shade_kernel(const PathBuffers B, cons
                 const float alpha = M.params.x;
                 const float3 po = p + nrm * R.eps;
                 surf_o = po;
-                if (kMode == 2u) {
-                    // training sample: radiance collected so far by this path
-                    const float4 before = B.fb[pixel];
-                    cp.p_rough = make_float4(p.x, p.y, p.z, type == kMatLambert ? 1.0f : alpha);
-                    cp.wo_aux = make_float4(-d.x, -d.y, -d.z, __uint_as_float(pixel));
-                    cp.n_pad = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
-                    cp.albedo = M.albedo_type;
-                    cp.beta = make_float4(beta.x, beta.y, beta.z, 0.0f);
-                    before_rad = before;
-                    want_sample = true;
-                }
                 if (kMode == 1u && (type == kMatLambert || alpha >= C.specular_alpha)) flags = kQueryNextFlag;
                 // next-event estimation: one quad light
                 const float ul = rng.uniform(), u1 = rng.uniform(), u2 = rng.uniform();
@@ -252,14 +227,6 @@ __global__ void __launch_bounds__(kBlock) shade_kernel(const PathBuffers B, cons
         if (kMode == 1u) {
             const uint32_t kq = append_slot(C.query_count, want_query, active);
             if (want_query && kq < C.query_cap) C.queries[kq] = cp;
-        } else if (kMode == 2u) {
-            const uint32_t kt = append_slot(C.sample_count, want_sample, active);
-            if (want_sample && kt < C.sample_cap) {
-                NRC::TrainSample ts;
-                ts.pt = cp;
-                ts.before = before_rad;
-                C.samples[kt] = ts;
-            }
         }
         const uint32_t kn = append_slot(B.counts + nxt, want_next, active);
         if (want_next) {
@@ -294,9 +261,9 @@ __global__ void __launch_bounds__(kBlock) finalize_kernel(const float4* fb, floa
 }  // namespace
 
 cudaError_t LaunchGenerate(const PathBuffers& B, const RenderParams& R, uint64_t wave_base, uint32_t wave_n,
-                           bool training, uint32_t train_seed, cudaStream_t s) {
+                           cudaStream_t s) {
     const uint32_t blocks = (wave_n + kBlock - 1) / kBlock;
-    generate_kernel<<<blocks ? blocks : 1, kBlock, 0, s>>>(B, R, wave_base, wave_n, training, train_seed);
+    generate_kernel<<<blocks ? blocks : 1, kBlock, 0, s>>>(B, R, wave_base, wave_n);
     return cudaGetLastError();
 }
 
@@ -304,8 +271,6 @@ cudaError_t LaunchShade(const PathBuffers& B, const RenderParams& R, const Shade
                         uint32_t bounce, int grid, cudaStream_t s) {
     if (C.mode == 1u)
         shade_kernel<1u><<<grid, kBlock, 0, s>>>(B, R, S, C, cur, bounce);
-    else if (C.mode == 2u)
-        shade_kernel<2u><<<grid, kBlock, 0, s>>>(B, R, S, C, cur, bounce);
     else
         shade_kernel<0u><<<grid, kBlock, 0, s>>>(B, R, S, C, cur, bounce);
     return cudaGetLastError();

@@ -72,34 +72,43 @@ struct PathBuffers {
     float4* fb;          // per-pixel radiance sums
 };
 
-// Radiance-cache hooks of the shade stage.
+// Radiance-cache hook of the shade stage.
 //  mode 0: plain path tracing;
 //  mode 1: render with the cache: after the first non-specular bounce the
 //          next non-emissive vertex becomes a cache query (its reflected
-//          radiance comes from the network) and the path ends there;
-//  mode 2: training paths: every non-emissive vertex is recorded as a
-//          training sample; contributions accumulate per path slot.
+//          radiance comes from the network) and the path ends there.
 struct CacheIO {
     uint32_t mode;
     float specular_alpha;  // GGX alpha below which a vertex counts as specular
     NRC::CachePoint* queries;
     uint32_t* query_count;
     uint32_t query_cap;
+};
+
+// The cache's training paths (train_paths.cu): n full paths through random
+// pixels, one thread each; every non-emissive vertex becomes a training
+// sample with its target.
+struct TrainPathsArgs {
+    RT::DeviceScene scene;
+    RenderParams R;
+    ShadeScene S;
+    uint32_t n;
+    uint32_t seed;
     NRC::TrainSample* samples;
+    float4* targets;
     uint32_t* sample_count;
     uint32_t sample_cap;
-    uint32_t train_seed;   // picks the pixels of training paths
+    uint32_t* status;
 };
+cudaError_t LaunchTrainingPaths(const TrainPathsArgs& A, cudaStream_t s);
 
 constexpr uint32_t kQueryNextFlag = 0x80000000u;  // in PathBuffers::rng.w
 
 // Statistics counters appended after the queue counts.
 constexpr int kCountExt0 = 0, kCountExt1 = 1, kCountShadow = 2, kStatExt = 4, kStatShadow = 6;  // 64-bit at 4, 6
 
-// training = true: wave_n training paths through random pixels; the path
-// slot replaces the pixel as the accumulation index (fb = per-path totals).
 cudaError_t LaunchGenerate(const PathBuffers& B, const RenderParams& R, uint64_t wave_base, uint32_t wave_n,
-                           bool training, uint32_t train_seed, cudaStream_t s);
+                           cudaStream_t s);
 cudaError_t LaunchShade(const PathBuffers& B, const RenderParams& R, const ShadeScene& S, const CacheIO& C, int cur,
                         uint32_t bounce, int grid, cudaStream_t s);
 cudaError_t LaunchResolve(const PathBuffers& B, int grid, cudaStream_t s);

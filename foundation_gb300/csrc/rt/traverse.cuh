@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../../include/fnd_rt.h"
 #include "../bvh/wide_bvh.hpp"
 #include "device_scene.hpp"
 
@@ -170,6 +171,80 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
     out.group = (imask << 8) | hits;
     out.tris = tris;
     return out;
+}
+
+}  // namespace RT
+}  // namespace Foundation
+
+namespace Foundation {
+namespace RT {
+
+// Single-ray traversal with a thread-local stack and no warp refill, for
+// latency-bound work where each thread follows its own path (the radiance
+// cache's training paths). Same node / triangle tests and tie rule as the
+// persistent kernels. Returns true on a hit (best_t / best_p updated; the
+// caller initialises best_t to the ray's tmax).
+template <bool kAny>
+__device__ __forceinline__ bool trace_single(const DeviceScene& sc, const RayState& r, float& best_t,
+                                             uint32_t& best_p, uint32_t* status) {
+    best_p = FND_INVALID_ID;
+    if (sc.num_nodes == 0) return false;
+    uint2 stack[kMaxStack];
+    int sp = 0;
+    uint32_t ng_base = 0, ng_group = (1u << 8) | (1u << r.oct), tg_base = 0, tg_mask = 0;
+    for (;;) {
+        if (ng_group & 0xFFu) {
+            const uint32_t b = (uint32_t)__ffs(ng_group & 0xFFu) - 1u;
+            ng_group &= ~(1u << b);
+            const uint32_t slot = b ^ r.oct;
+            const uint32_t child = ng_base + (uint32_t)__popc((ng_group >> 8) & ((1u << slot) - 1u));
+            if (ng_group & 0xFFu) {
+                if (sp >= kMaxStack) {
+                    atomicOr(status, kStatusStackOverflow);
+                    break;
+                }
+                stack[sp++] = make_uint2(ng_base, ng_group);
+            }
+            if (child >= sc.num_nodes) {
+                atomicOr(status, kStatusBadIndex);
+                break;
+            }
+            const NodeHits h = intersect_node(r, sc.nodes, child, best_t);
+            ng_base = h.child_base;
+            ng_group = h.group;
+            tg_base = h.tri_base;
+            tg_mask = h.tris;
+            if (tg_mask && (uint64_t)tg_base + (uint64_t)(32 - __clz(tg_mask)) > sc.num_tris) {
+                atomicOr(status, kStatusBadIndex);
+                break;
+            }
+        }
+        while (tg_mask) {
+            const uint32_t k = (uint32_t)__ffs(tg_mask) - 1u;
+            tg_mask &= tg_mask - 1u;
+            const uint32_t ti = tg_base + k;
+            const float4 v0 = __ldg(sc.v0 + ti);
+            float t;
+            if (intersect_tri(r, v0, __ldg(sc.v1 + ti), __ldg(sc.v2 + ti), best_t, t)) {
+                const uint32_t pid = __float_as_uint(v0.w);
+                if (kAny) {
+                    best_t = t;
+                    best_p = pid;
+                    return true;
+                }
+                if (best_p == FND_INVALID_ID || t < best_t || (t == best_t && pid < best_p)) {
+                    best_t = t;
+                    best_p = pid;
+                }
+            }
+        }
+        if (ng_group & 0xFFu) continue;
+        if (sp == 0) break;
+        const uint2 e = stack[--sp];
+        ng_base = e.x;
+        ng_group = e.y;
+    }
+    return best_p != FND_INVALID_ID;
 }
 
 }  // namespace RT

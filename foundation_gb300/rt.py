@@ -165,6 +165,7 @@ SIGNATURES = {
     "fnd_rt_cache_eval": (_I32, [_P, _P, _U32, _P]),
     "fnd_rt_cache_gradient": (_I32, [_P, _P, _P, _U32, _P, _P]),
     "fnd_rt_cache_adam_step": (_I32, [_P, _P, C.c_float]),
+    "fnd_rt_cache_encode": (_I32, [_P, _P, _U32, _P]),
 }
 
 _lib = None
@@ -330,6 +331,14 @@ class Context:
         loss = C.c_double()
         _check(load().fnd_rt_cache_gradient(self._h, _ptr(f), _ptr(t), len(f), _ptr(g), C.byref(loss)), self._h)
         return g, loss.value
+
+    def cache_encode(self, points) -> np.ndarray:
+        """points: (n, 13) position, outgoing direction, normal, roughness,
+        albedo -> (n, 96) network input features."""
+        p = np.ascontiguousarray(points, np.float32).reshape(-1, 13)
+        out = np.empty((len(p), CACHE_NUM_FEATURES), np.float32)
+        _check(load().fnd_rt_cache_encode(self._h, _ptr(p), len(p), _ptr(out)), self._h)
+        return out
 
     def cache_adam_step(self, grad, learning_rate: float = 1e-2):
         g = np.ascontiguousarray(grad, np.float32)

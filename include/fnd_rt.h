@@ -368,6 +368,10 @@ int fnd_rt_cache_eval(fnd_rt_ctx* ctx, const float* features, uint32_t n, float*
  * (n x 3): grad receives FND_CACHE_NUM_PARAMS floats, loss the mean loss. */
 int fnd_rt_cache_gradient(fnd_rt_ctx* ctx, const float* features, const float* targets, uint32_t n, float* grad,
                           double* loss);
+/* The network's input features of n points, each 13 host floats: position,
+ * outgoing direction, normal, roughness, albedo -> n x 96 host floats (the
+ * BF16 values the network sees, widened to float). */
+int fnd_rt_cache_encode(fnd_rt_ctx* ctx, const float* points, uint32_t n, float* out);
 /* One Adam step with the given gradient (FND_CACHE_NUM_PARAMS host floats). */
 int fnd_rt_cache_adam_step(fnd_rt_ctx* ctx, const float* grad, float learning_rate);
 

@@ -36,6 +36,14 @@ template <typename T>
 static inline T __ldg(const T* p) {
     return *p;
 }
+static inline int __ffs(uint32_t x) { return x ? __builtin_ctz(x) + 1 : 0; }
+static inline int __popc(uint32_t x) { return __builtin_popcount(x); }
+static inline int __clz(uint32_t x) { return x ? __builtin_clz(x) : 32; }
+static inline uint32_t atomicOr(uint32_t* p, uint32_t v) {
+    const uint32_t o = *p;
+    *p |= v;
+    return o;
+}
 using std::copysignf;
 
 using std::signbit;
@@ -149,6 +157,21 @@ void emu_trace(const emu_bvh* e, const float* rays, uint64_t n, uint32_t* hits, 
     stats[0] = nodes;
     stats[1] = tris;
     stats[2] = max_sp;
+}
+
+// The same rays through RT::trace_single (the per-thread traversal of the
+// cache's training paths).
+void emu_trace_single(const emu_bvh* e, const float* rays, uint64_t n, uint32_t* hits, int any) {
+    uint32_t status = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* rp = rays + 8 * i;
+        const RayState r = setup_ray(float4{rp[0], rp[1], rp[2], rp[3]}, float4{rp[4], rp[5], rp[6], rp[7]});
+        float t = r.tmax;
+        uint32_t p = FND_INVALID_ID;
+        const bool h = any ? trace_single<true>(e->view, r, t, p, &status) : trace_single<false>(e->view, r, t, p, &status);
+        hits[2 * i] = h ? p : FND_INVALID_ID;
+        hits[2 * i + 1] = h ? __float_as_uint(t) : 0x7F800000u;
+    }
 }
 
 }  // extern "C"

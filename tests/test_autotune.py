@@ -1,0 +1,39 @@
+"""Tuned-parameter table: keys, nearest-bucket lookup, persistence (CPU),
+and one tuning pass on the GPU."""
+import numpy as np
+import pytest
+
+from foundation_gb300 import autotune as AT
+
+
+def test_table_keys_lookup_and_persistence(tmp_path):
+    t = AT.TuneTable()
+    table = [dict(block=128, short_stack=8, refill_min=8, ms=2.0), dict(block=64, short_stack=4, refill_min=16, ms=1.5)]
+    e = t.record(256012, "incoherent", 0, dict(block=64, short_stack=4, refill_min=16), table)
+    assert e["ms"] == 1.5 and e["default_ms"] == 2.0
+    assert AT.key(256012, "incoherent", 0) == "17:incoherent:closest"
+    assert t.lookup(300000, "incoherent", 0)["block"] == 64     # same bucket
+    assert t.lookup(5_000_000, "incoherent", 0)["block"] == 64  # nearest bucket
+    assert t.lookup(1000, "coherent", 0) is None
+    p = str(tmp_path / "tune.json")
+    t.save(p)
+    t2 = AT.TuneTable.load(p)
+    assert t2.entries == t.entries
+    assert AT.TuneTable.load(str(tmp_path / "missing.json")).entries == {}
+
+
+@pytest.mark.gpu
+def test_tune_pass_on_gpu(built, tmp_path):
+    import torch
+    import foundation_gb300 as fg
+    from foundation_gb300 import scenes as S
+    cs = S.cornell_scene(num_spheres=50)
+    with fg.Context(0) as ctx:
+        s = ctx.upload(cs.verts, cs.idx)
+        rays = torch.from_numpy(S.incoherent_rays(1 << 17, *cs.bounds, seed=5)).cuda()
+        t = AT.TuneTable()
+        e = AT.tune_workload(ctx, t, s, rays, "incoherent", reps=1)
+        assert e["ms"] <= e["default_ms"] + 1e-6
+        cfg = t.apply(ctx, s.info()["num_tris"], "incoherent")
+        assert ctx.trace_config() == cfg
+        t.save(str(tmp_path / "t.json"))

@@ -22,6 +22,7 @@ def emu(built):
     L.emu_trace.argtypes = [P, P, C.c_uint64, P, C.c_int, P]
     L.emu_stats.argtypes = [P, P, P, P]
     L.emu_free.argtypes = [P]
+    L.emu_trace_single.argtypes = [P, P, C.c_uint64, P, C.c_int]
     return L
 
 
@@ -80,6 +81,13 @@ def test_emulated_wide_traversal_matches_oracle(emu, case):
     assert int(st[2]) <= 64
     prim_a, _, _ = e.trace(rays, any_hit=True)
     assert np.array_equal((prim_a != 0xFFFFFFFF).astype(np.uint8), b.any(rays))
+    # the single-ray traversal of the training-path megakernel
+    out = np.zeros(2 * len(rays), np.uint32)
+    emu.emu_trace_single(e.h, _p(np.ascontiguousarray(rays, np.float32)), len(rays), _p(out), 0)
+    assert np.array_equal(out[0::2], ref["prim"])
+    assert np.array_equal(out[1::2], ref["t"].view(np.uint32))
+    emu.emu_trace_single(e.h, _p(np.ascontiguousarray(rays, np.float32)), len(rays), _p(out), 1)
+    assert np.array_equal((out[0::2] != 0xFFFFFFFF).astype(np.uint8), b.any(rays))
 
 
 def test_emulated_edge_cases(emu):

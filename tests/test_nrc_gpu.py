@@ -88,6 +88,27 @@ def test_adam_matches_oracle(cache_ctx):
         assert np.all(np.isfinite(w1)) and not np.array_equal(w1, w0.astype(np.float32))
 
 
+def test_encoding_matches_oracle(cache_ctx):
+    ctx, s, _ = cache_ctx
+    info = s.info()
+    lo, hi = np.array(info["bounds_lo"]), np.array(info["bounds_hi"])
+    pad = 1e-3 * (hi - lo) + 1e-6
+    r = np.random.default_rng(8)
+    n = 500
+    p = lo + r.uniform(0, 1, (n, 3)) * (hi - lo)
+    wo = r.normal(size=(n, 3))
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    nr = r.normal(size=(n, 3))
+    nr /= np.linalg.norm(nr, axis=1, keepdims=True)
+    pts = np.concatenate([p, wo, nr, r.uniform(0.05, 1, (n, 1)), r.uniform(0, 1, (n, 3))], 1).astype(np.float32)
+    got = ctx.cache_encode(pts)
+    ref = np.stack([O.nrc_encode(q[0:3], q[3:6], q[6:9], q[9], q[10:13], (lo - pad).astype(np.float32),
+                                 (hi + pad).astype(np.float32)) for q in pts])
+    # features are bf16: agree to within one bf16 step (2^-8 relative, 2^-9 absolute near 0)
+    tol = np.maximum(np.abs(ref) * 2.0 ** -7, 2.0 ** -9)
+    assert np.all(np.abs(got - ref) <= tol), np.abs(got - ref).max()
+
+
 def test_overfit_and_checkpoint(cache_ctx, tmp_path):
     ctx, _, _ = cache_ctx
     x = features(512, 5)
