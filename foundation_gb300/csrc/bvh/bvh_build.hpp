@@ -38,11 +38,18 @@ struct BinaryBvh {
 struct BuildParams {
     uint32_t bins = 32;
     uint32_t max_leaf = 4;
-    uint32_t threads = 0;  // 0: hardware concurrency
+    uint32_t threads = 0;          // 0: hardware concurrency
+    bool spatial_splits = false;   // BuildBinarySbvh only
+    float spatial_alpha = 1e-5f;   // try spatial splits when child overlap > alpha x root half area
+    double max_refs_factor = 2.0;  // at most this many references per triangle in total
 };
 
 // tri: 9 floats per triangle (v0, v1, v2). nt > 0.
 void BuildBinaryBvh(const float* tri, uint32_t nt, const BuildParams& params, BinaryBvh& out);
+
+// Binned SAH with spatial splits (sbvh_build.cpp): leaves may reference a
+// triangle more than once; out.prims holds the references.
+void BuildBinarySbvh(const float* tri, uint32_t nt, const BuildParams& params, BinaryBvh& out);
 
 }  // namespace RT
 }  // namespace Foundation

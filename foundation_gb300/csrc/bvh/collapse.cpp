@@ -55,9 +55,10 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
     out.margin = margin;
     out.nodes.clear();
     out.nodes.reserve(bin.nodes.size() / 4 + 1);
-    out.v0.assign(4 * (size_t)nt, 0.0f);
-    out.v1.assign(4 * (size_t)nt, 0.0f);
-    out.v2.assign(4 * (size_t)nt, 0.0f);
+    const size_t nrefs = bin.prims.size();  // == nt unless spatial splits duplicated references
+    out.v0.assign(4 * nrefs, 0.0f);
+    out.v1.assign(4 * nrefs, 0.0f);
+    out.v2.assign(4 * nrefs, 0.0f);
     out.depth = 0;
     out.leaves = 0;
     uint32_t next_tri = 0;
@@ -207,7 +208,8 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
         next_tri += tri_off;
         out.nodes[it.wnode] = nd;
     }
-    CHECK_CODE(next_tri == nt, FND_ERR_INVALID_SCENE, "collapse lost triangles (%u of %u)", next_tri, nt);
+    CHECK_CODE(next_tri == nrefs, FND_ERR_INVALID_SCENE, "collapse lost references (%u of %zu)", next_tri, nrefs);
+    (void)nt;
 }
 
 }  // namespace RT

@@ -19,6 +19,10 @@ size_t Align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 void FreeCache(fnd_rt_ctx* ctx) {
     if (!ctx->cache) return;
+    if (ctx->cache->train_stream) cudaStreamSynchronize(ctx->cache->train_stream);
+    if (ctx->cache->ev_start) cudaEventDestroy(ctx->cache->ev_start);
+    if (ctx->cache->ev_trained) cudaEventDestroy(ctx->cache->ev_trained);
+    if (ctx->cache->train_stream) cudaStreamDestroy(ctx->cache->train_stream);
     if (ctx->cache->d_block) cudaFree(ctx->cache->d_block);
     delete ctx->cache;
     ctx->cache = nullptr;
@@ -57,6 +61,7 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
     net.grad = reinterpret_cast<float*>(take(sizes[5]));
     net.loss = reinterpret_cast<double*>(take(sizes[6]));
     if (c.d_block) {
+        if (c.train_stream) CUDA_CHECK(cudaStreamSynchronize(c.train_stream));
         // keep the trained state: copy the network, moments and images across
         CUDA_CHECK(cudaMemcpyAsync(net.fwd, c.net.fwd, sizes[0], cudaMemcpyDeviceToDevice, ctx->stream));
         CUDA_CHECK(cudaMemcpyAsync(net.bwd, c.net.bwd, sizes[1], cudaMemcpyDeviceToDevice, ctx->stream));
@@ -120,6 +125,9 @@ int fnd_rt_cache_create(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ca
             ctx->cache->net.hi[a] = hi + pad;
         }
         try {
+            CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->cache->train_stream, cudaStreamNonBlocking));
+            CUDA_CHECK(cudaEventCreateWithFlags(&ctx->cache->ev_start, cudaEventDisableTiming));
+            CUDA_CHECK(cudaEventCreateWithFlags(&ctx->cache->ev_trained, cudaEventDisableTiming));
             EnsureCacheBuffers(ctx, 1024, 8);
             CUDA_CHECK(NRC::InitNet(ctx->cache->net, desc->seed, ctx->stream));
             CUDA_CHECK(cudaStreamSynchronize(ctx->stream));

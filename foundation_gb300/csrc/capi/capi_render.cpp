@@ -297,11 +297,16 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         CUDA_CHECK(cudaMemsetAsync(ctx->d_render_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
         PT::CacheIO C{};
         if (use_cache) {
-            // 1) training paths: full paths through random pixels, one thread
-            //    each, one training sample (with its target) per vertex
+            // 1) training, on the cache's own stream so it overlaps the render
+            //    wave: full training paths through random pixels (one thread
+            //    each, one sample + target per vertex), then the optimiser
+            //    steps. The render wave's cache queries wait for it (event).
             FndCacheState& cs = *ctx->cache;
             const fnd_cache_desc& cd = cs.desc;
-            CUDA_CHECK(cudaMemsetAsync(cs.counters + 1, 0, sizeof(uint32_t), ctx->stream));
+            cudaStream_t ts = cs.train_stream;
+            CUDA_CHECK(cudaEventRecord(cs.ev_start, ctx->stream));
+            CUDA_CHECK(cudaStreamWaitEvent(ts, cs.ev_start, 0));
+            CUDA_CHECK(cudaMemsetAsync(cs.counters + 1, 0, sizeof(uint32_t), ts));
             PT::TrainPathsArgs T{};
             T.scene = scene->view;
             T.R = R;
@@ -314,11 +319,12 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
             T.sample_count = cs.counters + 1;
             T.sample_cap = cs.sample_cap;
             T.status = ctx->d_status;
-            CUDA_CHECK(PT::LaunchTrainingPaths(T, ctx->stream));
+            CUDA_CHECK(PT::LaunchTrainingPaths(T, ts));
             const int grid_train = std::max(1, std::min<int>((int)((cd.batch + 63) / 64), ctx->sm_count));
             for (uint32_t st = 0; st < cd.train_steps; ++st)
                 CUDA_CHECK(NRC::TrainStep(cs.net, cs.samples, cs.targets, cs.counters + 1, cd.batch,
-                                          Mix32(tseed, st + 1), cd.learning_rate, grid_train, ctx->stream));
+                                          Mix32(tseed, st + 1), cd.learning_rate, grid_train, ts));
+            CUDA_CHECK(cudaEventRecord(cs.ev_trained, ts));
             cs.frames++;
             // 2) render waves end their paths in cache queries
             C.mode = 1;
@@ -333,9 +339,11 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
             if (use_cache) CUDA_CHECK(cudaMemsetAsync(C.query_count, 0, sizeof(uint32_t), ctx->stream));
             CUDA_CHECK(PT::LaunchGenerate(B, R, wave_base, wave_n, ctx->stream));
             RunBounces(ctx, scene, B, R, S, C, D.max_depth, grid_shade);
-            if (use_cache)
+            if (use_cache) {
+                CUDA_CHECK(cudaStreamWaitEvent(ctx->stream, ctx->cache->ev_trained, 0));
                 CUDA_CHECK(NRC::Infer(ctx->cache->net, C.queries, C.query_count, C.query_cap, B.fb,
                                       ctx->sm_count * 2, ctx->stream));
+            }
         }
         ctx->fb_samples += D.spp;
         const float scale = 1.0f / (float)ctx->fb_samples;

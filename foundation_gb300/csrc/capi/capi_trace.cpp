@@ -187,6 +187,8 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         CHECK_CODE(bp.bins >= 2 && bp.bins <= 64, FND_ERR_INVALID_ARG, "sah_bins %u not in [2, 64]", bp.bins);
         CHECK_CODE(bp.max_leaf >= 1 && bp.max_leaf <= 4, FND_ERR_INVALID_ARG, "max_leaf_tris %u not in [1, 4]",
                    bp.max_leaf);
+        CHECK_CODE(!bvh || (bvh->flags & ~(uint32_t)FND_BVH_SPATIAL_SPLITS) == 0, FND_ERR_INVALID_ARG,
+                   "unknown BVH flags 0x%x", bvh ? bvh->flags : 0u);
         UseDevice(ctx);
         auto scene = std::make_unique<fnd_rt_scene>();
         scene->ctx = ctx;
@@ -252,7 +254,10 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         }
         auto t0 = std::chrono::steady_clock::now();
         RT::BinaryBvh bin;
-        RT::BuildBinaryBvh(tri.data(), nt, bp, bin);
+        if (bvh && (bvh->flags & FND_BVH_SPATIAL_SPLITS))
+            RT::BuildBinarySbvh(tri.data(), nt, bp, bin);
+        else
+            RT::BuildBinaryBvh(tri.data(), nt, bp, bin);
         scene->info.build_ms = MsSince(t0);
         t0 = std::chrono::steady_clock::now();
         RT::WideBvh wide;
@@ -268,7 +273,8 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         I.num_wide_nodes = (uint32_t)wide.nodes.size();
         I.wide_depth = wide.depth;
         I.node_bytes = wide.nodes.size() * sizeof(RT::WideNode);
-        I.tri_bytes = 3ull * 16ull * nt;
+        I.num_refs = (uint32_t)bin.prims.size();
+        I.tri_bytes = 3ull * 16ull * I.num_refs;
         for (int a = 0; a < 3; ++a) {
             I.bounds_lo[a] = wide.lo[a];
             I.bounds_hi[a] = wide.hi[a];
@@ -279,7 +285,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             CUDA_CHECK(cudaMalloc(&scene->d_nodes, I.node_bytes));
             CUDA_CHECK(cudaMalloc(&scene->d_tris, I.tri_bytes));
             char* tris = static_cast<char*>(scene->d_tris);
-            const size_t plane = 16ull * nt;
+            const size_t plane = 16ull * I.num_refs;
             CUDA_CHECK(cudaMemcpy(scene->d_nodes, wide.nodes.data(), I.node_bytes, cudaMemcpyHostToDevice));
             CUDA_CHECK(cudaMemcpy(tris, wide.v0.data(), plane, cudaMemcpyHostToDevice));
             CUDA_CHECK(cudaMemcpy(tris + plane, wide.v1.data(), plane, cudaMemcpyHostToDevice));
@@ -303,13 +309,13 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         }
         I.upload_ms = MsSince(t0);
         char* tris = static_cast<char*>(scene->d_tris);
-        const size_t plane = 16ull * nt;
+        const size_t plane = 16ull * I.num_refs;
         scene->view.nodes = static_cast<const uint4*>(scene->d_nodes);
         scene->view.v0 = reinterpret_cast<const float4*>(tris);
         scene->view.v1 = reinterpret_cast<const float4*>(tris + plane);
         scene->view.v2 = reinterpret_cast<const float4*>(tris + 2 * plane);
         scene->view.num_nodes = I.num_wide_nodes;
-        scene->view.num_tris = nt;
+        scene->view.num_tris = I.num_refs;
         *out_scene = scene.release();
         ctx->live_scenes++;
     });

@@ -28,6 +28,9 @@ struct FndCacheState {
     uint32_t query_cap = 0;
     uint32_t train_cap = 0;
     uint64_t frames = 0;
+    // training runs on its own stream, overlapping the render wave
+    cudaStream_t train_stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_trained = nullptr;
 };
 
 struct fnd_rt_ctx {

@@ -41,6 +41,7 @@ MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("albedo", "<f4", 3), ("roughness", 
 LIGHT_DTYPE = np.dtype([("corner", "<f4", 3), ("edge_u", "<f4", 3), ("edge_v", "<f4", 3), ("radiance", "<f4", 3)])
 MAT_LAMBERT, MAT_GGX, MAT_EMISSIVE = 0, 1, 2
 RENDER_ACCUMULATE = 1
+BVH_SPATIAL_SPLITS = 1
 RENDER_CACHE = 2
 CACHE_NUM_PARAMS = 22720
 CACHE_NUM_FEATURES = 96
@@ -66,7 +67,8 @@ class SceneInfo(C.Structure):
                 ("binary_depth", C.c_uint32), ("wide_depth", C.c_uint32), ("num_leaves", C.c_uint32),
                 ("node_bytes", C.c_uint64), ("tri_bytes", C.c_uint64), ("sah_cost", C.c_double),
                 ("build_ms", C.c_double), ("collapse_ms", C.c_double), ("upload_ms", C.c_double),
-                ("bounds_lo", C.c_float * 3), ("bounds_hi", C.c_float * 3), ("box_margin", C.c_float)]
+                ("bounds_lo", C.c_float * 3), ("bounds_hi", C.c_float * 3), ("box_margin", C.c_float),
+                ("num_refs", C.c_uint32)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -246,8 +248,9 @@ class Context:
     def __exit__(self, *a):
         self.close()
 
-    def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0) -> "Scene":
-        return Scene(self, verts, idx, bins, max_leaf, threads)
+    def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0,
+               spatial_splits: bool = False) -> "Scene":
+        return Scene(self, verts, idx, bins, max_leaf, threads, spatial_splits)
 
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
@@ -351,12 +354,12 @@ class Context:
 
 
 class Scene:
-    def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0):
+    def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0, spatial_splits=False):
         self._h = None
         self.ctx = ctx
         v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
-        bd = _BvhDesc(bins, max_leaf, threads, 0)
+        bd = _BvhDesc(bins, max_leaf, threads, BVH_SPATIAL_SPLITS if spatial_splits else 0)
         h = C.c_void_p()
         _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),
                ctx.handle)

@@ -86,8 +86,14 @@ typedef struct fnd_rt_bvh_desc {
     uint32_t sah_bins;      /* 2..64, default 32 */
     uint32_t max_leaf_tris; /* 1..4, default 4 */
     uint32_t build_threads; /* 0: all host cores */
-    uint32_t flags;         /* reserved, 0 */
+    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS or 0 */
 } fnd_rt_bvh_desc;
+
+/* Spatial splits (Stich et al. 2009): references of triangles that straddle
+ * a split plane are clipped and duplicated (at most 2x the triangle count),
+ * which tightens the tree of scenes with long, overlapping triangles. Hits
+ * are identical either way. */
+enum { FND_BVH_SPATIAL_SPLITS = 1u };
 
 typedef struct fnd_rt_scene_info {
     uint32_t num_tris;
@@ -105,6 +111,7 @@ typedef struct fnd_rt_scene_info {
     float bounds_lo[3];
     float bounds_hi[3];
     float box_margin; /* absolute outward inflation applied to every node box */
+    uint32_t num_refs; /* triangle references in the leaves (num_tris without spatial splits) */
 } fnd_rt_scene_info;
 
 /* ---- context --------------------------------------------------------- */

@@ -63,7 +63,15 @@ struct emu_bvh {
 
 extern "C" {
 
+emu_bvh* emu_build2(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads,
+                    int spatial);
+
 emu_bvh* emu_build(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads) {
+    return emu_build2(verts, nv, idx, nt, threads, 0);
+}
+
+emu_bvh* emu_build2(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads,
+                    int spatial) {
     auto* e = new emu_bvh();
     std::vector<float> tri(9 * (size_t)nt);
     for (uint32_t t = 0; t < nt; ++t)
@@ -71,14 +79,17 @@ emu_bvh* emu_build(const float* verts, uint32_t nv, const uint32_t* idx, uint32_
             for (int c = 0; c < 3; ++c) tri[9 * (size_t)t + 3 * k + c] = verts[3 * (size_t)idx[3 * (size_t)t + k] + c];
     BuildParams p;
     p.threads = threads;
-    BuildBinaryBvh(tri.data(), nt, p, e->bin);
+    if (spatial)
+        BuildBinarySbvh(tri.data(), nt, p, e->bin);
+    else
+        BuildBinaryBvh(tri.data(), nt, p, e->bin);
     CollapseToWide(e->bin, tri.data(), nt, e->wide);
     e->view.nodes = reinterpret_cast<const uint4*>(e->wide.nodes.data());
     e->view.v0 = reinterpret_cast<const float4*>(e->wide.v0.data());
     e->view.v1 = reinterpret_cast<const float4*>(e->wide.v1.data());
     e->view.v2 = reinterpret_cast<const float4*>(e->wide.v2.data());
     e->view.num_nodes = (uint32_t)e->wide.nodes.size();
-    e->view.num_tris = nt;
+    e->view.num_tris = (uint32_t)e->bin.prims.size();
     (void)nv;
     return e;
 }
