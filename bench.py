@@ -256,6 +256,46 @@ def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
             "wide_nodes": info["num_wide_nodes"], "wide_depth": info["wide_depth"], "build_ms": info["build_ms"]}
 
 
+def time_to_relmse_block(fg, torch, stream, local, ref_spp: int = 8192):
+    """The second half of the metric: wall time to relMSE 1e-3 at 1920x1080
+    on the Cornell scene, radiance cache (1 spp per frame, 65,536 training
+    paths and 4 Adam steps of 16,384 samples per frame, lr 1e-2, 32 warm-up
+    frames counted in the time) vs the plain tracer (8 spp per frame), both
+    against a plain render of `ref_spp` spp on the same GPU; plus the cache's
+    bias (its relMSE after 512 accumulated frames)."""
+    from foundation_gb300 import convergence as CV
+    from foundation_gb300 import scenes
+    cs = scenes.cornell_scene()
+    ctx = fg.Context(local, stream=stream.cuda_stream)
+    s = ctx.upload(cs.verts, cs.idx)
+    s.set_materials(cs.tri_material, scenes.material_records(cs))
+    s.set_lights(scenes.light_records(cs))
+    W, H, cam = 1920, 1080, scenes.CORNELL_CAMERA
+    t0 = time.perf_counter()
+    ref = CV.render_reference(ctx, s, W, H, cam, ref_spp, seed=9001)
+    ref_s = time.perf_counter() - t0
+    half = CV.render_reference(ctx, s, W, H, cam, 1024, seed=4242)
+    ref_noise = CV.relmse(half, ref) * 1024 / (ref_spp + 1024)  # relMSE of a 1024-spp image ~ noise(1024)+noise(ref)
+    plain = CV.time_to_relmse(ctx, s, ref, W, H, cam, mode="plain", spp_per_frame=8, max_frames=400, stream=stream)
+    ctx.cache_create(s, train_paths=65536, train_steps=4, batch=16384, learning_rate=1e-2, seed=1)
+    cache = CV.time_to_relmse(ctx, s, ref, W, H, cam, mode="cache", warmup=32, max_frames=1200, stream=stream)
+    # bias: a fresh cache trained 32 frames, then 512 accumulated frames
+    ctx.cache_create(s, train_paths=65536, train_steps=4, batch=16384, learning_rate=1e-2, seed=2)
+    long = CV.time_to_relmse(ctx, s, ref, W, H, cam, mode="cache", warmup=32, max_frames=32 + 512, target=0.0,
+                             stream=stream)
+    st = ctx.cache_stats()
+    ctx.close()
+    speedup = plain["time_ms"] / cache["time_ms"] if plain["reached"] and cache["reached"] else None
+    return {"workload": "cornell200 1920x1080, max depth 8, RR from bounce 3, NEE; target relMSE 1e-3 "
+                        "(eps 1e-2 in the denominator, FP64 reduction)",
+            "reference": {"spp": ref_spp, "render_s": ref_s, "est_relmse_noise": ref_noise},
+            "plain": {k: plain[k] for k in ("reached", "time_ms", "spp", "relmse")},
+            "cache": {k: cache[k] for k in ("reached", "time_ms", "frames", "spp", "relmse")},
+            "speedup_cache_vs_plain": speedup, "target_speedup": 3.0,
+            "cache_relmse_after_512_frames": long["relmse"],
+            "cache_loss_last": st["loss_last"]}
+
+
 def cpu_baseline(sc, rays):
     import oracle
     cores = os.cpu_count() or 1
@@ -418,6 +458,7 @@ def main():
         if not args.no_extra:
             line["path_tracer"] = path_tracer_block(fg, torch, stream, local)
             line["incoherent_1m_tris"] = incoherent_1m_block(fg, torch, stream, local)
+            line["time_to_relmse_1080p"] = time_to_relmse_block(fg, torch, stream, local)
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, rays)
         print(json.dumps(line), flush=True)

@@ -56,18 +56,20 @@ std::vector<RT::TraceConfig> Candidates() {
     std::vector<RT::TraceConfig> out;
     for (int block : {64, 128, 256})
         for (int st : {4, 8, 16})
-            for (uint32_t refill : {4u, 8u, 16u, 24u}) {
-                RT::TraceConfig c;
-                c.block = block;
-                c.short_stack = st;
-                c.refill_min = refill;
-                out.push_back(c);
-            }
+            for (uint32_t refill : {4u, 8u, 16u, 24u})
+                for (uint32_t postpone : {0u, 8u}) {
+                    RT::TraceConfig c;
+                    c.block = block;
+                    c.short_stack = st;
+                    c.refill_min = refill;
+                    c.postpone_min = postpone;
+                    out.push_back(c);
+                }
     return out;
 }
 
 fnd_rt_trace_config ToAbi(const RT::TraceConfig& c) {
-    return fnd_rt_trace_config{(uint32_t)c.block, (uint32_t)c.short_stack, c.refill_min, 0u};
+    return fnd_rt_trace_config{(uint32_t)c.block, (uint32_t)c.short_stack, c.refill_min, c.postpone_min};
 }
 
 RT::TraceConfig FromAbi(const fnd_rt_trace_config& a) {
@@ -75,6 +77,7 @@ RT::TraceConfig FromAbi(const fnd_rt_trace_config& a) {
     c.block = (int)a.block;
     c.short_stack = (int)a.short_stack;
     c.refill_min = a.refill_min;
+    c.postpone_min = a.postpone_min;
     return c;
 }
 
@@ -151,8 +154,9 @@ int fnd_rt_set_trace_config(fnd_rt_ctx* ctx, const fnd_rt_trace_config* config) 
     if (!ctx || !config) return FND_ERR_INVALID_ARG;
     return Guard(ctx, [&] {
         const RT::TraceConfig c = FromAbi(*config);
-        CHECK_CODE(RT::ValidTraceConfig(c), FND_ERR_INVALID_ARG, "launch shape block %u / short stack %u / refill %u",
-                   config->block, config->short_stack, config->refill_min);
+        CHECK_CODE(RT::ValidTraceConfig(c), FND_ERR_INVALID_ARG,
+                   "launch shape block %u / short stack %u / refill %u / postpone %u", config->block,
+                   config->short_stack, config->refill_min, config->postpone_min);
         ctx->trace_cfg = c;
         ctx->refill_min = c.refill_min;
     });

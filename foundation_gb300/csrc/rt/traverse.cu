@@ -38,6 +38,7 @@ struct Common {
     uint32_t* status;
     unsigned long long* stats;
     uint32_t refill_min;
+    uint32_t postpone_min;  // postpone a triangle group when fewer lanes than this have one (0: never)
 };
 
 // ---- work sources -----------------------------------------------------------
@@ -194,6 +195,20 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                     ng_group = 0;
                     sp = 0;
                 }
+                // triangle postponement (Ylitie et al. 2017): when only a few
+                // lanes of the warp have triangles to test, keep traversing
+                // nodes with the rest and test the triangles later
+                if (C.postpone_min) {
+                    const uint32_t tri_lanes = __ballot_sync(__activemask(), tg_mask != 0u);
+                    if (tg_mask && (ng_group & 0xFFu) && (uint32_t)__popc(tri_lanes) < C.postpone_min &&
+                        sp < kMaxStack) {
+                        const int s = (sp & (kShort - 1)) * kBlock + tid;
+                        if (sp >= kShort) l_stack[sp - kShort] = s_stack[s];
+                        s_stack[s] = make_uint2(tg_base | kTriGroupFlag, tg_mask);
+                        sp++;
+                        tg_mask = 0;
+                    }
+                }
             } else {
                 atomicOr(C.status, kStatusBadIndex);
                 ng_group = 0;
@@ -276,7 +291,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const 
     src.occluded = L.occluded;
     src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
     if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
-    const Common C{L.counter, L.status, L.stats, L.refill_min};
+    const Common C{L.counter, L.status, L.stats, L.refill_min, L.postpone_min};
     persistent_trace<SingleSource, kAny ? 1 : 0, kStats, kShort, kBlock>(src, C, s_stack);
 }
 
@@ -288,7 +303,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) batch_kernel(const 
     src.prefix = B.prefix;
     src.njobs = B.njobs;
     src.n = B.total;
-    const Common C{B.counter, B.status, nullptr, B.refill_min};
+    const Common C{B.counter, B.status, nullptr, B.refill_min, B.postpone_min};
     persistent_trace<BatchSource, 2, false, kShort, kBlock>(src, C, s_stack);
 }
 
@@ -336,7 +351,7 @@ int normalized_block(int b) { return b == 64 || b == 256 ? b : 128; }
 bool ValidTraceConfig(const TraceConfig& c) {
     return (c.block == 64 || c.block == 128 || c.block == 256) &&
            (c.short_stack == 4 || c.short_stack == 8 || c.short_stack == 16) && c.refill_min >= 1 &&
-           c.refill_min <= 32 && c.blocks_per_sm >= 0 && c.blocks_per_sm <= 32;
+           c.refill_min <= 32 && c.postpone_min <= 32 && c.blocks_per_sm >= 0 && c.blocks_per_sm <= 32;
 }
 
 cudaError_t TraceOccupancy(int variant, int* blocks_per_sm) {
@@ -366,6 +381,7 @@ cudaError_t LaunchTraceConfigured(const TraceLaunch& L, bool any, bool stats, co
     const int block = stats ? 128 : normalized_block(c.block);
     TraceLaunch arg = L;
     arg.refill_min = c.refill_min ? c.refill_min : L.refill_min;
+    arg.postpone_min = c.postpone_min;
     void* params[] = {&arg};
     return cudaLaunchKernel(fn, dim3(grid), dim3(block), params, 0, stream);
 }
@@ -382,6 +398,7 @@ cudaError_t LaunchBatch(const BatchLaunch& B, const TraceConfig& c, int grid, cu
     if (e != cudaSuccess) return e;
     BatchLaunch arg = B;
     arg.refill_min = c.refill_min ? c.refill_min : B.refill_min;
+    arg.postpone_min = c.postpone_min;
     void* params[] = {&arg};
     return cudaLaunchKernel(select_batch(c), dim3(grid), dim3(normalized_block(c.block)), params, 0, stream);
 }

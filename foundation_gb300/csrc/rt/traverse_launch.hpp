@@ -25,6 +25,7 @@ struct TraceLaunch {
     uint32_t* status;    // latched kStatus* bits
     unsigned long long* stats;  // [0] node fetches, [1] triangle tests (stats variants)
     uint32_t refill_min;        // refill a warp once this many lanes are idle
+    uint32_t postpone_min;      // triangle postponement threshold (0: off)
 };
 
 // Launch shape of a traversal kernel (the autotuner's search space).
@@ -32,6 +33,7 @@ struct TraceConfig {
     int block = kTraceBlock;             // 64, 128 or 256 threads
     int short_stack = kTraceShortStack;  // 4, 8 or 16 shared-memory stack entries per thread
     uint32_t refill_min = 8;             // 1..32 idle lanes before a warp refills
+    uint32_t postpone_min = 0;           // postpone triangles when fewer lanes have them (0: never)
     int blocks_per_sm = 0;               // 0: as many as fit
 };
 bool ValidTraceConfig(const TraceConfig& c);
@@ -53,6 +55,7 @@ struct BatchLaunch {
     uint32_t* counter;
     uint32_t* status;
     uint32_t refill_min;
+    uint32_t postpone_min;
 };
 
 // variant: 0 closest, 1 any, 2 closest+stats, 3 any+stats, 4 batch

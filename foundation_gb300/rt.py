@@ -95,10 +95,11 @@ class RenderStats(C.Structure):
 
 class TraceConfig(C.Structure):
     _fields_ = [("block", C.c_uint32), ("short_stack", C.c_uint32), ("refill_min", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("postpone_min", C.c_uint32)]
 
     def as_dict(self):
-        return dict(block=self.block, short_stack=self.short_stack, refill_min=self.refill_min)
+        return dict(block=self.block, short_stack=self.short_stack, refill_min=self.refill_min,
+                    postpone_min=self.postpone_min)
 
 
 class TuneEntry(C.Structure):
@@ -273,8 +274,8 @@ class Context:
         return img
 
     # ---- launch shape -------------------------------------------------
-    def set_trace_config(self, block: int = 128, short_stack: int = 8, refill_min: int = 8):
-        c = TraceConfig(block, short_stack, refill_min, 0)
+    def set_trace_config(self, block: int = 128, short_stack: int = 8, refill_min: int = 8, postpone_min: int = 0):
+        c = TraceConfig(block, short_stack, refill_min, postpone_min)
         _check(load().fnd_rt_set_trace_config(self._h, C.byref(c)), self._h)
 
     def trace_config(self) -> dict:
@@ -285,10 +286,10 @@ class Context:
     def tune(self, scene: "Scene", rays, kind: int = QUERY_CLOSEST, reps: int = 3):
         """Times every launch shape on device rays; returns (best, table)."""
         n = rays.numel() * rays.element_size() // 32
-        table = (TuneEntry * 64)()
+        table = (TuneEntry * 128)()
         tn = C.c_uint32()
         best = TraceConfig()
-        _check(load().fnd_rt_tune(self._h, scene.handle, _ptr(rays), n, kind, reps, table, 64, C.byref(tn),
+        _check(load().fnd_rt_tune(self._h, scene.handle, _ptr(rays), n, kind, reps, table, 128, C.byref(tn),
                                   C.byref(best)), self._h)
         return best.as_dict(), [dict(table[i].config.as_dict(), ms=table[i].ms) for i in range(tn.value)]
 
@@ -478,10 +479,10 @@ class Batch:
         _check(load().fnd_rt_batch_launch(self._h), self.ctx.handle)
 
     def tune(self, reps: int = 2):
-        table = (TuneEntry * 64)()
+        table = (TuneEntry * 128)()
         tn = C.c_uint32()
         best = TraceConfig()
-        _check(load().fnd_rt_batch_tune(self._h, reps, table, 64, C.byref(tn), C.byref(best)), self.ctx.handle)
+        _check(load().fnd_rt_batch_tune(self._h, reps, table, 128, C.byref(tn), C.byref(best)), self.ctx.handle)
         return best.as_dict(), [dict(table[i].config.as_dict(), ms=table[i].ms) for i in range(tn.value)]
 
     def close(self):

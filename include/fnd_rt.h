@@ -199,7 +199,8 @@ typedef struct fnd_rt_trace_config {
     uint32_t block;        /* 64, 128 or 256 threads */
     uint32_t short_stack;  /* 4, 8 or 16 entries per thread */
     uint32_t refill_min;   /* 1..32 idle lanes before a warp refills */
-    uint32_t reserved;
+    uint32_t postpone_min; /* postpone a node's triangles while fewer than this many lanes
+                              of the warp have triangles to test (0..32, 0: never) */
 } fnd_rt_trace_config;
 
 typedef struct fnd_rt_tune_entry {

@@ -69,7 +69,7 @@ def test_batch_matches_oracle_with_graph_and_tuning(ctx):
     eh = eo.cpu().numpy().view(np.uint32)
     assert (eh[0::2] == fg.INVALID_ID).all() and np.isinf(eh[1::2].view(np.float32)).all()
     best, table = batch.tune(reps=1)
-    assert len(table) == 36 and best["block"] in (64, 128, 256)
+    assert len(table) == 72 and best["block"] in (64, 128, 256)
     for _, _, out, _ in jobs[:-2]:
         out.zero_()
     batch.launch()
@@ -93,9 +93,11 @@ def test_tuner_and_launch_shapes_keep_parity(ctx):
     rays = S.incoherent_rays(1 << 18, *cs.bounds, seed=31)
     rd = torch.from_numpy(rays).cuda()
     best, table = ctx.tune(s, rd, reps=1)
-    assert len(table) == 36 and all(e["ms"] > 0 for e in table)
+    assert len(table) == 72 and all(e["ms"] > 0 for e in table)
     ref = O.OracleBVH(cs.verts, cs.idx).closest(rays)
-    for cfg in (best, dict(block=64, short_stack=4, refill_min=1), dict(block=256, short_stack=16, refill_min=32)):
+    for cfg in (best, dict(block=64, short_stack=4, refill_min=1, postpone_min=0),
+                dict(block=256, short_stack=16, refill_min=32, postpone_min=8),
+                dict(block=128, short_stack=4, refill_min=8, postpone_min=32)):
         ctx.set_trace_config(**cfg)
         assert ctx.trace_config() == cfg
         h = s.closest(rays)
