@@ -2,7 +2,9 @@
 
 The native tuner (fnd_rt_tune / fnd_rt_batch_tune) times every launch shape
 (block 64/128/256 x shared short stack 4/8/16 x refill threshold
-4/8/16/24 x triangle postponement off/8) on a ray batch. This module runs it on representative workloads
+4/8/16/24 x triangle postponement off/8) on a ray batch, and for single
+scenes then the best shape with each coherence-order key width (9..21 bits,
+sort time included). This module runs it on representative workloads
 and keeps the winners in a JSON file keyed by
 
     "<scene size bucket>:<coherence>:<query kind>"
@@ -48,7 +50,8 @@ class TuneTable:
     def record(self, num_tris: int, coherence: str, kind: int, best: dict, table: list) -> dict:
         ms = min(e["ms"] for e in table) if table else None
         default = next((e["ms"] for e in table if (e["block"], e["short_stack"], e["refill_min"],
-                                                    e.get("postpone_min", 0)) == (128, 8, 8, 0)), None)
+                                                    e.get("postpone_min", 0), e.get("sort_bits", 0)) ==
+                        (128, 8, 8, 0, 0)), None)
         entry = dict(best, ms=ms, default_ms=default)
         self.entries[key(num_tris, coherence, kind)] = entry
         return entry
@@ -63,9 +66,9 @@ class TuneTable:
 
     def apply(self, ctx: "rt.Context", num_tris: int, coherence: str, kind: int = rt.QUERY_CLOSEST) -> dict:
         e = self.lookup(num_tris, coherence, kind)
-        cfg = dict(block=128, short_stack=8, refill_min=8, postpone_min=0) if e is None else \
+        cfg = dict(block=128, short_stack=8, refill_min=8, postpone_min=0, sort_bits=0) if e is None else \
             dict(block=e["block"], short_stack=e["short_stack"], refill_min=e["refill_min"],
-                 postpone_min=e.get("postpone_min", 0))
+                 postpone_min=e.get("postpone_min", 0), sort_bits=e.get("sort_bits", 0))
         ctx.set_trace_config(**cfg)
         return cfg
 

@@ -69,7 +69,8 @@ std::vector<RT::TraceConfig> Candidates() {
 }
 
 fnd_rt_trace_config ToAbi(const RT::TraceConfig& c) {
-    return fnd_rt_trace_config{(uint32_t)c.block, (uint32_t)c.short_stack, c.refill_min, c.postpone_min};
+    return fnd_rt_trace_config{(uint32_t)c.block, (uint32_t)c.short_stack, c.refill_min, c.postpone_min,
+                               c.sort_bits};
 }
 
 RT::TraceConfig FromAbi(const fnd_rt_trace_config& a) {
@@ -78,14 +79,16 @@ RT::TraceConfig FromAbi(const fnd_rt_trace_config& a) {
     c.short_stack = (int)a.short_stack;
     c.refill_min = a.refill_min;
     c.postpone_min = a.postpone_min;
+    c.sort_bits = a.sort_bits;
     return c;
 }
 
 // Times every candidate shape: one warm-up launch, then the best of `reps`
-// CUDA-event-timed launches on the context stream.
+// CUDA-event-timed launches on the context stream. With `sort_stage`, the
+// winning shape is then timed with every coherence-order key width.
 RT::TraceConfig RunTuner(fnd_rt_ctx* ctx, uint32_t reps,
                          const std::function<cudaError_t(const RT::TraceConfig&)>& launch, fnd_rt_tune_entry* table,
-                         uint32_t table_cap, uint32_t* table_n) {
+                         uint32_t table_cap, uint32_t* table_n, bool sort_stage = false) {
     cudaEvent_t e0, e1;
     CUDA_CHECK(cudaEventCreate(&e0));
     CUDA_CHECK(cudaEventCreate(&e1));
@@ -93,7 +96,7 @@ RT::TraceConfig RunTuner(fnd_rt_ctx* ctx, uint32_t reps,
     float best_ms = 1e30f;
     uint32_t k = 0;
     try {
-        for (const RT::TraceConfig& c : Candidates()) {
+        auto time_one = [&](const RT::TraceConfig& c) {
             CUDA_CHECK(launch(c));
             float ms = 1e30f;
             for (uint32_t r = 0; r < std::max(1u, reps); ++r) {
@@ -110,6 +113,15 @@ RT::TraceConfig RunTuner(fnd_rt_ctx* ctx, uint32_t reps,
             if (ms < best_ms) {
                 best_ms = ms;
                 best = c;
+            }
+        };
+        for (const RT::TraceConfig& c : Candidates()) time_one(c);
+        if (sort_stage) {
+            const RT::TraceConfig shape = best;
+            for (uint32_t bits : {9u, 12u, 15u, 18u, 21u}) {
+                RT::TraceConfig c = shape;
+                c.sort_bits = bits;
+                time_one(c);
             }
         }
     } catch (...) {
@@ -155,8 +167,8 @@ int fnd_rt_set_trace_config(fnd_rt_ctx* ctx, const fnd_rt_trace_config* config) 
     return Guard(ctx, [&] {
         const RT::TraceConfig c = FromAbi(*config);
         CHECK_CODE(RT::ValidTraceConfig(c), FND_ERR_INVALID_ARG,
-                   "launch shape block %u / short stack %u / refill %u / postpone %u", config->block,
-                   config->short_stack, config->refill_min, config->postpone_min);
+                   "launch shape block %u / short stack %u / refill %u / postpone %u / sort bits %u", config->block,
+                   config->short_stack, config->refill_min, config->postpone_min, config->sort_bits);
         ctx->trace_cfg = c;
         ctx->refill_min = c.refill_min;
     });
@@ -191,9 +203,9 @@ int fnd_rt_tune(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays,
         const RT::TraceConfig b = RunTuner(
             ctx, reps,
             [&](const RT::TraceConfig& c) {
-                return RT::LaunchTraceConfigured(L, any, false, c, CApi::TraceGrid(ctx, c, any ? 1 : 0), ctx->stream);
+                return CApi::LaunchTraceOrdered(ctx, scene, L, any, false, c, CApi::TraceGrid(ctx, c, any ? 1 : 0));
             },
-            table, table_cap, table_n);
+            table, table_cap, table_n, true);
         if (best) *best = ToAbi(b);
     });
 }

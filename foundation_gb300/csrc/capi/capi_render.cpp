@@ -6,6 +6,7 @@
 // A call renders width*height*spp paths in waves of `capacity` paths. Each
 // wave is a fixed kernel sequence on the context stream; queue lengths stay
 // on the device, so the host never waits inside a frame.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -87,11 +88,18 @@ bool Normalize(double v[3]) {
     return true;
 }
 
-// One wave's bounce loop: extend -> shade -> shadow -> resolve, max_depth times.
+// One wave's bounce loop: extend -> shade -> shadow -> resolve, max_depth
+// times. After each bounce but the last, the tail megakernel finishes the
+// wave when at most `tail_paths` paths continue (tail_paths 0: never).
 void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffers& B, const PT::RenderParams& R,
-                const PT::ShadeScene& S, const PT::CacheIO& C, uint32_t max_depth, int grid_shade) {
+                const PT::ShadeScene& S, const PT::CacheIO& C, uint32_t max_depth, int grid_shade,
+                uint32_t tail_paths) {
     const int g_closest = CApi::TraceGrid(ctx, ctx->trace_cfg, 0);
     const int g_any = CApi::TraceGrid(ctx, ctx->trace_cfg, 1);
+    if (tail_paths && ctx->tail_blocks_per_sm == 0) ctx->tail_blocks_per_sm = PT::TailBlocksPerSm();
+    const int g_tail = ctx->sm_count * std::max(1, ctx->tail_blocks_per_sm);
+    RT::TraceConfig cfg0 = ctx->trace_cfg;
+    cfg0.sort_bits = 0;
     for (uint32_t b = 0; b < max_depth; ++b) {
         const int cur = (int)(b & 1u), nxt = cur ^ 1;
         RT::TraceLaunch L{};
@@ -104,7 +112,9 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
         L.counter = ctx->d_counter;
         L.status = ctx->d_status;
         L.refill_min = ctx->refill_min;
-        CUDA_CHECK(RT::LaunchTraceConfigured(L, false, false, ctx->trace_cfg, g_closest, ctx->stream));
+        // camera rays keep their (already coherent) order; later bounces and
+        // shadow rays take the context's coherence ordering, if any
+        CUDA_CHECK(CApi::LaunchTraceOrdered(ctx, scene, L, false, false, b == 0 ? cfg0 : ctx->trace_cfg, g_closest));
         CUDA_CHECK(cudaMemsetAsync(B.counts + nxt, 0, sizeof(uint32_t), ctx->stream));
         CUDA_CHECK(cudaMemsetAsync(B.counts + PT::kCountShadow, 0, sizeof(uint32_t), ctx->stream));
         CUDA_CHECK(PT::LaunchShade(B, R, S, C, cur, b, grid_shade, ctx->stream));
@@ -118,8 +128,22 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
         A.counter = ctx->d_counter;
         A.status = ctx->d_status;
         A.refill_min = ctx->refill_min;
-        CUDA_CHECK(RT::LaunchTraceConfigured(A, true, false, ctx->trace_cfg, g_any, ctx->stream));
+        CUDA_CHECK(CApi::LaunchTraceOrdered(ctx, scene, A, true, false, ctx->trace_cfg, g_any));
         CUDA_CHECK(PT::LaunchResolve(B, grid_shade, ctx->stream));
+        if (tail_paths && b + 1 < max_depth) {
+            PT::TailArgs T{};
+            T.scene = scene->view;
+            T.B = B;
+            T.R = R;
+            T.S = S;
+            T.C = C;
+            T.q = nxt;
+            T.bounce = b + 1;
+            T.threshold = tail_paths;
+            T.status = ctx->d_status;
+            T.ray_stats = ctx->d_render_stats;
+            CUDA_CHECK(PT::LaunchTail(T, g_tail, ctx->stream));
+        }
     }
 }
 
@@ -295,6 +319,13 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         PT::PathBuffers& B = ctx->paths;
         const int grid_shade = std::max(1, std::min<int>((int)((cap + 255) / 256), ctx->sm_count * 8));
         CUDA_CHECK(cudaMemsetAsync(ctx->d_render_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        // tail megakernel threshold: by default two paths per resident tail thread
+        if (ctx->tail_blocks_per_sm == 0) ctx->tail_blocks_per_sm = PT::TailBlocksPerSm();
+        const uint32_t tail_paths =
+            (D.flags & FND_RENDER_WAVEFRONT)
+                ? 0u
+                : (D.tail_paths ? D.tail_paths
+                                : 2u * (uint32_t)ctx->sm_count * (uint32_t)ctx->tail_blocks_per_sm * PT::kTailBlock);
         PT::CacheIO C{};
         if (use_cache) {
             // 1) training, on the cache's own stream so it overlaps the render
@@ -338,7 +369,7 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
             const uint32_t wave_n = (uint32_t)std::min<uint64_t>(cap, total - wave_base);
             if (use_cache) CUDA_CHECK(cudaMemsetAsync(C.query_count, 0, sizeof(uint32_t), ctx->stream));
             CUDA_CHECK(PT::LaunchGenerate(B, R, wave_base, wave_n, ctx->stream));
-            RunBounces(ctx, scene, B, R, S, C, D.max_depth, grid_shade);
+            RunBounces(ctx, scene, B, R, S, C, D.max_depth, grid_shade, tail_paths);
             if (use_cache) {
                 CUDA_CHECK(cudaStreamWaitEvent(ctx->stream, ctx->cache->ev_trained, 0));
                 CUDA_CHECK(NRC::Infer(ctx->cache->net, C.queries, C.query_count, C.query_cap, B.fb,

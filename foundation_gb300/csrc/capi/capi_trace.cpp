@@ -56,6 +56,31 @@ void EnsureDevice(void*& ptr, size_t& cap, size_t bytes) {
     cap = want;
 }
 
+cudaError_t LaunchTraceOrdered(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, RT::TraceLaunch L, bool any, bool stats,
+                               const RT::TraceConfig& cfg, int grid) {
+    L.order = nullptr;
+    if (cfg.sort_bits && L.n > 1 && scene->view.num_nodes) {
+        const size_t m = size_t(1) << cfg.sort_bits;
+        const size_t need = sizeof(uint32_t) * (2 * (size_t)L.n + m + RT::kMaxSortTiles) + 1024;
+        EnsureDevice(ctx->d_sort, ctx->d_sort_cap, need);
+        auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+        char* p = static_cast<char*>(ctx->d_sort);
+        RT::RaySortBuffers B{};
+        B.keys = reinterpret_cast<uint32_t*>(p);
+        p += align(sizeof(uint32_t) * (size_t)L.n);
+        B.order = reinterpret_cast<uint32_t*>(p);
+        p += align(sizeof(uint32_t) * (size_t)L.n);
+        B.hist = reinterpret_cast<uint32_t*>(p);
+        p += align(sizeof(uint32_t) * m);
+        B.sums = reinterpret_cast<uint32_t*>(p);
+        const cudaError_t e = RT::LaunchRaySort(L.rays, L.n, L.n_dev, scene->info.bounds_lo, scene->info.bounds_hi,
+                                                cfg.sort_bits, B, ctx->stream);
+        if (e != cudaSuccess) return e;
+        L.order = B.order;
+    }
+    return RT::LaunchTraceConfigured(L, any, stats, cfg, grid, ctx->stream);
+}
+
 int ReadStatus(fnd_rt_ctx* ctx) {
     CUDA_CHECK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
@@ -145,6 +170,7 @@ int fnd_rt_destroy(fnd_rt_ctx* ctx) {
     if (ctx->d_paths) cudaFree(ctx->d_paths);
     if (ctx->d_fb) cudaFree(ctx->d_fb);
     if (ctx->d_rgb) cudaFree(ctx->d_rgb);
+    if (ctx->d_sort) cudaFree(ctx->d_sort);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -387,7 +413,7 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
         if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
         const int variant = (any ? 1 : 0) + (stats ? 2 : 0);
         const int grid = TraceGrid(ctx, ctx->trace_cfg, variant);
-        CUDA_CHECK(RT::LaunchTraceConfigured(L, any, stats != nullptr, ctx->trace_cfg, grid, ctx->stream));
+        CUDA_CHECK(LaunchTraceOrdered(ctx, scene, L, any, stats != nullptr, ctx->trace_cfg, grid));
         if (stats) {
             unsigned long long h[2] = {0, 0};
             CUDA_CHECK(cudaMemcpyAsync(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));

@@ -10,6 +10,7 @@
 #include "../../../include/fnd_rt.h"
 #include "../core/core.hpp"
 #include "../pt/integrator.hpp"
+#include "../rt/ray_sort.hpp"
 #include "../rt/traverse_launch.hpp"
 
 #include <vector>
@@ -62,6 +63,9 @@ struct fnd_rt_ctx {
     float* d_rgb = nullptr;  // finalize target for host outputs
     size_t rgb_cap = 0;
     unsigned long long* d_render_stats = nullptr;  // [0] extension rays, [1] shadow rays
+    int tail_blocks_per_sm = 0;                    // occupancy of the tail megakernel (0: not yet queried)
+    void* d_sort = nullptr;                        // coherence-order scratch (rt/ray_sort.hpp)
+    size_t d_sort_cap = 0;
     fnd_render_stats last_render{};
     FndCacheState* cache = nullptr;
     std::string last_error;
@@ -123,6 +127,12 @@ int ReadStatus(fnd_rt_ctx* ctx);
 // Persistent grid (SMs x resident blocks) of a traversal variant under a
 // launch shape (variant as in RT::TraceOccupancyFor).
 int TraceGrid(fnd_rt_ctx* ctx, const Foundation::RT::TraceConfig& cfg, int variant);
+
+// Launches a traversal under a launch shape; with cfg.sort_bits the rays
+// (L.n, or *L.n_dev when set) are first put in coherence order over the
+// scene box (context scratch), otherwise taken in input order.
+cudaError_t LaunchTraceOrdered(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, Foundation::RT::TraceLaunch L, bool any,
+                               bool stats, const Foundation::RT::TraceConfig& cfg, int grid);
 
 // Radiance-cache session storage (capi_cache.cpp).
 void FreeCache(fnd_rt_ctx* ctx);

@@ -20,6 +20,7 @@
 
 #include "../../../include/fnd_rt.h"
 #include "pt_math.cuh"
+#include "shade.cuh"
 
 namespace Foundation {
 namespace PT {
@@ -58,6 +59,8 @@ __global__ void __launch_bounds__(kBlock) generate_kernel(const PathBuffers B, c
         B.counts[kCountExt0] = wave_n;
         B.counts[kCountExt1] = 0;
         B.counts[kCountShadow] = 0;
+        B.counts[kCountTailDone] = 0;
+        B.counts[kCountTailFetch] = 0;
     }
     if (i >= wave_n) return;
     const uint64_t npix = (uint64_t)R.width * R.height;
@@ -93,147 +96,55 @@ __global__ void __launch_bounds__(kBlock) shade_kernel(const PathBuffers B, cons
         const uint2 hit = B.hits[j];
         const float4 r0 = B.ext_rays[cur][2 * (size_t)j];
         const float4 r1 = B.ext_rays[cur][2 * (size_t)j + 1];
-        float4 beta4 = B.beta[slot];
+        const float4 beta4 = B.beta[slot];
         const uint4 rs = B.rng[slot];
         Pcg32 rng;
         rng.state = (uint64_t)rs.x | ((uint64_t)rs.y << 32);
         rng.inc = ((uint64_t)rs.z << 1) | 1u;
         const uint32_t pixel = rs.w & ~kQueryNextFlag;
-        uint32_t flags = rs.w & kQueryNextFlag;
-        float3 beta = xyz(beta4);
-        const float3 o = xyz(r0), d = xyz(r1);
-
-        bool want_shadow = false, want_sun = false, want_next = false, want_query = false;
-        NRC::CachePoint cp;
-        float3 sh_o, sh_d, sh_c, sun_c, next_d, surf_o = f3(0.f, 0.f, 0.f);
-        float sh_tmax = 0.0f;
-        if (hit.x == FND_INVALID_ID) {
-            const float3 L = beta * ld3(R.sky);
-            if (max3(L) > 0.0f) add_radiance(B.fb, pixel, L);
-        } else {
-            const float t = __uint_as_float(hit.y);
-            const float4 sh = S.tri_shade[hit.x];
-            const DevMaterial M = S.materials[min(__float_as_uint(sh.w), S.num_materials - 1u)];
-            const uint32_t type = __float_as_uint(M.albedo_type.w);
-            const float3 ng = xyz(sh);
-            const float dn = dot(d, ng);
-            const float3 p = o + d * t;
-            if (type == kMatEmissive) {
-                const float3 Le = xyz(M.emission_light);
-                if (dn < 0.0f && max3(Le) > 0.0f) {
-                    float w = 1.0f;
-                    const int li = __float_as_int(M.emission_light.w);
-                    if (bounce > 0 && li >= 0 && (uint32_t)li < S.num_lights) {
-                        const float area = S.lights[li].corner_area.w;
-                        const float pdf_l = t * t / (-dn * area * (float)S.num_lights);
-                        w = power_heuristic(beta4.w, pdf_l);
-                    }
-                    add_radiance(B.fb, pixel, beta * Le * w);
-                }
-            } else if (kMode == 1u && flags) {
-                // cache query: the network supplies this vertex's reflected radiance
-                const float3 nrm = dn < 0.0f ? ng : -ng;
-                cp.p_rough = make_float4(p.x, p.y, p.z, type == kMatLambert ? 1.0f : M.params.x);
-                cp.wo_aux = make_float4(-d.x, -d.y, -d.z, __uint_as_float(pixel));
-                cp.n_pad = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
-                cp.albedo = M.albedo_type;
-                cp.beta = make_float4(beta.x, beta.y, beta.z, 0.0f);
-                want_query = true;
-            } else {
-                const float3 nrm = dn < 0.0f ? ng : -ng;
-                float3 tb, bb;
-                onb(nrm, tb, bb);
-                const float3 wo = f3(-dot(d, tb), -dot(d, bb), -dot(d, nrm));
-                const float3 albedo = xyz(M.albedo_type);
-                const float alpha = M.params.x;
-                const float3 po = p + nrm * R.eps;
-                surf_o = po;
-                if (kMode == 1u && (type == kMatLambert || alpha >= C.specular_alpha)) flags = kQueryNextFlag;
-                // next-event estimation: one quad light
-                const float ul = rng.uniform(), u1 = rng.uniform(), u2 = rng.uniform();
-                if (S.num_lights > 0) {
-                    const uint32_t k = min((uint32_t)(ul * (float)S.num_lights), S.num_lights - 1u);
-                    const DevQuadLight Lq = S.lights[k];
-                    const float3 y = xyz(Lq.corner_area) + xyz(Lq.eu) * u1 + xyz(Lq.ev) * u2;
-                    float3 wl = y - po;
-                    const float d2 = dot(wl, wl);
-                    const float dist = sqrtf(d2);
-                    wl = wl * (1.0f / dist);
-                    const float cos_l = -dot(wl, xyz(Lq.normal));
-                    const float cos_x = dot(wl, nrm);
-                    if (cos_l > 0.0f && cos_x > 0.0f) {
-                        const float3 wi = f3(dot(wl, tb), dot(wl, bb), cos_x);
-                        const BsdfEval ev = eval_bsdf(type, albedo, alpha, wo, wi);
-                        const float pdf_l = d2 / (cos_l * Lq.corner_area.w * (float)S.num_lights);
-                        const float w = power_heuristic(pdf_l, ev.pdf);
-                        sh_c = beta * ev.f * xyz(Lq.radiance) * (cos_x * w / pdf_l);
-                        if (max3(sh_c) > 0.0f) {
-                            want_shadow = true;
-                            sh_o = po;
-                            sh_d = wl;
-                            sh_tmax = dist * (1.0f - 1e-3f);
-                        }
-                    }
-                }
-                if (R.has_sun) {
-                    const float3 sd = ld3(R.sun_dir);
-                    const float cos_x = dot(sd, nrm);
-                    if (cos_x > 0.0f) {
-                        const float3 wi = f3(dot(sd, tb), dot(sd, bb), cos_x);
-                        const BsdfEval ev = eval_bsdf(type, albedo, alpha, wo, wi);
-                        sun_c = beta * ev.f * ld3(R.sun_E) * cos_x;
-                        want_sun = max3(sun_c) > 0.0f;
-                    }
-                }
-                // continuation
-                const float ub1 = rng.uniform(), ub2 = rng.uniform(), urr = rng.uniform();
-                if (bounce + 1 < R.max_depth) {
-                    const BsdfSample bs = sample_bsdf(type, albedo, alpha, wo, ub1, ub2);
-                    if (bs.ok) {
-                        beta = beta * bs.weight;
-                        bool alive = max3(beta) > 0.0f;
-                        if (alive && bounce >= R.rr_start) {
-                            const float q = fminf(fmaxf(max3(beta), 0.05f), 1.0f);
-                            if (urr >= q)
-                                alive = false;
-                            else
-                                beta = beta * (1.0f / q);
-                        }
-                        if (alive) {
-                            want_next = true;
-                            next_d = tb * bs.wi.x + bb * bs.wi.y + nrm * bs.wi.z;
-                            beta4 = make_float4(beta.x, beta.y, beta.z, bs.pdf);
-                        }
-                    }
-                }
-            }
-        }
+        VertexIn in;
+        in.o = xyz(r0);
+        in.d = xyz(r1);
+        in.hit = hit.x != FND_INVALID_ID;
+        in.prim = hit.x;
+        in.t = __uint_as_float(hit.y);
+        in.beta = xyz(beta4);
+        in.last_pdf = beta4.w;
+        in.query_here = (rs.w & kQueryNextFlag) != 0u;
+        VertexOut v;
+        shade_vertex<kMode>(R, S, C.specular_alpha, bounce, R.max_depth, in, rng, v);
+        if (max3(v.add) > 0.0f) add_radiance(B.fb, pixel, v.add);
         // queue appends (all lanes of `active` take part)
-        const uint32_t ks = append_slot(B.counts + kCountShadow, want_shadow, active);
-        if (want_shadow) {
-            B.sh_rays[2 * (size_t)ks] = make_float4(sh_o.x, sh_o.y, sh_o.z, 0.0f);
-            B.sh_rays[2 * (size_t)ks + 1] = make_float4(sh_d.x, sh_d.y, sh_d.z, sh_tmax);
+        const uint32_t ks = append_slot(B.counts + kCountShadow, v.shadow, active);
+        if (v.shadow) {
+            B.sh_rays[2 * (size_t)ks] = make_float4(v.surf_o.x, v.surf_o.y, v.surf_o.z, 0.0f);
+            B.sh_rays[2 * (size_t)ks + 1] = make_float4(v.sh_d.x, v.sh_d.y, v.sh_d.z, v.sh_tmax);
             B.sh_pixel[ks] = pixel;
-            B.sh_contrib[ks] = make_float4(sh_c.x, sh_c.y, sh_c.z, 0.0f);
+            B.sh_contrib[ks] = make_float4(v.sh_c.x, v.sh_c.y, v.sh_c.z, 0.0f);
         }
-        const uint32_t kz = append_slot(B.counts + kCountShadow, want_sun, active);
-        if (want_sun) {
-            B.sh_rays[2 * (size_t)kz] = make_float4(surf_o.x, surf_o.y, surf_o.z, 0.0f);
+        const uint32_t kz = append_slot(B.counts + kCountShadow, v.sun, active);
+        if (v.sun) {
+            B.sh_rays[2 * (size_t)kz] = make_float4(v.surf_o.x, v.surf_o.y, v.surf_o.z, 0.0f);
             B.sh_rays[2 * (size_t)kz + 1] = make_float4(R.sun_dir[0], R.sun_dir[1], R.sun_dir[2],
                                                         __int_as_float(0x7F800000));
             B.sh_pixel[kz] = pixel;
-            B.sh_contrib[kz] = make_float4(sun_c.x, sun_c.y, sun_c.z, 0.0f);
+            B.sh_contrib[kz] = make_float4(v.sun_c.x, v.sun_c.y, v.sun_c.z, 0.0f);
         }
         if (kMode == 1u) {
-            const uint32_t kq = append_slot(C.query_count, want_query, active);
-            if (want_query && kq < C.query_cap) C.queries[kq] = cp;
+            const uint32_t kq = append_slot(C.query_count, v.query, active);
+            if (v.query && kq < C.query_cap) {
+                v.cp.wo_aux.w = __uint_as_float(pixel);
+                C.queries[kq] = v.cp;
+            }
         }
-        const uint32_t kn = append_slot(B.counts + nxt, want_next, active);
-        if (want_next) {
-            B.ext_rays[nxt][2 * (size_t)kn] = make_float4(surf_o.x, surf_o.y, surf_o.z, 0.0f);
-            B.ext_rays[nxt][2 * (size_t)kn + 1] = make_float4(next_d.x, next_d.y, next_d.z, __int_as_float(0x7F800000));
+        const uint32_t kn = append_slot(B.counts + nxt, v.next, active);
+        if (v.next) {
+            const uint32_t flags = (rs.w & kQueryNextFlag) | (v.query_next ? kQueryNextFlag : 0u);
+            B.ext_rays[nxt][2 * (size_t)kn] = make_float4(v.surf_o.x, v.surf_o.y, v.surf_o.z, 0.0f);
+            B.ext_rays[nxt][2 * (size_t)kn + 1] =
+                make_float4(v.next_d.x, v.next_d.y, v.next_d.z, __int_as_float(0x7F800000));
             B.ext_path[nxt][kn] = slot;
-            B.beta[slot] = beta4;
+            B.beta[slot] = make_float4(v.beta.x, v.beta.y, v.beta.z, v.pdf);
             B.rng[slot] = make_uint4((uint32_t)rng.state, (uint32_t)(rng.state >> 32), rs.z, pixel | flags);
         }
     }

@@ -104,8 +104,34 @@ cudaError_t LaunchTrainingPaths(const TrainPathsArgs& A, cudaStream_t s);
 
 constexpr uint32_t kQueryNextFlag = 0x80000000u;  // in PathBuffers::rng.w
 
-// Statistics counters appended after the queue counts.
+// Statistics counters appended after the queue counts; the tail kernel's
+// block-completion and path-fetch counters (reset by generate).
 constexpr int kCountExt0 = 0, kCountExt1 = 1, kCountShadow = 2, kStatExt = 4, kStatShadow = 6;  // 64-bit at 4, 6
+constexpr int kCountTailDone = 8, kCountTailFetch = 9;
+
+// The tail of a wave: once the extension queue `q` (the paths that continue
+// to interaction `bounce`) holds at most `threshold` paths, one persistent
+// megakernel finishes every one of them (lanes fetch paths dynamically and
+// run them to the end with single-ray traversal and the shade stage's
+// vertex logic) and empties the queue, so the remaining wavefront stages of
+// the wave find nothing to do. Above the threshold it returns at once.
+// Results are those of the wavefront stages: same random numbers per path,
+// same hits; only the order of the frame-buffer additions differs.
+struct TailArgs {
+    RT::DeviceScene scene;
+    PathBuffers B;
+    RenderParams R;
+    ShadeScene S;
+    CacheIO C;
+    int q;
+    uint32_t bounce;
+    uint32_t threshold;
+    uint32_t* status;
+    unsigned long long* ray_stats;  // [0] extension rays, [1] shadow rays
+};
+cudaError_t LaunchTail(const TailArgs& A, int grid, cudaStream_t s);
+int TailBlocksPerSm();  // resident tail blocks per SM (occupancy)
+constexpr int kTailBlock = 128;
 
 cudaError_t LaunchGenerate(const PathBuffers& B, const RenderParams& R, uint64_t wave_base, uint32_t wave_n,
                            cudaStream_t s);

@@ -1,9 +1,9 @@
 // train_paths.cu — the radiance cache's training paths as one megakernel.
 //
 // Each thread follows one training path from the camera through a random
-// pixel to its end (at most max_depth interactions) with the same light
-// transport as the wavefront stages (integrator.cu): NEE with MIS to the quad
-// lights, the sun, the sky, Russian roulette. Every non-emissive vertex
+// pixel to its end (at most max_depth interactions) with the vertex logic of
+// the wavefront stages (shade.cuh): NEE with MIS to the quad lights, the sun,
+// the sky, Russian roulette. Every non-emissive vertex
 // becomes a training sample whose target is the radiance the path collected
 // after that vertex divided by the throughput that reached it (an unbiased
 // single-path estimate of the reflected radiance there).
@@ -17,6 +17,7 @@
 #include "../rt/traverse.cuh"
 #include "integrator.hpp"
 #include "pt_math.cuh"
+#include "shade.cuh"
 
 namespace Foundation {
 namespace PT {
@@ -26,7 +27,6 @@ constexpr int kBlock = 128;
 constexpr int kMaxDepthTrain = 16;
 
 __device__ __forceinline__ float3 ld3(const float* p) { return f3(p[0], p[1], p[2]); }
-__device__ __forceinline__ float3 xyz(float4 v) { return f3(v.x, v.y, v.z); }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t v) {
     const uint32_t s = v * 747796405u + 2891336453u;
@@ -63,98 +63,42 @@ __global__ void __launch_bounds__(kBlock) training_paths_kernel(const TrainPaths
         float3 beta = f3(1.f, 1.f, 1.f);
         float last_pdf = 0.0f;
         for (uint32_t bounce = 0; bounce < depth; ++bounce) {
-            const RT::RayState rs = make_ray(o, d, __int_as_float(0x7F800000));
+            VertexIn in;
             float t = __int_as_float(0x7F800000);
             uint32_t prim;
-            if (!RT::trace_single<false>(A.scene, rs, t, prim, A.status)) {
-                total = total + beta * ld3(R.sky);
-                break;
+            in.hit = RT::trace_single<false>(A.scene, make_ray(o, d, t), t, prim, A.status);
+            in.o = o;
+            in.d = d;
+            in.prim = prim;
+            in.t = t;
+            in.beta = beta;
+            in.last_pdf = last_pdf;
+            in.query_here = false;
+            VertexOut v;
+            shade_vertex<2u>(R, S, 0.0f, bounce, depth, in, rng, v);
+            total = total + v.add;
+            if (v.sample) {
+                pts[ns] = v.cp;
+                before[ns] = total;
+                ns++;
             }
-            const float4 sh = S.tri_shade[prim];
-            const DevMaterial M = S.materials[min(__float_as_uint(sh.w), S.num_materials - 1u)];
-            const uint32_t type = __float_as_uint(M.albedo_type.w);
-            const float3 ng = xyz(sh);
-            const float dn = dot(d, ng);
-            const float3 p = o + d * t;
-            if (type == kMatEmissive) {
-                const float3 Le = xyz(M.emission_light);
-                if (dn < 0.0f && max3(Le) > 0.0f) {
-                    float w = 1.0f;
-                    const int li = __float_as_int(M.emission_light.w);
-                    if (bounce > 0 && li >= 0 && (uint32_t)li < S.num_lights) {
-                        const float pdf_l = t * t / (-dn * S.lights[li].corner_area.w * (float)S.num_lights);
-                        w = power_heuristic(last_pdf, pdf_l);
-                    }
-                    total = total + beta * Le * w;
-                }
-                break;
+            if (v.shadow) {
+                float ts = v.sh_tmax;
+                uint32_t sp;
+                if (!RT::trace_single<true>(A.scene, make_ray(v.surf_o, v.sh_d, ts), ts, sp, A.status))
+                    total = total + v.sh_c;
             }
-            const float3 nrm = dn < 0.0f ? ng : -ng;
-            float3 tb, bb;
-            onb(nrm, tb, bb);
-            const float3 wo = f3(-dot(d, tb), -dot(d, bb), -dot(d, nrm));
-            const float3 albedo = xyz(M.albedo_type);
-            const float alpha = M.params.x;
-            const float3 po = p + nrm * R.eps;
-            // training sample at this vertex
-            NRC::CachePoint& cp = pts[ns];
-            cp.p_rough = make_float4(p.x, p.y, p.z, type == kMatLambert ? 1.0f : alpha);
-            cp.wo_aux = make_float4(-d.x, -d.y, -d.z, 0.0f);
-            cp.n_pad = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
-            cp.albedo = M.albedo_type;
-            cp.beta = make_float4(beta.x, beta.y, beta.z, 0.0f);
-            before[ns] = total;
-            ns++;
-            // next-event estimation
-            const float ul = rng.uniform(), u1 = rng.uniform(), u2 = rng.uniform();
-            if (S.num_lights > 0) {
-                const uint32_t k = min((uint32_t)(ul * (float)S.num_lights), S.num_lights - 1u);
-                const DevQuadLight Lq = S.lights[k];
-                const float3 y = xyz(Lq.corner_area) + xyz(Lq.eu) * u1 + xyz(Lq.ev) * u2;
-                float3 wl = y - po;
-                const float d2 = dot(wl, wl);
-                const float dist = sqrtf(d2);
-                wl = wl * (1.0f / dist);
-                const float cos_l = -dot(wl, xyz(Lq.normal));
-                const float cos_x = dot(wl, nrm);
-                if (cos_l > 0.0f && cos_x > 0.0f) {
-                    const BsdfEval ev = eval_bsdf(type, albedo, alpha, wo, f3(dot(wl, tb), dot(wl, bb), cos_x));
-                    const float pdf_l = d2 / (cos_l * Lq.corner_area.w * (float)S.num_lights);
-                    const float3 c = beta * ev.f * xyz(Lq.radiance) * (cos_x * power_heuristic(pdf_l, ev.pdf) / pdf_l);
-                    if (max3(c) > 0.0f) {
-                        float ts = dist * (1.0f - 1e-3f);
-                        uint32_t sp;
-                        if (!RT::trace_single<true>(A.scene, make_ray(po, wl, ts), ts, sp, A.status)) total = total + c;
-                    }
-                }
+            if (v.sun) {
+                float ts = __int_as_float(0x7F800000);
+                uint32_t sp;
+                if (!RT::trace_single<true>(A.scene, make_ray(v.surf_o, ld3(R.sun_dir), ts), ts, sp, A.status))
+                    total = total + v.sun_c;
             }
-            if (R.has_sun) {
-                const float3 sd = ld3(R.sun_dir);
-                const float cos_x = dot(sd, nrm);
-                if (cos_x > 0.0f) {
-                    const BsdfEval ev = eval_bsdf(type, albedo, alpha, wo, f3(dot(sd, tb), dot(sd, bb), cos_x));
-                    const float3 c = beta * ev.f * ld3(R.sun_E) * cos_x;
-                    if (max3(c) > 0.0f) {
-                        float ts = __int_as_float(0x7F800000);
-                        uint32_t sp;
-                        if (!RT::trace_single<true>(A.scene, make_ray(po, sd, ts), ts, sp, A.status)) total = total + c;
-                    }
-                }
-            }
-            const float ub1 = rng.uniform(), ub2 = rng.uniform(), urr = rng.uniform();
-            if (bounce + 1 >= depth) break;
-            const BsdfSample bs = sample_bsdf(type, albedo, alpha, wo, ub1, ub2);
-            if (!bs.ok) break;
-            beta = beta * bs.weight;
-            if (!(max3(beta) > 0.0f)) break;
-            if (bounce >= R.rr_start) {
-                const float q = fminf(fmaxf(max3(beta), 0.05f), 1.0f);
-                if (urr >= q) break;
-                beta = beta * (1.0f / q);
-            }
-            last_pdf = bs.pdf;
-            o = po;
-            d = tb * bs.wi.x + bb * bs.wi.y + nrm * bs.wi.z;
+            if (!v.next) break;
+            last_pdf = v.pdf;
+            beta = v.beta;
+            o = v.surf_o;
+            d = v.next_d;
         }
     }
     // compact the warp's samples: one atomic per warp

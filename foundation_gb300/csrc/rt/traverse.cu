@@ -23,6 +23,7 @@
 #include <cfloat>
 
 #include "traverse.cuh"
+#include "ray_sort.hpp"
 #include "traverse_launch.hpp"
 
 namespace Foundation {
@@ -48,8 +49,10 @@ struct SingleSource {
     const float4* rays;
     void* hits;
     uint8_t* occluded;
+    const uint32_t* order;  // fetch position -> ray index (coherence order), or null
     uint32_t n;
     struct Lane {};
+    __device__ __forceinline__ uint32_t map(uint32_t pos) const { return order ? __ldg(order + pos) : pos; }
     __device__ __forceinline__ void load(uint32_t id, float4& r0, float4& r1, Lane&) const {
         r0 = __ldcs(rays + 2 * (size_t)id);
         r1 = __ldcs(rays + 2 * (size_t)id + 1);
@@ -79,6 +82,7 @@ struct BatchSource {
         DeviceScene scene;
         bool any;
     };
+    __device__ __forceinline__ uint32_t map(uint32_t pos) const { return pos; }
     __device__ __forceinline__ void load(uint32_t id, float4& r0, float4& r1, Lane& ln) const {
         uint32_t lo = 0, hi = njobs;  // prefix[lo] <= id < prefix[hi]
         while (hi - lo > 1) {
@@ -139,8 +143,9 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
             base = __shfl_sync(kFull, base, 0);
             if (base + cnt >= n) exhausted = true;
             if (!active) {
-                const uint32_t id = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                if (id < n) {
+                const uint32_t pos = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (pos < n) {
+                    const uint32_t id = src.map(pos);
                     float4 r0, r1;
                     src.load(id, r0, r1, ln);
                     if (kKind == 2) any_hit = src.any_of(ln, false);
@@ -289,6 +294,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const 
     src.rays = L.rays;
     src.hits = L.hits;
     src.occluded = L.occluded;
+    src.order = L.order;
     src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
     if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
     const Common C{L.counter, L.status, L.stats, L.refill_min, L.postpone_min};
@@ -351,7 +357,8 @@ int normalized_block(int b) { return b == 64 || b == 256 ? b : 128; }
 bool ValidTraceConfig(const TraceConfig& c) {
     return (c.block == 64 || c.block == 128 || c.block == 256) &&
            (c.short_stack == 4 || c.short_stack == 8 || c.short_stack == 16) && c.refill_min >= 1 &&
-           c.refill_min <= 32 && c.postpone_min <= 32 && c.blocks_per_sm >= 0 && c.blocks_per_sm <= 32;
+           c.refill_min <= 32 && c.postpone_min <= 32 && c.blocks_per_sm >= 0 && c.blocks_per_sm <= 32 &&
+           ValidSortBits(c.sort_bits);
 }
 
 cudaError_t TraceOccupancy(int variant, int* blocks_per_sm) {

@@ -26,6 +26,7 @@ struct TraceLaunch {
     unsigned long long* stats;  // [0] node fetches, [1] triangle tests (stats variants)
     uint32_t refill_min;        // refill a warp once this many lanes are idle
     uint32_t postpone_min;      // triangle postponement threshold (0: off)
+    const uint32_t* order;      // fetch position -> ray index (ray_sort.hpp), or null: input order
 };
 
 // Launch shape of a traversal kernel (the autotuner's search space).
@@ -35,6 +36,7 @@ struct TraceConfig {
     uint32_t refill_min = 8;             // 1..32 idle lanes before a warp refills
     uint32_t postpone_min = 0;           // postpone triangles when fewer lanes have them (0: never)
     int blocks_per_sm = 0;               // 0: as many as fit
+    uint32_t sort_bits = 0;              // coherence order key bits (ray_sort.hpp), 0: input order
 };
 bool ValidTraceConfig(const TraceConfig& c);
 

@@ -43,6 +43,7 @@ MAT_LAMBERT, MAT_GGX, MAT_EMISSIVE = 0, 1, 2
 RENDER_ACCUMULATE = 1
 BVH_SPATIAL_SPLITS = 1
 RENDER_CACHE = 2
+RENDER_WAVEFRONT = 4
 CACHE_NUM_PARAMS = 22720
 CACHE_NUM_FEATURES = 96
 
@@ -85,7 +86,7 @@ class _RenderDesc(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32), ("max_depth", C.c_uint32),
                 ("rr_start", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64), ("camera", _Camera),
                 ("sky", C.c_float * 3), ("sun_dir", C.c_float * 3), ("sun_irradiance", C.c_float * 3),
-                ("wave_paths", C.c_uint32)]
+                ("wave_paths", C.c_uint32), ("tail_paths", C.c_uint32)]
 
 
 class RenderStats(C.Structure):
@@ -95,11 +96,11 @@ class RenderStats(C.Structure):
 
 class TraceConfig(C.Structure):
     _fields_ = [("block", C.c_uint32), ("short_stack", C.c_uint32), ("refill_min", C.c_uint32),
-                ("postpone_min", C.c_uint32)]
+                ("postpone_min", C.c_uint32), ("sort_bits", C.c_uint32)]
 
     def as_dict(self):
         return dict(block=self.block, short_stack=self.short_stack, refill_min=self.refill_min,
-                    postpone_min=self.postpone_min)
+                    postpone_min=self.postpone_min, sort_bits=self.sort_bits)
 
 
 class TuneEntry(C.Structure):
@@ -256,16 +257,18 @@ class Context:
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
                sun_irradiance=(0.0, 0.0, 0.0), accumulate: bool = False, wave_paths: int = 0, out=None,
-               cache: bool = False):
+               cache: bool = False, tail_paths: int = 0, wavefront: bool = False):
         """Path-traces spp samples per pixel. Host: returns (height, width, 3)
         float32 mean radiance. Device: out is a CUDA tensor of
-        width*height*3 floats, filled asynchronously."""
+        width*height*3 floats, filled asynchronously. tail_paths: threshold
+        of the tail megakernel (0: automatic); wavefront: never use it."""
         cam = _Camera((C.c_float * 3)(*camera["eye"]), (C.c_float * 3)(*camera["target"]),
                       (C.c_float * 3)(*camera.get("up", (0.0, 1.0, 0.0))), camera.get("vfov_deg", 45.0))
-        flags = (RENDER_ACCUMULATE if accumulate else 0) | (RENDER_CACHE if cache else 0)
+        flags = (RENDER_ACCUMULATE if accumulate else 0) | (RENDER_CACHE if cache else 0) | \
+            (RENDER_WAVEFRONT if wavefront else 0)
         d = _RenderDesc(width, height, spp, max_depth, rr_start, flags, seed, cam,
                         (C.c_float * 3)(*sky), (C.c_float * 3)(*sun_dir), (C.c_float * 3)(*sun_irradiance),
-                        wave_paths)
+                        wave_paths, tail_paths)
         if out is not None and _is_device(out):
             _check(load().fnd_rt_render(self._h, scene.handle, C.byref(d), _ptr(out), FND_MEM_DEVICE), self._h)
             return out
@@ -274,8 +277,9 @@ class Context:
         return img
 
     # ---- launch shape -------------------------------------------------
-    def set_trace_config(self, block: int = 128, short_stack: int = 8, refill_min: int = 8, postpone_min: int = 0):
-        c = TraceConfig(block, short_stack, refill_min, postpone_min)
+    def set_trace_config(self, block: int = 128, short_stack: int = 8, refill_min: int = 8, postpone_min: int = 0,
+                         sort_bits: int = 0):
+        c = TraceConfig(block, short_stack, refill_min, postpone_min, sort_bits)
         _check(load().fnd_rt_set_trace_config(self._h, C.byref(c)), self._h)
 
     def trace_config(self) -> dict:

@@ -201,6 +201,11 @@ typedef struct fnd_rt_trace_config {
     uint32_t refill_min;   /* 1..32 idle lanes before a warp refills */
     uint32_t postpone_min; /* postpone a node's triangles while fewer than this many lanes
                               of the warp have triangles to test (0..32, 0: never) */
+    uint32_t sort_bits;    /* 0: rays traced in input order; 6..21 (multiple of 3): rays
+                              first bucketed by origin cell (Morton order on a grid over
+                              the scene box) and direction octant, a key of this many
+                              bits; results are unchanged, only the schedule. Single-scene
+                              traces and the path tracer's secondary and shadow rays. */
 } fnd_rt_trace_config;
 
 typedef struct fnd_rt_tune_entry {
@@ -213,7 +218,8 @@ enum { FND_QUERY_CLOSEST = 0, FND_QUERY_ANY = 1 };
 int fnd_rt_set_trace_config(fnd_rt_ctx* ctx, const fnd_rt_trace_config* config);
 int fnd_rt_get_trace_config(const fnd_rt_ctx* ctx, fnd_rt_trace_config* out);
 /* Times every launch shape on n device rays (FND_QUERY_CLOSEST / _ANY) with
- * `reps` timed runs each; fills up to table_cap entries, *table_n, *best
+ * `reps` timed runs each, then the best shape with each coherence-order key
+ * width (sort time included); fills up to table_cap entries, *table_n, *best
  * (the context keeps its own config; apply *best with fnd_rt_set_trace_config). */
 int fnd_rt_tune(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n, uint32_t kind,
                 uint32_t reps, fnd_rt_tune_entry* table, uint32_t table_cap, uint32_t* table_n,
@@ -288,7 +294,9 @@ typedef struct fnd_camera {
     float vfov_deg;
 } fnd_camera;
 
-enum { FND_RENDER_ACCUMULATE = 1u };
+/* FND_RENDER_WAVEFRONT: run every bounce as wavefront stages (no tail
+ * megakernel; for comparison and testing, same results). */
+enum { FND_RENDER_ACCUMULATE = 1u, FND_RENDER_WAVEFRONT = 4u };
 
 typedef struct fnd_render_desc {
     uint32_t width, height;
@@ -302,6 +310,8 @@ typedef struct fnd_render_desc {
     float sun_dir[3];      /* towards the sun; zero vector: no sun */
     float sun_irradiance[3];
     uint32_t wave_paths;   /* paths in flight per wave, 0: automatic */
+    uint32_t tail_paths;   /* once at most this many paths of a wave remain, one
+                              megakernel finishes them; 0: automatic */
 } fnd_render_desc;
 
 typedef struct fnd_render_stats {
@@ -333,7 +343,7 @@ int fnd_rt_render_stats_get(fnd_rt_ctx* ctx, fnd_render_stats* out);
  * `train_steps` optimiser steps on their vertices, then renders: paths end at
  * the vertex after their first non-specular bounce, where the network
  * supplies the reflected radiance. The plain tracer (no flag) stays the
- * fallback and the judge of the cache's error. No reference counterpart
+ * unbiased estimator against which the cache's error is measured. No reference counterpart
  * (the reference has no ray tracer); the session state lives in the context
  * like the renderer's per-frame resources (src/Renderer/Renderer.hpp:13-36). */
 enum { FND_RENDER_CACHE = 2u };

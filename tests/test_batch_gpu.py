@@ -93,11 +93,14 @@ def test_tuner_and_launch_shapes_keep_parity(ctx):
     rays = S.incoherent_rays(1 << 18, *cs.bounds, seed=31)
     rd = torch.from_numpy(rays).cuda()
     best, table = ctx.tune(s, rd, reps=1)
-    assert len(table) == 72 and all(e["ms"] > 0 for e in table)
+    # 72 launch shapes, then the best one with 5 coherence-order key widths
+    assert len(table) == 77 and all(e["ms"] > 0 for e in table)
+    assert [e["sort_bits"] for e in table[72:]] == [9, 12, 15, 18, 21]
     ref = O.OracleBVH(cs.verts, cs.idx).closest(rays)
-    for cfg in (best, dict(block=64, short_stack=4, refill_min=1, postpone_min=0),
-                dict(block=256, short_stack=16, refill_min=32, postpone_min=8),
-                dict(block=128, short_stack=4, refill_min=8, postpone_min=32)):
+    for cfg in (best, dict(block=64, short_stack=4, refill_min=1, postpone_min=0, sort_bits=0),
+                dict(block=256, short_stack=16, refill_min=32, postpone_min=8, sort_bits=6),
+                dict(block=128, short_stack=4, refill_min=8, postpone_min=32, sort_bits=21),
+                dict(block=128, short_stack=8, refill_min=8, postpone_min=0, sort_bits=15)):
         ctx.set_trace_config(**cfg)
         assert ctx.trace_config() == cfg
         h = s.closest(rays)
@@ -105,5 +108,8 @@ def test_tuner_and_launch_shapes_keep_parity(ctx):
         assert np.array_equal(h["t"].view(np.uint32), ref["t"].view(np.uint32))
     with pytest.raises(fg.FndError):
         ctx.set_trace_config(block=96)
+    for bad in (3, 10, 24):
+        with pytest.raises(fg.FndError):
+            ctx.set_trace_config(sort_bits=bad)
     ctx.set_trace_config()
     s.close()

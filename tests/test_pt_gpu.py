@@ -106,3 +106,33 @@ def test_render_argument_errors(ctx):
     img = ctx.render(s, 8, 8, 1, S.CORNELL_CAMERA)  # context still usable
     assert np.isfinite(img).all()
     s.close()
+
+
+@pytest.mark.parametrize("cache", [False, True])
+def test_tail_megakernel_matches_wavefront(ctx, cache):
+    """The tail megakernel runs the same paths as the wavefront stages: the
+    same extension and shadow ray counts, and images equal up to the order of
+    the frame-buffer additions. Thresholds: never (wavefront), everything
+    from the second interaction on, and the automatic one; and the wavefront
+    with coherence-ordered secondary and shadow rays."""
+    cs = S.cornell_scene()
+    s = upload(ctx, cs)
+    kw = dict(seed=5, sky=(0.05, 0.06, 0.08), sun_dir=(0.3, 1.0, 0.2), sun_irradiance=(0.5, 0.5, 0.4))
+    if cache:
+        ctx.cache_create(s, train_paths=4096, train_steps=0, batch=1024, seed=3)
+    imgs, stats = [], []
+    # the last variant also puts secondary and shadow rays in coherence order
+    for opts, bits in ((dict(wavefront=True), 0), (dict(tail_paths=1 << 28), 0), (dict(), 0),
+                       (dict(wavefront=True), 15)):
+        ctx.set_trace_config(sort_bits=bits)
+        imgs.append(ctx.render(s, 96, 54, 64, S.CORNELL_CAMERA, cache=cache, **kw, **opts))
+        st = ctx.render_stats()
+        stats.append((st["extension_rays"], st["shadow_rays"]))
+    ctx.set_trace_config()
+    assert len(set(stats)) == 1, stats
+    assert stats[0][0] > 96 * 54 * 64
+    for img in imgs[1:]:
+        np.testing.assert_allclose(img, imgs[0], rtol=1e-4, atol=1e-6)
+    if cache:
+        ctx.cache_destroy()
+    s.close()

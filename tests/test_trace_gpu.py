@@ -71,8 +71,20 @@ def test_soup_1m_tris(ctx):
     sc = ctx.upload(so.verts, so.idx)
     rays = S.incoherent_rays(1 << 19, (0, 0, 0), (1, 1, 1), seed=2)
     b = O.OracleBVH(so.verts, so.idx)
-    assert_same(sc.closest(rays), b.closest(rays))
+    ref = b.closest(rays)
+    assert_same(sc.closest(rays), ref)
+    # coherence order changes the schedule only
+    for bits in (9, 18, 21):
+        ctx.set_trace_config(sort_bits=bits)
+        assert_same(sc.closest(rays), ref)
+        assert np.array_equal(sc.any(rays), b.any(rays))
+    ctx.set_trace_config()
     sc.close()
+    # spatial splits: references duplicated across leaves, same hits
+    ss = ctx.upload(so.verts, so.idx, spatial_splits=True)
+    assert ss.info()["num_refs"] > len(so.idx)
+    assert_same(ss.closest(rays), ref)
+    ss.close()
 
 
 def test_device_pointers_and_stats(ctx):
