@@ -29,6 +29,11 @@ COMMON = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-pthread,-W
 # host sources: contraction off so host float code matches its stated
 # expression trees on both x86-64 and aarch64 hosts
 HOST_FLAGS = ["-Xcompiler", "-ffp-contract=off"]
+# path-tracing stages: the vertex logic (pt/shade.cuh) is inlined into the
+# wavefront shade kernel, the tail megakernel and the training megakernel;
+# without contraction the three evaluate it to the same bits, so a path gives
+# the same result whichever kernel runs it
+PT_FLAGS = ["-fmad=false"]
 
 
 def nvcc() -> str:
@@ -65,6 +70,8 @@ def _compile(src: str, force: bool, newest_header: float) -> tuple[str, bool]:
     cmd = [nvcc(), *ARCH, *COMMON]
     if src.endswith(".cpp"):
         cmd += HOST_FLAGS
+    elif os.path.basename(os.path.dirname(src)) == "pt":
+        cmd += PT_FLAGS
     cmd += ["-c", src, "-o", obj + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

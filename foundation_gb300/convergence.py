@@ -8,8 +8,8 @@ time_to_relmse runs frames until the accumulated image reaches the target:
  * plain: `spp_per_frame` samples per frame, accumulated from frame 0;
  * cache: 1 sample per frame with the radiance cache (each frame also runs
    the cache's training paths and optimiser steps); the first `warmup`
-   frames train the cache without entering the accumulated image, and their
-   time counts.
+   frames only train the cache (training paths and optimiser steps, no
+   image), and their time counts.
 Render time is measured with CUDA events on the pass's stream; the relMSE
 checks between frames are outside the timed region.
 """
@@ -52,7 +52,7 @@ def time_to_relmse(ctx, scene, ref, width, height, camera, *, mode: str = "plain
         accumulate = f > warmup if cache else f > 0
         e0.record(st)
         ctx.render(scene, width, height, spp_per_frame, camera, seed=seed + f, accumulate=accumulate, cache=cache,
-                   out=out, **kw)
+                   out=out, train_only=cache and f < warmup, **kw)
         e1.record(st)
         ctx.sync()
         t_ms += e0.elapsed_time(e1)

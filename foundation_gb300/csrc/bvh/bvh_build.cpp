@@ -217,7 +217,7 @@ private:
                 }
             }
         }
-        const double split_cost = best_axis >= 0 ? 1.0 + best / area : DBL_MAX;
+        const double split_cost = best_axis >= 0 ? (double)m_p.trav_cost + best / area : DBL_MAX;
         const bool leaf = n <= m_p.max_leaf && (best_axis < 0 || (double)n <= split_cost);
         if (leaf) {
             nd.a = t.begin;
@@ -237,7 +237,7 @@ private:
             std::sort(prims + t.begin, prims + t.end);
             mid = t.begin + n / 2;
         }
-        sah += area;
+        sah += (double)m_p.trav_cost * area;
         const uint32_t left = m_next.fetch_add(2);
         CHECK_CODE(left + 1 < m_out.nodes.size(), FND_ERR_INVALID_SCENE, "BVH node pool exhausted");
         nd.a = left;
@@ -267,6 +267,7 @@ void BuildBinaryBvh(const float* tri, uint32_t nt, const BuildParams& params, Bi
     CHECK(nt > 0);
     CHECK(params.bins >= 2 && params.bins <= 64);
     CHECK(params.max_leaf >= 1 && params.max_leaf <= 4);
+    CHECK(params.trav_cost > 0.0f && params.trav_cost <= 64.0f);
     Builder b(tri, nt, params, out);
     b.Run();
 }

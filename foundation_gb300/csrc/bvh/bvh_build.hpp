@@ -4,9 +4,11 @@
 // Hierarchies"): per node, bin triangle bounding-box centroids into K bins
 // along each axis with non-zero centroid extent, sweep bin bounds from both
 // ends, split where C_trav + C_isect * (A_L N_L + A_R N_R) / A_node is least
-// (C_trav = C_isect = 1, half surface areas, first minimum wins, axes in
-// x, y, z order); make a leaf when the node holds at most max_leaf triangles
-// and the leaf cost N is not above the split cost; when all centroids of a
+// (C_isect = 1, C_trav = trav_cost, 1 by default; half surface areas, first
+// minimum wins, axes in x, y, z order); make a leaf when the node holds at
+// most max_leaf triangles and the leaf cost N is not above the split cost.
+// A larger trav_cost gives fuller leaves, hence fewer binary nodes and
+// fuller 8-wide nodes after the collapse; when all centroids of a
 // node coincide, split at the median of the triangle indices. The tree this
 // produces is a function of the triangle set only (not of thread timing).
 #pragma once
@@ -39,6 +41,7 @@ struct BuildParams {
     uint32_t bins = 32;
     uint32_t max_leaf = 4;
     uint32_t threads = 0;          // 0: hardware concurrency
+    float trav_cost = 1.0f;        // SAH cost of a traversal step relative to a triangle test
     bool spatial_splits = false;   // BuildBinarySbvh only
     float spatial_alpha = 1e-5f;   // try spatial splits when child overlap > alpha x root half area
     double max_refs_factor = 2.0;  // at most this many references per triangle in total

@@ -253,7 +253,7 @@ private:
                 if (sp.cost < best.cost) best = sp;
             }
         }
-        const double split_cost = best.axis >= 0 ? 1.0 + best.cost / area : DBL_MAX;
+        const double split_cost = best.axis >= 0 ? (double)m_p.trav_cost + best.cost / area : DBL_MAX;
         if (n <= m_p.max_leaf && (best.axis < 0 || (double)n <= split_cost)) {
             MakeLeaf(refs, out, node, area);
             return false;
@@ -307,7 +307,7 @@ private:
                 }
             }
         }
-        out.sah += area;
+        out.sah += (double)m_p.trav_cost * area;
         return true;
     }
 

@@ -239,9 +239,13 @@ int fnd_rt_scene_set_lights(fnd_rt_scene* scene, const fnd_quad_light* lights, u
 int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_desc* desc, float* rgb, int mem) {
     if (!ctx) return FND_ERR_INVALID_ARG;
     return Guard(ctx, [&] {
-        CHECK(scene != nullptr && scene->ctx == ctx && desc != nullptr && rgb != nullptr);
+        CHECK(scene != nullptr && scene->ctx == ctx && desc != nullptr);
         CHECK(mem == FND_MEM_HOST || mem == FND_MEM_DEVICE);
         const fnd_render_desc& D = *desc;
+        const bool train_only = (D.flags & FND_RENDER_TRAIN_ONLY) != 0;
+        CHECK_CODE(rgb != nullptr || train_only, FND_ERR_INVALID_ARG, "rgb is NULL");
+        CHECK_CODE(!train_only || (D.flags & FND_RENDER_CACHE), FND_ERR_INVALID_ARG,
+                   "FND_RENDER_TRAIN_ONLY needs FND_RENDER_CACHE");
         CHECK_CODE(D.width > 0 && D.height > 0 && (uint64_t)D.width * D.height <= (1ull << 26), FND_ERR_INVALID_ARG,
                    "image %ux%u out of range", D.width, D.height);
         CHECK_CODE(D.spp >= 1 && D.max_depth >= 1 && D.max_depth <= 64, FND_ERR_INVALID_ARG,
@@ -258,25 +262,28 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         CHECK_CODE(!use_cache || ctx->cache != nullptr, FND_ERR_INVALID_ARG,
                    "FND_RENDER_CACHE needs a cache (fnd_rt_cache_create)");
         const uint32_t train_paths = use_cache ? ctx->cache->desc.train_paths : 0u;
-        EnsurePathBuffers(ctx, cap);
+        if (!train_only) EnsurePathBuffers(ctx, cap);
         if (use_cache) CApi::EnsureCacheBuffers(ctx, cap, D.max_depth);
         // frame buffer (restart unless accumulating into a frame of the same size)
+        const bool keep_fb = train_only;
         const bool accumulate = (D.flags & FND_RENDER_ACCUMULATE) && ctx->d_fb && ctx->fb_width == D.width &&
                                 ctx->fb_height == D.height;
-        if (ctx->fb_pixels < npix) {
+        if (!keep_fb && ctx->fb_pixels < npix) {
             if (ctx->d_fb) CUDA_CHECK(cudaFree(ctx->d_fb));
             ctx->d_fb = nullptr;
             ctx->fb_pixels = 0;
             CUDA_CHECK(cudaMalloc(&ctx->d_fb, sizeof(float4) * (size_t)npix));
             ctx->fb_pixels = npix;
         }
-        if (!accumulate) {
-            CUDA_CHECK(cudaMemsetAsync(ctx->d_fb, 0, sizeof(float4) * (size_t)npix, ctx->stream));
-            ctx->fb_samples = 0;
+        if (!keep_fb) {
+            if (!accumulate) {
+                CUDA_CHECK(cudaMemsetAsync(ctx->d_fb, 0, sizeof(float4) * (size_t)npix, ctx->stream));
+                ctx->fb_samples = 0;
+            }
+            ctx->fb_width = D.width;
+            ctx->fb_height = D.height;
+            ctx->paths.fb = ctx->d_fb;
         }
-        ctx->fb_width = D.width;
-        ctx->fb_height = D.height;
-        ctx->paths.fb = ctx->d_fb;
         // camera basis (lookAt convention)
         double eye[3] = {D.camera.eye[0], D.camera.eye[1], D.camera.eye[2]};
         double tgt[3] = {D.camera.target[0], D.camera.target[1], D.camera.target[2]};
@@ -357,6 +364,13 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
                                           Mix32(tseed, st + 1), cd.learning_rate, grid_train, ts));
             CUDA_CHECK(cudaEventRecord(cs.ev_trained, ts));
             cs.frames++;
+            if (train_only) {
+                // later work on the context stream sees the trained network
+                CUDA_CHECK(cudaStreamWaitEvent(ctx->stream, cs.ev_trained, 0));
+                ctx->last_render = fnd_render_stats{};
+                ctx->last_render.samples_accumulated = ctx->fb_samples;
+                return;
+            }
             // 2) render waves end their paths in cache queries
             C.mode = 1;
             C.specular_alpha = cd.specular_alpha;

@@ -209,7 +209,10 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             if (bvh->sah_bins) bp.bins = bvh->sah_bins;
             if (bvh->max_leaf_tris) bp.max_leaf = bvh->max_leaf_tris;
             bp.threads = bvh->build_threads;
+            if (bvh->traversal_cost != 0.0f) bp.trav_cost = bvh->traversal_cost;
         }
+        CHECK_CODE(bp.trav_cost > 0.0f && bp.trav_cost <= 64.0f, FND_ERR_INVALID_ARG, "traversal_cost %g not in (0, 64]",
+                   (double)bp.trav_cost);
         CHECK_CODE(bp.bins >= 2 && bp.bins <= 64, FND_ERR_INVALID_ARG, "sah_bins %u not in [2, 64]", bp.bins);
         CHECK_CODE(bp.max_leaf >= 1 && bp.max_leaf <= 4, FND_ERR_INVALID_ARG, "max_leaf_tris %u not in [1, 4]",
                    bp.max_leaf);

@@ -104,9 +104,31 @@ __device__ __forceinline__ bool intersect_tri(const RayState& r, float4 v0, floa
     return true;
 }
 
-// uint8 -> float without I2F: byte into the mantissa of 2^23, subtract 2^23.
-__device__ __forceinline__ float byte_to_float(uint32_t word, uint32_t sel) {
-    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | sel)) - 8388608.0f;
+// 2^23 + byte, exactly: the byte placed in the low mantissa bits of 2^23.
+__device__ __forceinline__ float byte_plus_2p23(uint32_t word, uint32_t sel) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | sel));
+}
+
+// max / min of three (one instruction on the sm_100 family; NaN operands
+// are dropped like nested fmaxf / fminf, which tests/test_minmax_gpu.py
+// checks on the GPU).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fminf(fminf(a, b), c);
+#endif
 }
 
 // Tests the 8 child boxes of one compressed node against the ray.
@@ -143,19 +165,29 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
     const uint32_t gy0 = fy ? w2.z : w4.x, gy1 = fy ? w2.w : w4.y;
     const uint32_t nz0 = fz ? w4.z : w3.x, nz1 = fz ? w4.w : w3.y;
     const uint32_t gz0 = fz ? w3.x : w4.z, gz1 = fz ? w3.y : w4.w;
+    // A plane's t is q * s + b with q the quantised byte. The byte is read
+    // as the float 2^23 + q (one PRMT) and the 2^23 * s is folded into the
+    // offset, near planes rounded down and far planes up:
+    //   near: rd((2^23+q) s + rd(b - 2^23 s)) <= rd(q s + b) <= rn(q s + b)
+    //   far:  ru((2^23+q) s + ru(b - 2^23 s)) >= ru(q s + b) >= rn(q s + b)
+    // so every child box is at least as wide as under round-to-nearest
+    // fma(q, s, b), the culling stays conservative and the hits exact.
+    const float bnx = __fmaf_rd(-8388608.0f, sx, bx), bfx = __fmaf_ru(-8388608.0f, sx, bx);
+    const float bny = __fmaf_rd(-8388608.0f, sy, by), bfy = __fmaf_ru(-8388608.0f, sy, by);
+    const float bnz = __fmaf_rd(-8388608.0f, sz, bz), bfz = __fmaf_ru(-8388608.0f, sz, bz);
     uint32_t hits = 0, tris = 0;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const uint32_t sel = (uint32_t)(s & 3);
         const uint32_t meta = __byte_perm(s < 4 ? w1.z : w1.w, 0u, 0x4440u | sel);
-        const float tnx = __fmaf_rn(byte_to_float(s < 4 ? nx0 : nx1, sel), sx, bx);
-        const float tny = __fmaf_rn(byte_to_float(s < 4 ? ny0 : ny1, sel), sy, by);
-        const float tnz = __fmaf_rn(byte_to_float(s < 4 ? nz0 : nz1, sel), sz, bz);
-        const float tfx = __fmaf_rn(byte_to_float(s < 4 ? gx0 : gx1, sel), sx, bx);
-        const float tfy = __fmaf_rn(byte_to_float(s < 4 ? gy0 : gy1, sel), sy, by);
-        const float tfz = __fmaf_rn(byte_to_float(s < 4 ? gz0 : gz1, sel), sz, bz);
-        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tfar));
+        const float tnx = __fmaf_rd(byte_plus_2p23(s < 4 ? nx0 : nx1, sel), sx, bnx);
+        const float tny = __fmaf_rd(byte_plus_2p23(s < 4 ? ny0 : ny1, sel), sy, bny);
+        const float tnz = __fmaf_rd(byte_plus_2p23(s < 4 ? nz0 : nz1, sel), sz, bnz);
+        const float tfx = __fmaf_ru(byte_plus_2p23(s < 4 ? gx0 : gx1, sel), sx, bfx);
+        const float tfy = __fmaf_ru(byte_plus_2p23(s < 4 ? gy0 : gy1, sel), sy, bfy);
+        const float tfz = __fmaf_ru(byte_plus_2p23(s < 4 ? gz0 : gz1, sel), sz, bfz);
+        const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
+        const float tf = min3f(tfx, tfy, fminf(tfz, tfar));
         if (meta != 0u && tn <= tf) {
             if (imask & (1u << s)) {
                 hits |= 1u << ((uint32_t)s ^ r.oct);

@@ -44,6 +44,7 @@ RENDER_ACCUMULATE = 1
 BVH_SPATIAL_SPLITS = 1
 RENDER_CACHE = 2
 RENDER_WAVEFRONT = 4
+RENDER_TRAIN_ONLY = 8
 CACHE_NUM_PARAMS = 22720
 CACHE_NUM_FEATURES = 96
 
@@ -60,7 +61,7 @@ class _Desc(C.Structure):
 
 class _BvhDesc(C.Structure):
     _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("build_threads", C.c_uint32),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("traversal_cost", C.c_float)]
 
 
 class SceneInfo(C.Structure):
@@ -251,24 +252,28 @@ class Context:
         self.close()
 
     def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0,
-               spatial_splits: bool = False) -> "Scene":
-        return Scene(self, verts, idx, bins, max_leaf, threads, spatial_splits)
+               spatial_splits: bool = False, traversal_cost: float = 0.0) -> "Scene":
+        return Scene(self, verts, idx, bins, max_leaf, threads, spatial_splits, traversal_cost)
 
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
                sun_irradiance=(0.0, 0.0, 0.0), accumulate: bool = False, wave_paths: int = 0, out=None,
-               cache: bool = False, tail_paths: int = 0, wavefront: bool = False):
+               cache: bool = False, tail_paths: int = 0, wavefront: bool = False, train_only: bool = False):
         """Path-traces spp samples per pixel. Host: returns (height, width, 3)
         float32 mean radiance. Device: out is a CUDA tensor of
         width*height*3 floats, filled asynchronously. tail_paths: threshold
-        of the tail megakernel (0: automatic); wavefront: never use it."""
+        of the tail megakernel (0: automatic); wavefront: never use it;
+        train_only (with cache): only train the cache, render nothing."""
         cam = _Camera((C.c_float * 3)(*camera["eye"]), (C.c_float * 3)(*camera["target"]),
                       (C.c_float * 3)(*camera.get("up", (0.0, 1.0, 0.0))), camera.get("vfov_deg", 45.0))
         flags = (RENDER_ACCUMULATE if accumulate else 0) | (RENDER_CACHE if cache else 0) | \
-            (RENDER_WAVEFRONT if wavefront else 0)
+            (RENDER_WAVEFRONT if wavefront else 0) | (RENDER_TRAIN_ONLY if train_only else 0)
         d = _RenderDesc(width, height, spp, max_depth, rr_start, flags, seed, cam,
                         (C.c_float * 3)(*sky), (C.c_float * 3)(*sun_dir), (C.c_float * 3)(*sun_irradiance),
                         wave_paths, tail_paths)
+        if train_only:
+            _check(load().fnd_rt_render(self._h, scene.handle, C.byref(d), None, FND_MEM_DEVICE), self._h)
+            return None
         if out is not None and _is_device(out):
             _check(load().fnd_rt_render(self._h, scene.handle, C.byref(d), _ptr(out), FND_MEM_DEVICE), self._h)
             return out
@@ -359,12 +364,13 @@ class Context:
 
 
 class Scene:
-    def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0, spatial_splits=False):
+    def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0, spatial_splits=False,
+                 traversal_cost=0.0):
         self._h = None
         self.ctx = ctx
         v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
-        bd = _BvhDesc(bins, max_leaf, threads, BVH_SPATIAL_SPLITS if spatial_splits else 0)
+        bd = _BvhDesc(bins, max_leaf, threads, BVH_SPATIAL_SPLITS if spatial_splits else 0, traversal_cost)
         h = C.c_void_p()
         _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),
                ctx.handle)

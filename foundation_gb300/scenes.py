@@ -19,6 +19,9 @@ shapes follow the workloads the path-tracer pass is measured on:
 * ``incoherent_rays`` origins uniform in a box, directions uniform on S^2
 * ``soup_scene``      triangle soup in the unit cube, edge lengths
                       log-uniform in [1e-3, 0.1] (seed 2)
+* ``terrain_scene``   value-noise heightfield (2237^2 vertices, 9,999,392
+                      tris) plus 4,096 level-4 icospheres (20,971,520 tris),
+                      sun + sky (seed 3)
 """
 from __future__ import annotations
 
@@ -306,6 +309,82 @@ def soup_scene(n: int, seed: int = 2, stream_base: int = 0) -> Scene:
     v = np.stack([p, p + d1 * l1[:, None], p + d2 * l2[:, None]], 1).astype(np.float32)
     f = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
     return Scene(v.reshape(-1, 3), f, bounds=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), name=f"soup{n}")
+
+
+def value_noise(x: np.ndarray, z: np.ndarray, seed: int, octaves: int = 8, amplitude: float = 0.2) -> np.ndarray:
+    """Value noise on [0,1]^2: octave o has a (2^(o+2)+1)^2 lattice of values
+    uniform in [-1, 1) (one PCG32 stream per lattice point, seed ``seed``),
+    blended with smoothstep weights t^2 (3 - 2t); octaves are summed with
+    weights 2^-o and scaled so the sum lies in [-amplitude, amplitude)."""
+    x = np.asarray(x, np.float64)
+    z = np.asarray(z, np.float64)
+    h = np.zeros(np.broadcast(x, z).shape, np.float64)
+    wsum = 0.0
+    base = 0
+    for o in range(octaves):
+        f = 1 << (o + 2)
+        g = Pcg32Streams(seed, np.arange(base, base + (f + 1) * (f + 1), dtype=np.uint64))
+        lat = (g.next_f64() * 2.0 - 1.0).reshape(f + 1, f + 1)
+        base += (f + 1) * (f + 1)
+        fx, fz = x * f, z * f
+        ix = np.minimum(np.floor(fx).astype(np.int64), f - 1)
+        iz = np.minimum(np.floor(fz).astype(np.int64), f - 1)
+        tx, tz = fx - ix, fz - iz
+        sx, sz = tx * tx * (3.0 - 2.0 * tx), tz * tz * (3.0 - 2.0 * tz)
+        a = lat[ix, iz] * (1.0 - sx) + lat[ix + 1, iz] * sx
+        b = lat[ix, iz + 1] * (1.0 - sx) + lat[ix + 1, iz + 1] * sx
+        w = 1.0 / (1 << o)
+        h += w * (a * (1.0 - sz) + b * sz)
+        wsum += w
+    return h * (amplitude / wsum)
+
+
+def terrain_scene(grid: int = 2237, instances: int = 4096, level: int = 4, seed: int = 3) -> Scene:
+    """Large scene: a heightfield over [0,1]^2 on a ``grid`` x ``grid`` vertex
+    lattice ((grid-1)^2 x 2 triangles; 9,999,392 for 2237), heights from
+    8-octave value noise (seed ``seed``, amplitude 0.2), and ``instances``
+    icospheres of ``level`` (5,120 tris each at level 4) at positions uniform
+    on the terrain, radii uniform in [0.001, 0.01], resting half sunk into
+    the ground; half Lambertian (albedo U[0.1,0.9]^3), half GGX (roughness
+    U[0.05,0.8]). The instances are stored flattened (one triangle list).
+    Lit by a directional sun and a constant sky (``TERRAIN_LIGHTING``)."""
+    n = grid
+    t = np.arange(n, dtype=np.float64) / float(n - 1)
+    X, Z = np.meshgrid(t, t, indexing="ij")
+    H = value_noise(X, Z, seed)
+    tv = np.stack([X, H, Z], -1).reshape(-1, 3)
+    i = np.arange(n - 1, dtype=np.uint32)
+    I, J = np.meshgrid(i, i, indexing="ij")
+    v00 = (I * n + J).ravel()
+    v01, v10, v11 = v00 + 1, v00 + n, v00 + n + 1
+    # winding with +y normals: (v00, v01, v10) and (v10, v01, v11)
+    tf = np.concatenate([np.stack([v00, v01, v10], 1), np.stack([v10, v01, v11], 1)], 0).astype(np.uint32)
+    parts = [(tv, tf)]
+    mats = [[MAT_LAMBERT, 0.42, 0.38, 0.33, 1.0, 0, 0, 0]]
+    tri_mat = [np.zeros(len(tf), np.uint32)]
+    sv, sf = icosphere(level)
+    g = Pcg32Streams(seed, np.arange(1 << 32, (1 << 32) + instances, dtype=np.uint64))
+    cx, cz = g.next_f64(), g.next_f64()
+    rad = 0.001 + g.next_f64() * 0.009
+    kind = g.next_u32() & np.uint32(1)
+    col = np.stack([0.1 + g.next_f64() * 0.8 for _ in range(3)], 1)
+    rough = 0.05 + g.next_f64() * 0.75
+    cy = value_noise(cx, cz, seed) + 0.5 * rad
+    iv = (sv[None, :, :] * rad[:, None, None] + np.stack([cx, cy, cz], 1)[:, None, :]).reshape(-1, 3)
+    off = (np.arange(instances, dtype=np.uint64) * np.uint64(len(sv)))[:, None, None]
+    if_ = (sf[None, :, :].astype(np.uint64) + off).reshape(-1, 3)
+    parts.append((iv, if_))
+    for k in range(instances):
+        mats.append([MAT_GGX if kind[k] else MAT_LAMBERT, col[k, 0], col[k, 1], col[k, 2],
+                     rough[k] if kind[k] else 1.0, 0, 0, 0])
+    tri_mat.append(np.repeat(np.arange(1, instances + 1, dtype=np.uint32), len(sf)))
+    v, f = _merge(parts)
+    return Scene(v, f, tri_material=np.concatenate(tri_mat), materials=np.asarray(mats, np.float32), lights=[],
+                 bounds=((0.0, -0.2, 0.0), (1.0, 0.25, 1.0)), name=f"terrain{n}x{instances}")
+
+
+TERRAIN_CAMERA = dict(eye=(0.5, 0.42, 1.32), target=(0.5, 0.0, 0.42), up=(0.0, 1.0, 0.0), vfov_deg=40.0)
+TERRAIN_LIGHTING = dict(sky=(0.30, 0.40, 0.55), sun_dir=(0.35, 0.6, 0.25), sun_irradiance=(3.0, 2.8, 2.5))
 
 
 def material_records(scene: Scene) -> np.ndarray:

@@ -87,6 +87,8 @@ typedef struct fnd_rt_bvh_desc {
     uint32_t max_leaf_tris; /* 1..4, default 4 */
     uint32_t build_threads; /* 0: all host cores */
     uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS or 0 */
+    float traversal_cost;   /* SAH cost of a traversal step relative to a triangle
+                               test, (0, 64]; 0: default 1 (the reference tree) */
 } fnd_rt_bvh_desc;
 
 /* Spatial splits (Stich et al. 2009): references of triangles that straddle
@@ -347,6 +349,10 @@ int fnd_rt_render_stats_get(fnd_rt_ctx* ctx, fnd_render_stats* out);
  * (the reference has no ray tracer); the session state lives in the context
  * like the renderer's per-frame resources (src/Renderer/Renderer.hpp:13-36). */
 enum { FND_RENDER_CACHE = 2u };
+/* With FND_RENDER_CACHE: run only the cache's training paths and optimiser
+ * steps of a call (the frame buffer and rgb are untouched; rgb may be NULL),
+ * e.g. to train the cache before its images are accumulated. */
+enum { FND_RENDER_TRAIN_ONLY = 8u };
 
 typedef struct fnd_cache_desc {
     uint32_t train_paths;   /* training paths per render call (65,536) */

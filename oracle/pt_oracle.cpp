@@ -1,7 +1,7 @@
 // pt_oracle.cpp — TEST INFRASTRUCTURE ONLY: FP64 path-tracing oracle.
 //
 // Renders a crop of an image with the light-transport definitions of the
-// device integrator (foundation_gb300/csrc/pt/integrator.cu), evaluated in
+// device integrator (foundation_gb300/csrc/pt/shade.cuh), evaluated in
 // double precision over the oracle's binary BVH: pinhole camera (glm lookAt
 // convention), two-sided surfaces, one-sided black emitters, Lambert and GGX
 // (Walter et al. 2007; height-correlated Smith; Schlick Fresnel; alpha =

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <bit>
+#include <cfenv>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -18,6 +19,17 @@ static inline float __fadd_rn(float a, float b) { return a + b; }
 static inline float __fmul_rn(float a, float b) { return a * b; }
 static inline float __fdiv_rn(float a, float b) { return a / b; }
 static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
+// directed-rounding fma: the host FPU in the requested mode (the harness is
+// built with -frounding-math so the compiler keeps the mode switches)
+static inline float fma_mode(float a, float b, float c, int mode) {
+    const int old = std::fegetround();
+    std::fesetround(mode);
+    volatile float r = std::fma(a, b, c);
+    std::fesetround(old);
+    return r;
+}
+static inline float __fmaf_rd(float a, float b, float c) { return fma_mode(a, b, c, FE_DOWNWARD); }
+static inline float __fmaf_ru(float a, float b, float c) { return fma_mode(a, b, c, FE_UPWARD); }
 static inline double __dmul_rn(double a, double b) { return a * b; }
 static inline double __dsub_rn(double a, double b) { return a - b; }
 static inline float __double2float_rn(double d) { return (float)d; }
@@ -70,8 +82,16 @@ emu_bvh* emu_build(const float* verts, uint32_t nv, const uint32_t* idx, uint32_
     return emu_build2(verts, nv, idx, nt, threads, 0);
 }
 
+emu_bvh* emu_build3(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads,
+                    int spatial, float trav_cost);
+
 emu_bvh* emu_build2(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads,
                     int spatial) {
+    return emu_build3(verts, nv, idx, nt, threads, spatial, 1.0f);
+}
+
+emu_bvh* emu_build3(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads,
+                    int spatial, float trav_cost) {
     auto* e = new emu_bvh();
     std::vector<float> tri(9 * (size_t)nt);
     for (uint32_t t = 0; t < nt; ++t)
@@ -79,6 +99,7 @@ emu_bvh* emu_build2(const float* verts, uint32_t nv, const uint32_t* idx, uint32
             for (int c = 0; c < 3; ++c) tri[9 * (size_t)t + 3 * k + c] = verts[3 * (size_t)idx[3 * (size_t)t + k] + c];
     BuildParams p;
     p.threads = threads;
+    p.trav_cost = trav_cost;
     if (spatial)
         BuildBinarySbvh(tri.data(), nt, p, e->bin);
     else
@@ -111,7 +132,7 @@ void emu_stats(const emu_bvh* e, uint64_t* out, double* sah, float* margin) {
 // Per-ray restatement of trace_kernel's lane logic (same group / stack
 // semantics, same node and triangle tests). max_sp receives the deepest stack.
 void emu_trace(const emu_bvh* e, const float* rays, uint64_t n, uint32_t* hits, int any, uint64_t* stats) {
-    uint64_t nodes = 0, tris = 0, max_sp = 0;
+    uint64_t nodes = 0, tris = 0, max_sp = 0, occupied = 0;
     for (uint64_t i = 0; i < n; ++i) {
         const float* rp = rays + 8 * i;
         const float4 r0{rp[0], rp[1], rp[2], rp[3]}, r1{rp[4], rp[5], rp[6], rp[7]};
@@ -130,6 +151,7 @@ void emu_trace(const emu_bvh* e, const float* rays, uint64_t n, uint32_t* hits, 
                 max_sp = std::max<uint64_t>(max_sp, stack.size());
                 const NodeHits h = intersect_node(r, e->view.nodes, child, best_t);
                 nodes++;
+                for (int k = 0; k < 8; ++k) occupied += e->wide.nodes[child].meta[k] != 0;
                 ng_base = h.child_base;
                 ng_group = h.group;
                 tg_base = h.tri_base;
@@ -168,6 +190,7 @@ void emu_trace(const emu_bvh* e, const float* rays, uint64_t n, uint32_t* hits, 
     stats[0] = nodes;
     stats[1] = tris;
     stats[2] = max_sp;
+    stats[3] = occupied;  // occupied child slots over the visited nodes
 }
 
 // The same rays through RT::trace_single (the per-thread traversal of the

@@ -47,7 +47,7 @@ class Emu:
     def trace(self, rays, any_hit=False):
         rays = np.ascontiguousarray(rays, np.float32)
         out = np.zeros(2 * len(rays), np.uint32)
-        st = np.zeros(3, np.uint64)
+        st = np.zeros(4, np.uint64)
         self.L.emu_trace(self.h, _p(rays), len(rays), _p(out), int(any_hit), _p(st))
         return out[0::2], out[1::2], st
 

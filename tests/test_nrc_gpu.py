@@ -153,3 +153,28 @@ def test_cache_render_beats_plain_at_equal_samples(built):
         print(f"relMSE cache16 {r_cache:.4g} plain16 {r_plain:.4g} cache bias (1024 spp) {bias:.4g}")
         assert r_cache < r_plain
         assert bias < 0.05
+
+
+def test_train_only_frames(built):
+    """FND_RENDER_TRAIN_ONLY runs the training paths and optimiser steps and
+    leaves the frame buffer (and its sample count) as it was."""
+    import foundation_gb300 as fg
+    cs = S.cornell_scene(num_spheres=20, level=2)
+    with fg.Context(0) as ctx:
+        s = ctx.upload(cs.verts, cs.idx)
+        s.set_materials(cs.tri_material, S.material_records(cs))
+        s.set_lights(S.light_records(cs))
+        ctx.cache_create(s, train_paths=8192, train_steps=2, batch=2048, seed=5)
+        a = ctx.render(s, 48, 27, 2, S.CORNELL_CAMERA, seed=1, cache=True)
+        w0 = ctx.cache_weights()
+        assert ctx.render(s, 48, 27, 1, S.CORNELL_CAMERA, seed=2, cache=True, train_only=True) is None
+        st = ctx.cache_stats()
+        assert st["steps"] == 4
+        assert not np.array_equal(ctx.cache_weights(), w0)
+        assert ctx.render_stats()["samples_accumulated"] == 2
+        b = ctx.render(s, 48, 27, 2, S.CORNELL_CAMERA, seed=3, cache=True, accumulate=True)
+        assert ctx.render_stats()["samples_accumulated"] == 4 and np.isfinite(b).all()
+        assert not np.array_equal(a, b)
+        with pytest.raises(fg.FndError):
+            ctx.render(s, 48, 27, 1, S.CORNELL_CAMERA, train_only=True)  # needs the cache flag
+        s.close()
