@@ -484,25 +484,37 @@ def shadow_segments(n: int, seed: int, stream_base: int) -> np.ndarray:
     return rays
 
 
+def batch_plan(num_scenes: int = 256, seed: int = 2, tris=(1000, 500000), rays=(4096, 1 << 20)) -> dict:
+    """Sizes and PCG stream bases of the batched-traversal workload: scene i
+    has nt[i] triangles (streams tri_base[i]...) and nr[i] rays per query
+    kind (closest: camera + random from ray_base[i], any: shadow segments
+    from ray_base[i] + nr[i])."""
+    nt = log_uniform_ints(num_scenes, tris[0], tris[1], seed, 1 << 50)
+    nr = log_uniform_ints(num_scenes, rays[0], rays[1], seed, (1 << 50) + 4096)
+    tri_base = np.concatenate([[0], np.cumsum(nt[:-1].astype(np.int64))]).astype(np.int64)
+    ray_base = (1 << 44) + np.concatenate([[0], np.cumsum(2 * nr[:-1].astype(np.int64))]).astype(np.int64)
+    return dict(seed=seed, nt=nt, nr=nr, tri_base=tri_base, ray_base=ray_base)
+
+
+def batch_item(plan: dict, i: int) -> dict:
+    """Scene i of a batch plan: a triangle soup in the unit cube and its ray
+    batches (half coherent camera rays, half uniform-random rays for closest
+    hit; as many shadow segments for any hit)."""
+    seed = plan["seed"]
+    sc = soup_scene(int(plan["nt"][i]), seed=seed, stream_base=int(plan["tri_base"][i]))
+    n = int(plan["nr"][i])
+    base = int(plan["ray_base"][i])
+    cam = cube_camera_rays(n // 2)
+    rnd = incoherent_rays(n - n // 2, (0, 0, 0), (1, 1, 1), seed=seed, stream_base=base)
+    sh = shadow_segments(n, seed, base + n)
+    return dict(scene=sc, closest=np.concatenate([cam, rnd], 0), any=sh)
+
+
 def batch_workload(num_scenes: int = 256, seed: int = 2, tris=(1000, 500000), rays=(4096, 1 << 20)):
     """The batched-traversal workload: `num_scenes` triangle soups in the unit
     cube (log-uniform triangle counts, edge lengths log-uniform in [1e-3,
     0.1]), each with a ray batch of log-uniform size: half coherent camera
     rays, half uniform-random rays (closest hit), plus as many any-hit
     shadow segments. Returns a list of dicts (scene, closest_rays, any_rays)."""
-    nt = log_uniform_ints(num_scenes, tris[0], tris[1], seed, 1 << 50)
-    nr = log_uniform_ints(num_scenes, rays[0], rays[1], seed, (1 << 50) + 4096)
-    out = []
-    tri_base = 0
-    ray_base = 1 << 44
-    for i in range(num_scenes):
-        sc = soup_scene(int(nt[i]), seed=seed, stream_base=tri_base)
-        tri_base += int(nt[i])
-        n = int(nr[i])
-        cam = cube_camera_rays(n // 2)
-        rnd = incoherent_rays(n - n // 2, (0, 0, 0), (1, 1, 1), seed=seed, stream_base=ray_base)
-        ray_base += n
-        sh = shadow_segments(n, seed, ray_base)
-        ray_base += n
-        out.append(dict(scene=sc, closest=np.concatenate([cam, rnd], 0), any=sh))
-    return out
+    plan = batch_plan(num_scenes, seed, tris, rays)
+    return [batch_item(plan, i) for i in range(num_scenes)]
