@@ -41,7 +41,7 @@ sys.path.insert(0, ROOT)
 N_RAYS = 8_388_608
 METRIC = "Mrays/s closest-hit"
 UNIT = "Mrays/s"
-PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "trace_closest_cornell_incoherent.txt")
+PROFILES = os.path.join(ROOT, "profiles")
 
 
 def parse_args():
@@ -53,17 +53,34 @@ def parse_args():
     p.add_argument("--rays", type=int, default=N_RAYS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the path-tracer and 1M-triangle blocks")
+    p.add_argument("--workload", default="cornell", choices=["cornell", "soup1m"],
+                   help="traversal workload of the timed steps (cornell: the headline)")
+    p.add_argument("--spatial-splits", action="store_true", help="build the scene with spatial splits")
     return p.parse_args()
 
 
-def workload(rank: int, n_rays: int):
+def workload(rank: int, n_rays: int, kind: str = "cornell"):
     from foundation_gb300 import scenes
+    if kind == "soup1m":
+        sc = scenes.soup_scene(1 << 20, seed=2)
+        rays = scenes.incoherent_rays(n_rays, (0, 0, 0), (1, 1, 1), seed=2, stream_base=(1 << 40) + rank * n_rays)
+        return sc, rays
     sc = scenes.cornell_scene()
     rays = scenes.incoherent_rays(n_rays, *sc.bounds, seed=1, stream_base=(1 << 40) + rank * n_rays)
     return sc, rays
 
 
-def config_block(sc, n_rays, world):
+def config_block(sc, n_rays, world, kind: str = "cornell"):
+    if kind == "soup1m":
+        return {
+            "workload": "soup1m incoherent closest-hit",
+            "scene": "1,048,576-triangle soup in the unit cube (seed 2)",
+            "scene_tris": sc.num_tris,
+            "rays_per_step_per_gpu": n_rays,
+            "rays": "origins uniform in the cube, directions uniform on S^2",
+            "l2": "inputs larger than L2: 268 MB of rays streamed per step per GPU",
+            "parallelism": f"replicas x{world}",
+        }
     return {
         "workload": "cornell200 incoherent closest-hit",
         "scene": "Cornell box + 200 level-3 icospheres (seed 1)",
@@ -150,12 +167,13 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def profile_traffic():
+def profile_traffic(kind: str = "cornell"):
     """dram bytes per launch of the traversal kernel from the committed ncu
-    summary (a line 'dram_bytes_per_launch: N'), or None."""
-    if not os.path.exists(PROFILE_SUMMARY):
+    summary of the workload (a line 'dram_bytes_per_launch: N'), or None."""
+    path = os.path.join(PROFILES, f"trace_closest_{kind}_incoherent.txt")
+    if not os.path.exists(path):
         return None
-    for line in open(PROFILE_SUMMARY):
+    for line in open(path):
         if line.strip().startswith("dram_bytes_per_launch:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
@@ -229,31 +247,55 @@ def path_tracer_block(fg, torch, stream, local):
 def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
     """Spec target workload: a 1,048,576-triangle soup in the unit cube
     (edge lengths log-uniform in [1e-3, 0.1], seed 2) and 8,388,608 rays with
-    origins uniform in the cube and directions uniform on the sphere."""
+    origins uniform in the cube and directions uniform on the sphere. Timed
+    on the reference tree (binned SAH, default launch shape) and on the
+    best configuration: spatial splits, launch shape and coherence order
+    picked by the autotuner in set-up (the timed launches include the
+    ray-sorting kernels when the tuner chose them)."""
     from foundation_gb300 import scenes
     so = scenes.soup_scene(1 << 20, seed=2)
     rays = scenes.incoherent_rays(n_rays, (0, 0, 0), (1, 1, 1), seed=2)
     ctx = fg.Context(local, stream=stream.cuda_stream)
-    s = ctx.upload(so.verts, so.idx)
     rd = torch.from_numpy(rays).to("cuda")
     hd = torch.empty(2 * n_rays, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
-    for _ in range(3):
-        s.closest(rd, hd)
-    ctx.sync()
-    reps = 20
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
-        s.closest(rd, hd)
-    e1.record(stream)
-    ctx.sync()
-    ms = e0.elapsed_time(e1) / reps
+
+    def time_it(s, reps=20):
+        for _ in range(3):
+            s.closest(rd, hd)
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            s.closest(rd, hd)
+        e1.record(stream)
+        ctx.sync()
+        return e0.elapsed_time(e1) / reps
+
+    s = ctx.upload(so.verts, so.idx)
     info = s.info()
+    ms_ref = time_it(s)
+    s.close()
+    best = None
+    for budget in (0.5, 1.0, 2.0):
+        s = ctx.upload(so.verts, so.idx, spatial_splits=True, split_budget=budget)
+        cfg, _ = ctx.tune(s, rd, reps=2)
+        ctx.set_trace_config(**cfg)
+        ms = time_it(s)
+        sinfo = s.info()
+        if best is None or ms < best["kernel_ms"]:
+            best = {"kernel_ms": ms, "split_budget": budget, "launch_shape": cfg, "refs": sinfo["num_refs"],
+                    "wide_nodes": sinfo["num_wide_nodes"], "node_bytes": sinfo["node_bytes"],
+                    "tri_bytes": sinfo["tri_bytes"], "build_ms": sinfo["build_ms"]}
+        ctx.set_trace_config()
+        s.close()
     ctx.close()
-    return {"workload": "soup 1,048,576 tris, 8,388,608 incoherent rays", "kernel_ms": ms,
-            "mrays_s": n_rays / (ms * 1e-3) / 1e6, "target_mrays_s": 1500.0,
-            "wide_nodes": info["num_wide_nodes"], "wide_depth": info["wide_depth"], "build_ms": info["build_ms"]}
+    best["mrays_s"] = n_rays / (best["kernel_ms"] * 1e-3) / 1e6
+    return {"workload": "soup 1,048,576 tris, 8,388,608 incoherent rays",
+            "reference_tree": {"kernel_ms": ms_ref, "mrays_s": n_rays / (ms_ref * 1e-3) / 1e6,
+                               "wide_nodes": info["num_wide_nodes"], "wide_depth": info["wide_depth"],
+                               "build_ms": info["build_ms"]},
+            "best": best, "target_mrays_s": 1500.0}
 
 
 def time_to_relmse_block(fg, torch, stream, local, ref_spp: int = 8192):
@@ -350,6 +392,73 @@ def batched_block(fg, torch, stream, local, num_scenes: int = 256, reps: int = 5
             "graph": True}
 
 
+def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 256, warmup_frames: int = 16):
+    """Config 5: heightfield terrain (2237^2 vertices, 8-octave value noise,
+    seed 3) plus 4,096 level-4 icospheres, 30,970,912 triangles, lit by a
+    directional sun and a constant sky; 3840x2160, max depth 6, RR from
+    bounce 3. Reported: the host build, incoherent closest-hit throughput on
+    the scene, the plain tracer's 16-spp frame, and the radiance cache
+    (training-only warm-up frames, then 1-spp frames) given the same wall
+    time; both scored by relMSE against a plain render of `ref_spp` spp."""
+    from foundation_gb300 import convergence as CV
+    from foundation_gb300 import scenes
+    t0 = time.perf_counter()
+    tr = scenes.terrain_scene()
+    gen_s = time.perf_counter() - t0
+    ctx = fg.Context(local, stream=stream.cuda_stream)
+    t0 = time.perf_counter()
+    s = ctx.upload(tr.verts, tr.idx)
+    upload_s = time.perf_counter() - t0
+    info = s.info()
+    s.set_materials(tr.tri_material, scenes.material_records(tr))
+    s.set_lights(scenes.light_records(tr))
+    W, H, cam = 3840, 2160, scenes.TERRAIN_CAMERA
+    kw = dict(max_depth=6, **scenes.TERRAIN_LIGHTING)
+    n_rays = N_RAYS
+    rd = torch.from_numpy(scenes.incoherent_rays(n_rays, *tr.bounds, seed=3)).to("cuda")
+    hd = torch.empty(2 * n_rays, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        ctx.sync()
+        return e0.elapsed_time(e1)
+
+    for _ in range(2):
+        s.closest(rd, hd)
+    trace_ms = sum(timed(lambda: s.closest(rd, hd)) for _ in range(5)) / 5
+    del rd, hd
+    ref = CV.render_reference(ctx, s, W, H, cam, ref_spp, chunk=16, seed=9001, **kw)
+    out = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
+    ctx.render(s, W, H, 1, cam, seed=5, out=out, **kw)  # warm-up (buffers)
+    plain_ms = timed(lambda: ctx.render(s, W, H, spp, cam, seed=1, out=out, **kw))
+    st = ctx.render_stats()
+    r_plain = CV.relmse(out, ref)
+    ctx.cache_create(s, train_paths=65536, train_steps=4, batch=16384, learning_rate=1e-2, seed=1)
+    t_cache, frames = 0.0, 0
+    for f in range(warmup_frames):
+        t_cache += timed(lambda: ctx.render(s, W, H, 1, cam, seed=100 + f, cache=True, train_only=True, **kw))
+    while t_cache < plain_ms and frames < 256:
+        t_cache += timed(lambda: ctx.render(s, W, H, 1, cam, seed=1000 + frames, cache=True, accumulate=frames > 0,
+                                            out=out, **kw))
+        frames += 1
+    r_cache = CV.relmse(out, ref)
+    ctx.close()
+    return {"workload": f"terrain 2237^2 + 4096 level-4 icospheres ({tr.num_tris} tris), sun + sky, "
+                        f"{W}x{H}, max depth 6",
+            "gen_s": gen_s, "upload_s": upload_s, "build_ms": info["build_ms"], "collapse_ms": info["collapse_ms"],
+            "wide_nodes": info["num_wide_nodes"], "node_bytes": info["node_bytes"], "tri_bytes": info["tri_bytes"],
+            "incoherent_mrays_s": n_rays / (trace_ms * 1e-3) / 1e6,
+            "reference_spp": ref_spp, "est_reference_relmse": r_plain * spp / ref_spp,
+            "plain": {"spp": spp, "ms": plain_ms, "relmse": r_plain, "extension_rays": st["extension_rays"],
+                      "shadow_rays": st["shadow_rays"],
+                      "grays_s_incl_shading": (st["extension_rays"] + st["shadow_rays"]) / (plain_ms * 1e-3) / 1e9},
+            "cache_same_time": {"ms": t_cache, "warmup_frames": warmup_frames, "frames": frames, "relmse": r_cache}}
+
+
 def cpu_baseline(sc, rays):
     import oracle
     cores = os.cpu_count() or 1
@@ -375,7 +484,7 @@ def run_reference(args):
         return 0
     import oracle
     oracle.build()
-    sc, rays = workload(0, args.rays)
+    sc, rays = workload(0, args.rays, args.workload)
     b = oracle.OracleBVH(sc.verts, sc.idx)
     cores = os.cpu_count() or 1
     sample = min(len(rays), 1 << 20)
@@ -392,7 +501,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_block(sc, args.rays, 1), "impl": "reference",
+            "config": config_block(sc, args.rays, 1, args.workload), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{sample} rays of the workload per step"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -415,11 +524,11 @@ def main():
         dist.init_process_group("nccl")
     import foundation_gb300 as fg
     fg.load()  # fails loudly when the native library is missing
-    sc, rays = workload(rank, args.rays)
+    sc, rays = workload(rank, args.rays, args.workload)
     n = len(rays)
     stream = torch.cuda.Stream()
     ctx = fg.Context(local, stream=stream.cuda_stream)
-    scene = ctx.upload(sc.verts, sc.idx)
+    scene = ctx.upload(sc.verts, sc.idx, spatial_splits=args.spatial_splits)
     info = scene.info()
     rd = torch.from_numpy(rays).to("cuda")
     hd = torch.empty(2 * n, dtype=torch.int32, device="cuda")
@@ -488,14 +597,14 @@ def main():
         bpr, nodes, tris = algorithmic_bytes_per_ray(sc, rays)
         kern_ms = float(np.mean(per_step))
         achieved = bpr * n / (kern_ms * 1e-3) / 1e9
-        traffic = profile_traffic()
+        traffic = profile_traffic(args.workload)
         l2 = l2_bandwidth_gbs(torch)
         l2_peak = max(l2.values())
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_block(sc, n, world),
+            "config": config_block(sc, n, world, args.workload),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8,
                     "steps": e2e_steps, "matches_device_result": e2e_ok},
             "gpu_launches": args.steps,
@@ -514,6 +623,7 @@ def main():
             line["incoherent_1m_tris"] = incoherent_1m_block(fg, torch, stream, local)
             line["time_to_relmse_1080p"] = time_to_relmse_block(fg, torch, stream, local)
             line["batched_256_scenes"] = batched_block(fg, torch, stream, local)
+            line["large_scene_4k"] = large_scene_block(fg, torch, stream, local)
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, rays)
         print(json.dumps(line), flush=True)

@@ -44,7 +44,7 @@ struct BuildParams {
     float trav_cost = 1.0f;        // SAH cost of a traversal step relative to a triangle test
     bool spatial_splits = false;   // BuildBinarySbvh only
     float spatial_alpha = 1e-5f;   // try spatial splits when child overlap > alpha x root half area
-    double max_refs_factor = 2.0;  // at most this many references per triangle in total
+    double max_refs_factor = 2.0;  // spatial splits add at most this many references per triangle
 };
 
 // tri: 9 floats per triangle (v0, v1, v2). nt > 0.

@@ -1,0 +1,770 @@
+// gpu_build.cu — BVH construction on the GPU (see gpu_build.hpp).
+//
+//  1. prep: per triangle its box, its shading normal, input validation, and
+//     the scene box / centroid box (warp-reduced float atomics);
+//  2. 30-bit Morton code of each centroid on a 1024^3 grid over the centroid
+//     box;
+//  3. stable LSD radix sort of (code, triangle) in four 8-bit passes: per
+//     2,048-element warp tile a digit histogram, one exclusive scan over the
+//     digit-major counts, then a scatter in which each warp ranks its
+//     elements in order with __match_any_sync;
+//  4. Karras (2012): internal node i of the n-1 finds its key range and
+//     split by binary searches on the common-prefix length of the sorted
+//     keys (ties between equal codes broken by sorted position);
+//  5. refit from the leaves upwards (the second thread to reach a node
+//     finishes it): box, triangle count and the SAH decision
+//     cost(n) = min(N A, C_trav A + cost(l) + cost(r)), a subtree of at most
+//     max_leaf triangles becoming one leaf when that is not dearer;
+//  6. collapse to 8-wide nodes, one wide level per launch: the greedy rule of
+//     collapse.cpp (expand the largest-area internal child until 8), octant
+//     slots, margin inflation and outward quantisation in double precision
+//     as on the host, children and leaf triangles allocated with atomics.
+#include "gpu_build.hpp"
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "../../../include/fnd_rt.h"
+#include "../core/core.hpp"
+#include "../rt/device_scene.hpp"
+#include "collapse.hpp"
+#include "wide_bvh.hpp"
+
+namespace Foundation {
+namespace RT {
+namespace {
+
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+constexpr uint32_t kLeafRef = 0x80000000u;  // reference to a sorted single-triangle leaf
+constexpr uint32_t kLeafNode = 0x80000000u;  // count word: this subtree is one leaf
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr int kMaxLevels = kMaxStack / 2;  // wide levels the traversal stack allows
+constexpr uint32_t kPrepBadIndex = 1u, kPrepNonFinite = 2u;
+
+struct Buffers {
+    float4 *blo, *bhi;            // triangle boxes (original order)
+    uint32_t *keys, *vals;        // sorted codes / triangle ids
+    uint32_t *keys2, *vals2;      // radix-sort ping-pong
+    uint32_t* cnt;                // digit-major tile counts
+    uint32_t* sums;               // scan tile sums
+    uint32_t *left, *right;       // internal node children (kLeafRef | sorted index for leaves)
+    uint32_t *parent_i, *parent_l;
+    uint32_t* first;              // internal node: first sorted leaf of its range
+    float4 *nlo, *nhi;            // internal node boxes
+    uint32_t* ncount;             // triangle count | kLeafNode
+    float* ncost;
+    uint32_t* flag;               // refit arrival counters
+    float* bounds;                // scene lo[3], hi[3], centroid lo[3], hi[3]
+    uint32_t* status;
+    uint32_t* counters;           // [0] nodes, [1] tris, [2] leaves, [4..] per-level queue counts
+    uint2 *qa, *qb;               // collapse queues (binary ref, wide node)
+};
+
+__device__ __forceinline__ void atomic_min_f(float* a, float v) {
+    if (v >= 0.0f)
+        atomicMin(reinterpret_cast<int*>(a), __float_as_int(v));
+    else
+        atomicMax(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float* a, float v) {
+    if (v >= 0.0f)
+        atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
+    else
+        atomicMin(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+
+__global__ void init_bounds_kernel(float* b) {
+    const int i = threadIdx.x;
+    if (i < 12) b[i] = (i % 6) < 3 ? __int_as_float(0x7F800000) : __int_as_float(0xFF800000);
+}
+
+__global__ void __launch_bounds__(256) prep_kernel(const float* __restrict__ verts, uint32_t nv,
+                                                   const uint32_t* __restrict__ idx, uint32_t nt, Buffers B,
+                                                   float4* __restrict__ shade) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    float lo[3], hi[3], c[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = c[a] = __int_as_float(0x7F800000);
+        hi[a] = __int_as_float(0xFF800000);
+    }
+    float cmax[3] = {hi[0], hi[1], hi[2]};
+    if (t < nt) {
+        uint32_t vi[3];
+        bool ok = true;
+        for (int k = 0; k < 3; ++k) {
+            vi[k] = idx[3 * (size_t)t + k];
+            if (vi[k] >= nv) ok = false;
+        }
+        if (!ok) {
+            atomicOr(B.status, kPrepBadIndex);
+        } else {
+            float v[9];
+            bool finite = true;
+            for (int k = 0; k < 3; ++k)
+                for (int a = 0; a < 3; ++a) {
+                    v[3 * k + a] = verts[3 * (size_t)vi[k] + a];
+                    finite = finite && isfinite(v[3 * k + a]);
+                }
+            if (!finite) atomicOr(B.status, kPrepNonFinite);
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fminf(fminf(v[a], v[3 + a]), v[6 + a]);
+                hi[a] = fmaxf(fmaxf(v[a], v[3 + a]), v[6 + a]);
+                c[a] = cmax[a] = __fmul_rn(0.5f, __fadd_rn(lo[a], hi[a]));
+            }
+            B.blo[t] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+            B.bhi[t] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+            // geometric normal (winding order), the host's expression tree
+            const float e1x = __fsub_rn(v[3], v[0]), e1y = __fsub_rn(v[4], v[1]), e1z = __fsub_rn(v[5], v[2]);
+            const float e2x = __fsub_rn(v[6], v[0]), e2y = __fsub_rn(v[7], v[1]), e2z = __fsub_rn(v[8], v[2]);
+            float nx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
+            float ny = __fsub_rn(__fmul_rn(e1z, e2x), __fmul_rn(e1x, e2z));
+            float nz = __fsub_rn(__fmul_rn(e1x, e2y), __fmul_rn(e1y, e2x));
+            const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz)));
+            if (l > 0.0f) {
+                nx = __fdiv_rn(nx, l);
+                ny = __fdiv_rn(ny, l);
+                nz = __fdiv_rn(nz, l);
+            } else {
+                nx = ny = 0.0f;
+                nz = 1.0f;
+            }
+            shade[t] = make_float4(nx, ny, nz, 0.0f);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(kFull, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(kFull, hi[a], o));
+            c[a] = fminf(c[a], __shfl_xor_sync(kFull, c[a], o));
+            cmax[a] = fmaxf(cmax[a], __shfl_xor_sync(kFull, cmax[a], o));
+        }
+    if ((threadIdx.x & 31u) == 0 && lo[0] <= hi[0]) {
+        for (int a = 0; a < 3; ++a) {
+            atomic_min_f(B.bounds + a, lo[a]);
+            atomic_max_f(B.bounds + 3 + a, hi[a]);
+            atomic_min_f(B.bounds + 6 + a, c[a]);
+            atomic_max_f(B.bounds + 9 + a, cmax[a]);
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void __launch_bounds__(256) morton_kernel(uint32_t nt, Buffers B) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const float4 lo = B.blo[t], hi = B.bhi[t];
+    const float c[3] = {__fmul_rn(0.5f, __fadd_rn(lo.x, hi.x)), __fmul_rn(0.5f, __fadd_rn(lo.y, hi.y)),
+                        __fmul_rn(0.5f, __fadd_rn(lo.z, hi.z))};
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+        const float e = B.bounds[9 + a] - B.bounds[6 + a];
+        const float u = e > 0.0f ? (c[a] - B.bounds[6 + a]) * (1024.0f / e) : 0.0f;
+        q[a] = (uint32_t)fminf(fmaxf(u, 0.0f), 1023.0f);
+    }
+    B.keys[t] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+    B.vals[t] = t;
+}
+
+// ---- stable LSD radix sort ---------------------------------------------------
+constexpr int kSortWarps = 8;
+constexpr uint32_t kSortIters = 64;
+constexpr uint32_t kSortTile = 32 * kSortIters;  // elements per warp tile
+constexpr int kScanThreads = 256;
+constexpr uint32_t kScanItems = 16;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096 counters per scan tile
+constexpr int kTopThreads = 1024;                           // scans up to 4 * 1024 tile sums
+
+__global__ void __launch_bounds__(32 * kSortWarps) hist_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+                                                               uint32_t shift, uint32_t units, uint32_t* cnt) {
+    __shared__ uint32_t s_cnt[kSortWarps][256];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t u = blockIdx.x * kSortWarps + warp;
+    if (u >= units) return;
+    for (uint32_t d = lane; d < 256; d += 32) s_cnt[warp][d] = 0;
+    __syncwarp();
+    const uint32_t base = u * kSortTile;
+    for (uint32_t it = 0; it < kSortIters; ++it) {
+        const uint32_t i = base + it * 32 + lane;
+        if (i < n) atomicAdd(&s_cnt[warp][(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncwarp();
+    for (uint32_t d = lane; d < 256; d += 32) cnt[(size_t)d * units + u] = s_cnt[warp][d];
+}
+
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t& total, uint32_t* s_warp) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += x;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    const uint32_t nw = blockDim.x >> 5;
+    if (warp == 0) {
+        uint32_t w = lane < nw ? s_warp[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(kFull, w, o);
+            if ((int)lane >= o) w += x;
+        }
+        if (lane < nw) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[nw - 1];
+    const uint32_t before = warp ? s_warp[warp - 1] : 0u;
+    __syncthreads();
+    return before + incl - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_tile_sum_kernel(const uint32_t* a, uint32_t m, uint32_t* sums) {
+    __shared__ uint32_t s_warp[32];
+    const uint32_t k = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v = 0;
+    for (uint32_t j = 0; j < kScanItems; ++j) v += k + j < m ? a[k + j] : 0u;
+    uint32_t total;
+    block_exclusive(v, total, s_warp);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kTopThreads) scan_top_kernel(uint32_t* sums, uint32_t tiles) {
+    __shared__ uint32_t s_warp[32];
+    const uint32_t k = 4u * threadIdx.x;
+    uint32_t c[4], v = 0;
+    for (uint32_t j = 0; j < 4; ++j) {
+        c[j] = k + j < tiles ? sums[k + j] : 0u;
+        v += c[j];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive(v, total, s_warp);
+    for (uint32_t j = 0; j < 4; ++j) {
+        if (k + j < tiles) sums[k + j] = run;
+        run += c[j];
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_tile_kernel(uint32_t* a, uint32_t m, const uint32_t* sums) {
+    __shared__ uint32_t s_warp[32];
+    const uint32_t k = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t c[kScanItems], v = 0;
+    for (uint32_t j = 0; j < kScanItems; ++j) {
+        c[j] = k + j < m ? a[k + j] : 0u;
+        v += c[j];
+    }
+    uint32_t total;
+    uint32_t run = sums[blockIdx.x] + block_exclusive(v, total, s_warp);
+    for (uint32_t j = 0; j < kScanItems; ++j) {
+        if (k + j < m) a[k + j] = run;
+        run += c[j];
+    }
+}
+
+__global__ void __launch_bounds__(32 * kSortWarps) scatter_kernel(const uint32_t* __restrict__ keys,
+                                                                  const uint32_t* __restrict__ vals, uint32_t n,
+                                                                  uint32_t shift, uint32_t units,
+                                                                  const uint32_t* __restrict__ cnt, uint32_t* ok_,
+                                                                  uint32_t* ov) {
+    __shared__ uint32_t s_run[kSortWarps][256];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t u = blockIdx.x * kSortWarps + warp;
+    if (u >= units) return;
+    for (uint32_t d = lane; d < 256; d += 32) s_run[warp][d] = cnt[(size_t)d * units + u];
+    __syncwarp();
+    const uint32_t base = u * kSortTile;
+    for (uint32_t it = 0; it < kSortIters; ++it) {
+        const uint32_t i = base + it * 32 + lane;
+        const bool ok = i < n;
+        const uint32_t k = ok ? keys[i] : 0u;
+        const uint32_t d = ok ? ((k >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(kFull, d);
+        const uint32_t rank = (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        const uint32_t start = ok ? s_run[warp][d] : 0u;
+        __syncwarp();
+        if (ok) {
+            ok_[start + rank] = k;
+            ov[start + rank] = vals[i];
+            if (lane == (uint32_t)__ffs(peers) - 1u) s_run[warp][d] = start + (uint32_t)__popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+// ---- hierarchy (Karras 2012) -------------------------------------------------
+__device__ __forceinline__ int prefix(const uint32_t* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint32_t a = k[i], b = k[j];
+    if (a != b) return __clz(a ^ b);
+    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+__global__ void __launch_bounds__(256) hierarchy_kernel(int n, Buffers B) {
+    const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n - 1) return;
+    const uint32_t* k = B.keys;
+    const int d = prefix(k, n, i, i + 1) - prefix(k, n, i, i - 1) > 0 ? 1 : -1;
+    const int dmin = prefix(k, n, i, i - d);
+    int lmax = 2;
+    while (prefix(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (prefix(k, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = prefix(k, n, i, j);
+    int s = 0;
+    for (int div = 2;; div <<= 1) {
+        const int t = (l + div - 1) / div;
+        if (prefix(k, n, i, i + (s + t) * d) > dnode) s += t;
+        if (t <= 1) break;
+    }
+    const int gamma = i + s * d + min(d, 0);
+    const int lo = min(i, j), hi = max(i, j);
+    const uint32_t lc = lo == gamma ? (kLeafRef | (uint32_t)gamma) : (uint32_t)gamma;
+    const uint32_t rc = hi == gamma + 1 ? (kLeafRef | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
+    B.left[i] = lc;
+    B.right[i] = rc;
+    B.first[i] = (uint32_t)lo;
+    if (lc & kLeafRef)
+        B.parent_l[gamma] = (uint32_t)i;
+    else
+        B.parent_i[gamma] = (uint32_t)i;
+    if (rc & kLeafRef)
+        B.parent_l[gamma + 1] = (uint32_t)i;
+    else
+        B.parent_i[gamma + 1] = (uint32_t)i;
+}
+
+__host__ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+struct RefBox {
+    float4 lo, hi;
+    uint32_t count;  // | kLeafNode when the subtree is one leaf
+    float cost;
+};
+
+__device__ __forceinline__ RefBox ref_box(const Buffers& B, uint32_t ref) {
+    RefBox r;
+    if (ref & kLeafRef) {
+        const uint32_t t = B.vals[ref & ~kLeafRef];
+        r.lo = B.blo[t];
+        r.hi = B.bhi[t];
+        r.count = 1u | kLeafNode;
+        r.cost = half_area(r.lo, r.hi);
+    } else {
+        r.lo = __ldcg(B.nlo + ref);
+        r.hi = __ldcg(B.nhi + ref);
+        r.count = __ldcg(B.ncount + ref);
+        r.cost = __ldcg(B.ncost + ref);
+    }
+    return r;
+}
+
+__global__ void __launch_bounds__(256) refit_kernel(uint32_t n, Buffers B, uint32_t max_leaf, float trav_cost) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || n < 2) return;
+    uint32_t p = B.parent_l[k];
+    // a root path has fewer than n nodes; the bound only guards the walk
+    for (uint32_t steps = 0; p != kNone; ++steps) {
+        if (steps >= n) {
+            atomicOr(B.status, 8u);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(B.flag + p, 1u) == 0u) return;  // the sibling subtree is not finished yet
+        __threadfence();
+        const RefBox l = ref_box(B, B.left[p]), r = ref_box(B, B.right[p]);
+        float4 lo = make_float4(fminf(l.lo.x, r.lo.x), fminf(l.lo.y, r.lo.y), fminf(l.lo.z, r.lo.z), 0.0f);
+        float4 hi = make_float4(fmaxf(l.hi.x, r.hi.x), fmaxf(l.hi.y, r.hi.y), fmaxf(l.hi.z, r.hi.z), 0.0f);
+        const uint32_t cnt = (l.count & ~kLeafNode) + (r.count & ~kLeafNode);
+        const float a = half_area(lo, hi);
+        const float split = trav_cost * a + l.cost + r.cost;
+        const bool leaf = cnt <= max_leaf && (float)cnt * a <= split;
+        B.nlo[p] = lo;
+        B.nhi[p] = hi;
+        B.ncount[p] = cnt | (leaf ? kLeafNode : 0u);
+        B.ncost[p] = leaf ? (float)cnt * a : split;
+        p = B.parent_i[p];
+    }
+}
+
+// ---- collapse to 8-wide nodes -------------------------------------------------
+struct CollapseArgs {
+    Buffers B;
+    const float* verts;
+    const uint32_t* idx;
+    WideNode* nodes;
+    float4 *v0, *v1, *v2;
+    float margin;
+    int level;
+};
+
+__global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
+    const Buffers& B = A.B;
+    uint32_t* counters = B.counters;
+    const uint32_t count = counters[4 + A.level];
+    const uint2* qin = (A.level & 1) ? B.qb : B.qa;
+    uint2* qout = (A.level & 1) ? B.qa : B.qb;
+    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < count; it += gridDim.x * blockDim.x) {
+        const uint2 item = qin[it];
+        uint32_t kids[kWidth];
+        int nk = 1;
+        kids[0] = item.x;
+        for (;;) {
+            int pick = -1;
+            float best = -1.0f;
+            for (int c = 0; c < nk; ++c) {
+                if (kids[c] & kLeafRef) continue;
+                if (__ldcg(B.ncount + kids[c]) & kLeafNode) continue;
+                const float a = half_area(__ldcg(B.nlo + kids[c]), __ldcg(B.nhi + kids[c]));
+                if (a > best) {
+                    best = a;
+                    pick = c;
+                }
+            }
+            if (pick < 0 || nk == kWidth) break;
+            const uint32_t p = kids[pick];
+            kids[pick] = B.left[p];
+            kids[nk++] = B.right[p];
+        }
+        // child boxes inflated by the margin (one ulp outward when the
+        // subtraction rounds back), node box
+        float clo[kWidth][3], chi[kWidth][3];
+        float nlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, nhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        uint32_t first[kWidth], cnt[kWidth];
+        bool is_leaf[kWidth];
+        for (int c = 0; c < nk; ++c) {
+            float4 lo, hi;
+            if (kids[c] & kLeafRef) {
+                const uint32_t sk = kids[c] & ~kLeafRef;
+                const uint32_t t = B.vals[sk];
+                lo = B.blo[t];
+                hi = B.bhi[t];
+                first[c] = sk;
+                cnt[c] = 1;
+                is_leaf[c] = true;
+            } else {
+                lo = __ldcg(B.nlo + kids[c]);
+                hi = __ldcg(B.nhi + kids[c]);
+                const uint32_t w = __ldcg(B.ncount + kids[c]);
+                is_leaf[c] = (w & kLeafNode) != 0u;
+                cnt[c] = w & ~kLeafNode;
+                first[c] = B.first[kids[c]];
+            }
+            const float l3[3] = {lo.x, lo.y, lo.z}, h3[3] = {hi.x, hi.y, hi.z};
+            for (int a = 0; a < 3; ++a) {
+                float x = l3[a] - A.margin, y = h3[a] + A.margin;
+                if (!(x < l3[a])) x = nextafterf(l3[a], -INFINITY);
+                if (!(y > h3[a])) y = nextafterf(h3[a], INFINITY);
+                clo[c][a] = x;
+                chi[c][a] = y;
+                nlo[a] = fminf(nlo[a], x);
+                nhi[a] = fmaxf(nhi[a], y);
+            }
+        }
+        // octant slots, greedy on the corner score (as collapse.cpp)
+        int child_in_slot[kWidth];
+        for (int s = 0; s < kWidth; ++s) child_in_slot[s] = -1;
+        {
+            const float cx = 0.5f * (nlo[0] + nhi[0]), cy = 0.5f * (nlo[1] + nhi[1]), cz = 0.5f * (nlo[2] + nhi[2]);
+            float dxs[kWidth], dys[kWidth], dzs[kWidth];
+            for (int c = 0; c < nk; ++c) {
+                dxs[c] = 0.5f * (clo[c][0] + chi[c][0]) - cx;
+                dys[c] = 0.5f * (clo[c][1] + chi[c][1]) - cy;
+                dzs[c] = 0.5f * (clo[c][2] + chi[c][2]) - cz;
+            }
+            uint32_t used_k = 0, used_s = 0;
+            for (int round = 0; round < nk; ++round) {
+                int bk = -1, bs = -1;
+                float bv = -FLT_MAX;
+                for (int c = 0; c < nk; ++c) {
+                    if (used_k & (1u << c)) continue;
+                    for (int s = 0; s < kWidth; ++s) {
+                        if (used_s & (1u << s)) continue;
+                        const float sc = ((s & 1) ? dxs[c] : -dxs[c]) + ((s & 2) ? dys[c] : -dys[c]) +
+                                         ((s & 4) ? dzs[c] : -dzs[c]);
+                        if (sc > bv || bk < 0) {
+                            bv = sc;
+                            bk = c;
+                            bs = s;
+                        }
+                    }
+                }
+                used_k |= 1u << bk;
+                used_s |= 1u << bs;
+                child_in_slot[bs] = bk;
+            }
+        }
+        WideNode nd;
+        uint32_t* ndw = reinterpret_cast<uint32_t*>(&nd);
+        for (int w = 0; w < 20; ++w) ndw[w] = 0u;
+        double step[3];
+        bool bad = false;
+        for (int a = 0; a < 3; ++a) {
+            nd.p[a] = nlo[a];
+            const double ext = (double)nhi[a] - (double)nlo[a];
+            int e = ext > 0.0 ? (int)ceil(log2(ext / 255.0)) : -100;
+            while (ldexp(255.0, e) < ext) e++;
+            while (e > -100 && ldexp(255.0, e - 1) >= ext) e--;
+            if (e < -100 || e > 100) bad = true;
+            nd.e[a] = (uint8_t)(e + 127);
+            step[a] = ldexp(1.0, e);
+        }
+        uint32_t n_int = 0, n_tri = 0;
+        for (int c = 0; c < nk; ++c) {
+            if (is_leaf[c])
+                n_tri += cnt[c];
+            else
+                n_int++;
+        }
+        const uint32_t child_base = n_int ? atomicAdd(counters + 0, n_int) : 0u;
+        const uint32_t tri_base = n_tri ? atomicAdd(counters + 1, n_tri) : 0u;
+        nd.child_base = child_base;
+        nd.tri_base = tri_base;
+        uint32_t tri_off = 0, int_off = 0, leaves = 0;
+        for (int s = 0; s < kWidth; ++s) {
+            const int c = child_in_slot[s];
+            if (c < 0) continue;
+            for (int a = 0; a < 3; ++a) {
+                const double p = nd.p[a];
+                double ql = floor(((double)clo[c][a] - p) / step[a]);
+                double qh = ceil(((double)chi[c][a] - p) / step[a]);
+                ql = fmin(fmax(ql, 0.0), 255.0);
+                qh = fmin(fmax(qh, 0.0), 255.0);
+                while (ql > 0.0 && p + ql * step[a] > (double)clo[c][a]) ql -= 1.0;
+                while (qh < 255.0 && p + qh * step[a] < (double)chi[c][a]) qh += 1.0;
+                if (!(p + ql * step[a] <= (double)clo[c][a] && p + qh * step[a] >= (double)chi[c][a])) bad = true;
+                nd.qlo[a][s] = (uint8_t)ql;
+                nd.qhi[a][s] = (uint8_t)qh;
+            }
+            if (is_leaf[c]) {
+                nd.meta[s] = (uint8_t)(kMetaLeafFlag | ((cnt[c] - 1u) << 5) | tri_off);
+                for (uint32_t i = 0; i < cnt[c]; ++i) {
+                    const uint32_t t = B.vals[first[c] + i];
+                    const size_t d = (size_t)tri_base + tri_off + i;
+                    float v[9];
+                    for (int k = 0; k < 3; ++k)
+                        for (int q = 0; q < 3; ++q) v[3 * k + q] = A.verts[3 * (size_t)A.idx[3 * (size_t)t + k] + q];
+                    A.v0[d] = make_float4(v[0], v[1], v[2], __uint_as_float(t));
+                    A.v1[d] = make_float4(v[3], v[4], v[5], 0.0f);
+                    A.v2[d] = make_float4(v[6], v[7], v[8], 0.0f);
+                }
+                tri_off += cnt[c];
+                leaves++;
+            } else {
+                nd.imask |= (uint8_t)(1u << s);
+                nd.meta[s] = kMetaInternal;
+                const uint32_t slot = atomicAdd(counters + 4 + A.level + 1, 1u);
+                qout[slot] = make_uint2(kids[c], child_base + int_off);
+                int_off++;
+            }
+        }
+        if (bad) atomicOr(B.status, 4u);
+        if (leaves) atomicAdd(counters + 2, leaves);
+        A.nodes[item.y] = nd;
+    }
+}
+
+__global__ void write_ids_kernel(float4* shade, const uint32_t* ids, uint32_t nt) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nt) reinterpret_cast<uint32_t*>(shade + t)[3] = ids[t];
+}
+
+double Ms(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void Check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess)
+        Core::Fail(e == cudaErrorMemoryAllocation ? FND_ERR_OUT_OF_MEMORY : FND_ERR_CUDA, "%s: %s", what,
+                   cudaGetErrorString(e));
+}
+
+// Owner of the temporary device allocations of one build.
+struct Scratch {
+    std::vector<void*> ptrs;
+    template <typename T>
+    T* get(size_t count) {
+        void* p = nullptr;
+        Check(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)), "cudaMalloc (GPU build scratch)");
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    ~Scratch() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+void RadixSort(Buffers& B, uint32_t n, cudaStream_t s) {
+    const uint32_t units = (n + kSortTile - 1) / kSortTile;
+    const uint32_t m = 256u * units;
+    const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
+    const uint32_t blocks = (units + kSortWarps - 1) / kSortWarps;
+    uint32_t *k_in = B.keys, *v_in = B.vals, *k_out = B.keys2, *v_out = B.vals2;
+    for (uint32_t shift = 0; shift < 32; shift += 8) {
+        hist_kernel<<<blocks, 32 * kSortWarps, 0, s>>>(k_in, n, shift, units, B.cnt);
+        scan_tile_sum_kernel<<<tiles, kScanThreads, 0, s>>>(B.cnt, m, B.sums);
+        scan_top_kernel<<<1, kTopThreads, 0, s>>>(B.sums, tiles);
+        scan_tile_kernel<<<tiles, kScanThreads, 0, s>>>(B.cnt, m, B.sums);
+        scatter_kernel<<<blocks, 32 * kSortWarps, 0, s>>>(k_in, v_in, n, shift, units, B.cnt, k_out, v_out);
+        std::swap(k_in, k_out);
+        std::swap(v_in, v_out);
+    }
+    Check(cudaGetLastError(), "radix sort launch");
+    // four passes: the sorted data is back in keys / vals
+}
+
+}  // namespace
+
+void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint32_t nt, const GpuBuildParams& p,
+                  GpuBuildOutput& out, cudaStream_t s) {
+    CHECK_CODE(nt >= 1 && nt <= kGpuBuildMaxTris, FND_ERR_INVALID_ARG, "GPU build takes 1..%u triangles, not %u",
+               kGpuBuildMaxTris, nt);
+    CHECK_CODE(p.max_leaf >= 1 && p.max_leaf <= (uint32_t)kMaxLeafTris, FND_ERR_INVALID_ARG, "max_leaf %u",
+               p.max_leaf);
+    int dev = 0, sms = 0;
+    Check(cudaGetDevice(&dev), "cudaGetDevice");
+    Check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    const auto t0 = std::chrono::steady_clock::now();
+    Scratch S;
+    Buffers B{};
+    const uint32_t n = nt;
+    const uint32_t units = (n + kSortTile - 1) / kSortTile;
+    B.blo = S.get<float4>(n);
+    B.bhi = S.get<float4>(n);
+    B.keys = S.get<uint32_t>(n);
+    B.vals = S.get<uint32_t>(n);
+    B.keys2 = S.get<uint32_t>(n);
+    B.vals2 = S.get<uint32_t>(n);
+    B.cnt = S.get<uint32_t>(256ull * units);
+    B.sums = S.get<uint32_t>(4 * kTopThreads);
+    B.left = S.get<uint32_t>(n);
+    B.right = S.get<uint32_t>(n);
+    B.parent_i = S.get<uint32_t>(n);
+    B.parent_l = S.get<uint32_t>(n);
+    B.first = S.get<uint32_t>(n);
+    B.nlo = S.get<float4>(n);
+    B.nhi = S.get<float4>(n);
+    B.ncount = S.get<uint32_t>(n);
+    B.ncost = S.get<float>(n);
+    B.flag = S.get<uint32_t>(n);
+    B.bounds = S.get<float>(12);
+    B.status = S.get<uint32_t>(1);
+    B.counters = S.get<uint32_t>(4 + kMaxLevels + 2);
+    B.qa = S.get<uint2>(n);
+    B.qb = S.get<uint2>(n);
+    float4* shade = nullptr;
+    Check(cudaMalloc(&shade, 16ull * n), "cudaMalloc (shading normals)");
+    out.d_tri_shade = shade;
+    Check(cudaMemsetAsync(B.status, 0, 4, s), "memset");
+    Check(cudaMemsetAsync(B.flag, 0, 4ull * n, s), "memset");
+    Check(cudaMemsetAsync(B.parent_i, 0xFF, 4ull * n, s), "memset");
+    Check(cudaMemsetAsync(B.parent_l, 0xFF, 4ull * n, s), "memset");
+    Check(cudaMemsetAsync(B.counters, 0, 4ull * (4 + kMaxLevels + 2), s), "memset");
+    init_bounds_kernel<<<1, 32, 0, s>>>(B.bounds);
+    const uint32_t g256 = (n + 255) / 256;
+    prep_kernel<<<g256, 256, 0, s>>>(d_verts, nv, d_idx, n, B, shade);
+    uint32_t h_status = 0;
+    float h_bounds[12];
+    Check(cudaMemcpyAsync(&h_status, B.status, 4, cudaMemcpyDeviceToHost, s), "status readback");
+    Check(cudaMemcpyAsync(h_bounds, B.bounds, sizeof(h_bounds), cudaMemcpyDeviceToHost, s), "bounds readback");
+    Check(cudaStreamSynchronize(s), "prep");
+    CHECK_CODE(!(h_status & kPrepBadIndex), FND_ERR_INVALID_ARG, "vertex index out of range (nv = %u)", nv);
+    CHECK_CODE(!(h_status & kPrepNonFinite), FND_ERR_INVALID_ARG, "non-finite vertex coordinate");
+    for (int a = 0; a < 3; ++a) {
+        out.lo[a] = h_bounds[a];
+        out.hi[a] = h_bounds[3 + a];
+    }
+    out.margin = SceneMargin(out.lo, out.hi);
+    morton_kernel<<<g256, 256, 0, s>>>(n, B);
+    RadixSort(B, n, s);
+    if (n >= 2) {
+        hierarchy_kernel<<<(n - 1 + 255) / 256, 256, 0, s>>>((int)n, B);
+        refit_kernel<<<g256, 256, 0, s>>>(n, B, p.max_leaf, p.trav_cost);
+    }
+    Check(cudaGetLastError(), "hierarchy launch");
+    // root item: internal node 0, or the single leaf
+    const uint2 root = make_uint2(n >= 2 ? 0u : kLeafRef, 0u);
+    Check(cudaMemcpyAsync(B.qa, &root, sizeof(root), cudaMemcpyHostToDevice, s), "root");
+    const uint32_t one[2] = {1u, 0u};  // one wide node (the root), level-0 queue of one item
+    Check(cudaMemcpyAsync(B.counters + 0, &one[0], 4, cudaMemcpyHostToDevice, s), "root count");
+    Check(cudaMemcpyAsync(B.counters + 4, &one[0], 4, cudaMemcpyHostToDevice, s), "queue count");
+    float root_cost = 0.0f;
+    float4 rlo{}, rhi{};
+    if (n >= 2) {
+        Check(cudaMemcpyAsync(&root_cost, B.ncost, 4, cudaMemcpyDeviceToHost, s), "cost readback");
+        Check(cudaMemcpyAsync(&rlo, B.nlo, 16, cudaMemcpyDeviceToHost, s), "root box");
+        Check(cudaMemcpyAsync(&rhi, B.nhi, 16, cudaMemcpyDeviceToHost, s), "root box");
+    }
+    Check(cudaStreamSynchronize(s), "LBVH");
+    out.build_ms = Ms(t0);
+    const auto t1 = std::chrono::steady_clock::now();
+    WideNode* nodes = nullptr;
+    char* tris = nullptr;
+    Check(cudaMalloc(&nodes, sizeof(WideNode) * (size_t)n), "cudaMalloc (wide nodes)");
+    Scratch S2;
+    S2.ptrs.push_back(nodes);
+    Check(cudaMalloc(&tris, 48ull * n), "cudaMalloc (triangles)");
+    out.d_tris = tris;
+    CollapseArgs A{};
+    A.B = B;
+    A.verts = d_verts;
+    A.idx = d_idx;
+    A.nodes = nodes;
+    A.v0 = reinterpret_cast<float4*>(tris);
+    A.v1 = reinterpret_cast<float4*>(tris + 16ull * n);
+    A.v2 = reinterpret_cast<float4*>(tris + 32ull * n);
+    A.margin = out.margin;
+    const int grid = std::max(1, sms * 8);
+    for (int level = 0; level < kMaxLevels; ++level) {
+        A.level = level;
+        collapse_kernel<<<grid, 128, 0, s>>>(A);
+    }
+    Check(cudaGetLastError(), "collapse launch");
+    uint32_t h_counters[4 + kMaxLevels + 2];
+    Check(cudaMemcpyAsync(h_counters, B.counters, sizeof(h_counters), cudaMemcpyDeviceToHost, s), "counters");
+    Check(cudaMemcpyAsync(&h_status, B.status, 4, cudaMemcpyDeviceToHost, s), "status readback");
+    Check(cudaStreamSynchronize(s), "collapse");
+    CHECK_CODE(h_counters[4 + kMaxLevels] == 0, FND_ERR_INVALID_SCENE,
+               "wide BVH deeper than the traversal stack bound %d", kMaxLevels);
+    CHECK_CODE(!(h_status & 4u), FND_ERR_INVALID_SCENE, "child box quantisation failed (scene extent out of range)");
+    CHECK_CODE(!(h_status & 8u), FND_ERR_INVALID_SCENE, "GPU build: malformed hierarchy");
+    CHECK_CODE(h_counters[1] == n, FND_ERR_INVALID_SCENE, "collapse placed %u of %u triangles", h_counters[1], n);
+    out.num_nodes = h_counters[0];
+    out.num_refs = n;
+    out.leaves = h_counters[2];
+    out.depth = 0;
+    for (int l = 0; l < kMaxLevels; ++l)
+        if (h_counters[4 + l]) out.depth = (uint32_t)l + 1;
+    out.num_binary_nodes = 2 * n - 1;
+    const float ra = n >= 2 ? half_area(rlo, rhi) : 0.0f;
+    out.sah_cost = n >= 2 && ra > 0.0f ? (double)root_cost / (double)ra : 0.0;
+    // exact-size node array
+    void* exact = nullptr;
+    Check(cudaMalloc(&exact, sizeof(WideNode) * (size_t)out.num_nodes), "cudaMalloc (wide nodes)");
+    Check(cudaMemcpyAsync(exact, nodes, sizeof(WideNode) * (size_t)out.num_nodes, cudaMemcpyDeviceToDevice, s),
+          "node copy");
+    Check(cudaStreamSynchronize(s), "node copy");
+    out.d_nodes = exact;
+    out.collapse_ms = Ms(t1);
+}
+
+cudaError_t WriteMaterialIds(float4* d_tri_shade, const uint32_t* d_ids, uint32_t nt, cudaStream_t s) {
+    if (nt == 0) return cudaSuccess;
+    write_ids_kernel<<<(nt + 255) / 256, 256, 0, s>>>(d_tri_shade, d_ids, nt);
+    return cudaGetLastError();
+}
+
+}  // namespace RT
+}  // namespace Foundation

@@ -9,8 +9,8 @@
 // reference is clipped to every slab it spans (exact triangle / slab
 // clipping, intersected with the reference's current box), and a reference
 // crossing the chosen plane is duplicated into both children with clipped
-// boxes. The total reference count is capped (max_refs_factor x triangles);
-// once the budget is used, nodes fall back to object splits.
+// boxes. The duplicates are capped (max_refs_factor x triangles extra
+// references); once the budget is used, nodes fall back to object splits.
 // Closest-hit results do not depend on the tree (ties break by triangle
 // index), so a duplicated reference cannot change any hit.
 #include <algorithm>

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <vector>
 
+#include "../bvh/gpu_build.hpp"
 #include "context.hpp"
 
 using namespace Foundation;
@@ -186,14 +187,23 @@ int fnd_rt_scene_set_materials(fnd_rt_scene* scene, const uint32_t* tri_material
             std::memcpy(&dm[i].emission_light.w, &lb, 4);
             dm[i].params = make_float4(m.roughness, 0.f, 0.f, 0.f);
         }
-        for (uint32_t t = 0; t < nt; ++t) {
+        for (uint32_t t = 0; t < nt; ++t)
             CHECK_CODE(tri_material[t] < nm, FND_ERR_INVALID_ARG, "triangle %u uses material %u of %u", t,
                        tri_material[t], nm);
-            std::memcpy(&scene->tri_shade[4 * (size_t)t + 3], &tri_material[t], 4);
-        }
         CUDA_CHECK(cudaSetDevice(ctx->device));
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
-        if (nt) CUDA_CHECK(cudaMemcpy(scene->d_tri_shade, scene->tri_shade.data(), 16ull * nt, cudaMemcpyHostToDevice));
+        if (nt) {
+            // material ids into the w of the device shading records
+            void* d_ids = nullptr;
+            CUDA_CHECK(cudaMalloc(&d_ids, 4ull * nt));
+            cudaError_t e = cudaMemcpyAsync(d_ids, tri_material, 4ull * nt, cudaMemcpyHostToDevice, ctx->stream);
+            if (e == cudaSuccess)
+                e = RT::WriteMaterialIds(static_cast<float4*>(scene->d_tri_shade), static_cast<const uint32_t*>(d_ids),
+                                         nt, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            cudaFree(d_ids);
+            CUDA_CHECK(e);
+        }
         if (scene->d_materials) CUDA_CHECK(cudaFree(scene->d_materials));
         scene->d_materials = nullptr;
         scene->num_materials = 0;

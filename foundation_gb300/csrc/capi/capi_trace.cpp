@@ -14,6 +14,7 @@
 
 #include "../bvh/bvh_build.hpp"
 #include "../bvh/collapse.hpp"
+#include "../bvh/gpu_build.hpp"
 #include "context.hpp"
 
 using namespace Foundation;
@@ -98,6 +99,83 @@ int ReadStatus(fnd_rt_ctx* ctx) {
 }  // namespace Foundation
 
 using namespace Foundation::CApi;
+
+namespace {
+
+// One grey Lambertian until fnd_rt_scene_set_materials.
+void DefaultMaterial(fnd_rt_scene* scene) {
+    PT::DevMaterial m{};
+    m.albedo_type = make_float4(0.8f, 0.8f, 0.8f, 0.0f);
+    m.emission_light = make_float4(0.f, 0.f, 0.f, __builtin_bit_cast(float, (int32_t)-1));
+    m.params = make_float4(1.0f, 0.f, 0.f, 0.f);
+    CUDA_CHECK(cudaMalloc(&scene->d_materials, sizeof(m)));
+    CUDA_CHECK(cudaMemcpy(scene->d_materials, &m, sizeof(m), cudaMemcpyHostToDevice));
+    scene->num_materials = 1;
+}
+
+// FND_BVH_GPU_BUILD: the vertices and indices go to the device once and the
+// tree is built there (bvh/gpu_build.cu).
+void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, uint32_t nv, const uint32_t* idx,
+                    uint32_t nt, const RT::BuildParams& bp) {
+    void *d_verts = nullptr, *d_idx = nullptr;
+    RT::GpuBuildOutput go;
+    try {
+        const auto t0 = std::chrono::steady_clock::now();
+        CUDA_CHECK(cudaMalloc(&d_verts, 12ull * std::max(nv, 1u)));
+        CUDA_CHECK(cudaMalloc(&d_idx, 12ull * nt));
+        if (nv) CUDA_CHECK(cudaMemcpyAsync(d_verts, verts, 12ull * nv, cudaMemcpyHostToDevice, ctx->stream));
+        CUDA_CHECK(cudaMemcpyAsync(d_idx, idx, 12ull * nt, cudaMemcpyHostToDevice, ctx->stream));
+        CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        const double upload_ms = MsSince(t0);
+        RT::GpuBuildParams gp;
+        gp.max_leaf = bp.max_leaf;
+        gp.trav_cost = bp.trav_cost;
+        RT::BuildWideGpu(static_cast<const float*>(d_verts), nv, static_cast<const uint32_t*>(d_idx), nt, gp, go,
+                         ctx->stream);
+        CUDA_CHECK(cudaFree(d_verts));
+        CUDA_CHECK(cudaFree(d_idx));
+        d_verts = d_idx = nullptr;
+        scene->d_nodes = go.d_nodes;
+        scene->d_tris = go.d_tris;
+        scene->d_tri_shade = go.d_tri_shade;
+        go.d_nodes = go.d_tris = go.d_tri_shade = nullptr;
+        DefaultMaterial(scene);
+        fnd_rt_scene_info& I = scene->info;
+        I.num_binary_nodes = go.num_binary_nodes;
+        I.binary_depth = 0;  // not tracked by the GPU build
+        I.num_leaves = go.leaves;
+        I.sah_cost = go.sah_cost;
+        I.num_wide_nodes = go.num_nodes;
+        I.wide_depth = go.depth;
+        I.node_bytes = (uint64_t)go.num_nodes * sizeof(RT::WideNode);
+        I.num_refs = go.num_refs;
+        I.tri_bytes = 48ull * go.num_refs;
+        for (int a = 0; a < 3; ++a) {
+            I.bounds_lo[a] = go.lo[a];
+            I.bounds_hi[a] = go.hi[a];
+        }
+        I.box_margin = go.margin;
+        I.build_ms = go.build_ms;
+        I.collapse_ms = go.collapse_ms;
+        I.upload_ms = upload_ms;
+    } catch (...) {
+        for (void* p : {go.d_nodes, go.d_tris, go.d_tri_shade, d_verts, d_idx, scene->d_nodes, scene->d_tris,
+                        scene->d_tri_shade, scene->d_materials})
+            if (p) cudaFree(p);
+        scene->d_nodes = scene->d_tris = scene->d_tri_shade = scene->d_materials = nullptr;
+        throw;
+    }
+    char* tris = static_cast<char*>(scene->d_tris);
+    const size_t plane = 16ull * scene->info.num_refs;
+    scene->view.nodes = static_cast<const uint4*>(scene->d_nodes);
+    scene->view.v0 = reinterpret_cast<const float4*>(tris);
+    scene->view.v1 = reinterpret_cast<const float4*>(tris + plane);
+    scene->view.v2 = reinterpret_cast<const float4*>(tris + 2 * plane);
+    scene->view.num_nodes = scene->info.num_wide_nodes;
+    scene->view.num_tris = scene->info.num_refs;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -210,19 +288,31 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             if (bvh->max_leaf_tris) bp.max_leaf = bvh->max_leaf_tris;
             bp.threads = bvh->build_threads;
             if (bvh->traversal_cost != 0.0f) bp.trav_cost = bvh->traversal_cost;
+            if (bvh->split_budget != 0.0f) bp.max_refs_factor = bvh->split_budget;
         }
+        CHECK_CODE(bp.max_refs_factor >= 0.0 && bp.max_refs_factor <= 4.0, FND_ERR_INVALID_ARG,
+                   "split_budget %g not in [0, 4]", bp.max_refs_factor);
         CHECK_CODE(bp.trav_cost > 0.0f && bp.trav_cost <= 64.0f, FND_ERR_INVALID_ARG, "traversal_cost %g not in (0, 64]",
                    (double)bp.trav_cost);
         CHECK_CODE(bp.bins >= 2 && bp.bins <= 64, FND_ERR_INVALID_ARG, "sah_bins %u not in [2, 64]", bp.bins);
         CHECK_CODE(bp.max_leaf >= 1 && bp.max_leaf <= 4, FND_ERR_INVALID_ARG, "max_leaf_tris %u not in [1, 4]",
                    bp.max_leaf);
-        CHECK_CODE(!bvh || (bvh->flags & ~(uint32_t)FND_BVH_SPATIAL_SPLITS) == 0, FND_ERR_INVALID_ARG,
-                   "unknown BVH flags 0x%x", bvh ? bvh->flags : 0u);
+        CHECK_CODE(!bvh || (bvh->flags & ~(uint32_t)(FND_BVH_SPATIAL_SPLITS | FND_BVH_GPU_BUILD)) == 0,
+                   FND_ERR_INVALID_ARG, "unknown BVH flags 0x%x", bvh ? bvh->flags : 0u);
+        const bool gpu_build = bvh && (bvh->flags & FND_BVH_GPU_BUILD);
+        CHECK_CODE(!(gpu_build && (bvh->flags & FND_BVH_SPATIAL_SPLITS)), FND_ERR_INVALID_ARG,
+                   "FND_BVH_GPU_BUILD does not combine with FND_BVH_SPATIAL_SPLITS");
         UseDevice(ctx);
         auto scene = std::make_unique<fnd_rt_scene>();
         scene->ctx = ctx;
         scene->info.num_tris = nt;
         if (nt == 0) {
+            *out_scene = scene.release();
+            ctx->live_scenes++;
+            return;
+        }
+        if (gpu_build) {
+            UploadGpuBuilt(ctx, scene.get(), verts, nv, idx, nt, bp);
             *out_scene = scene.release();
             ctx->live_scenes++;
             return;
@@ -321,14 +411,8 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             CUDA_CHECK(cudaMemcpy(tris + 2 * plane, wide.v2.data(), plane, cudaMemcpyHostToDevice));
             CUDA_CHECK(cudaMalloc(&scene->d_tri_shade, 16ull * nt));
             CUDA_CHECK(cudaMemcpy(scene->d_tri_shade, scene->tri_shade.data(), 16ull * nt, cudaMemcpyHostToDevice));
-            // default material table: one grey Lambertian
-            PT::DevMaterial m{};
-            m.albedo_type = make_float4(0.8f, 0.8f, 0.8f, 0.0f);
-            m.emission_light = make_float4(0.f, 0.f, 0.f, __builtin_bit_cast(float, (int32_t)-1));
-            m.params = make_float4(1.0f, 0.f, 0.f, 0.f);
-            CUDA_CHECK(cudaMalloc(&scene->d_materials, sizeof(m)));
-            CUDA_CHECK(cudaMemcpy(scene->d_materials, &m, sizeof(m), cudaMemcpyHostToDevice));
-            scene->num_materials = 1;
+            std::vector<float>().swap(scene->tri_shade);  // the device copy is the only one kept
+            DefaultMaterial(scene.get());
         } catch (...) {
             if (scene->d_nodes) cudaFree(scene->d_nodes);
             if (scene->d_tris) cudaFree(scene->d_tris);

@@ -79,7 +79,7 @@ struct fnd_rt_scene {
     Foundation::RT::DeviceScene view{};
     fnd_rt_scene_info info{};
     // shading data (original triangle order)
-    std::vector<float> tri_shade;  // 4 floats per triangle: unit normal, material id bits
+    std::vector<float> tri_shade;  // host staging of the shading records during upload (released after)
     void* d_tri_shade = nullptr;
     void* d_materials = nullptr;
     uint32_t num_materials = 0;

@@ -86,16 +86,25 @@ typedef struct fnd_rt_bvh_desc {
     uint32_t sah_bins;      /* 2..64, default 32 */
     uint32_t max_leaf_tris; /* 1..4, default 4 */
     uint32_t build_threads; /* 0: all host cores */
-    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS or 0 */
+    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD or 0 */
     float traversal_cost;   /* SAH cost of a traversal step relative to a triangle
                                test, (0, 64]; 0: default 1 (the reference tree) */
+    float split_budget;     /* FND_BVH_SPATIAL_SPLITS: references the splits may add,
+                               per triangle, [0, 4]; 0: default 2 */
 } fnd_rt_bvh_desc;
 
 /* Spatial splits (Stich et al. 2009): references of triangles that straddle
- * a split plane are clipped and duplicated (at most 2x the triangle count),
+ * a split plane are clipped and duplicated (by default at most 2 extra
+ * references per triangle, split_budget),
  * which tightens the tree of scenes with long, overlapping triangles. Hits
  * are identical either way. */
 enum { FND_BVH_SPATIAL_SPLITS = 1u };
+/* Build on the GPU: linear BVH over 30-bit Morton codes (Karras 2012) with
+ * SAH leaf merging, collapsed to the same 8-wide format on the device. Much
+ * faster to build, somewhat slower to trace than the binned-SAH tree; hits
+ * are identical. Up to 2^27 triangles; not combined with spatial splits;
+ * build_threads is ignored. */
+enum { FND_BVH_GPU_BUILD = 2u };
 
 typedef struct fnd_rt_scene_info {
     uint32_t num_tris;

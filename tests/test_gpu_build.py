@@ -1,0 +1,101 @@
+"""BVH built on the GPU (FND_BVH_GPU_BUILD: linear BVH + SAH leaf merging +
+device collapse to the 8-wide format): every hit equals the CPU oracle's
+(ids exact, t bit-identical), for tiny, degenerate and large scenes; bad
+input fails cleanly; a path-traced image equals the host-built scene's."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from foundation_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def ctx(built):
+    import foundation_gb300 as fg
+    c = fg.Context(0)
+    yield c
+    c.close()
+
+
+def assert_same(h, ref):
+    bad = np.nonzero(h["prim"] != ref["prim"])[0]
+    assert len(bad) == 0, f"{len(bad)} id mismatches, first {bad[:5]}"
+    assert np.array_equal(h["t"].view(np.uint32), ref["t"].view(np.uint32))
+
+
+@pytest.mark.parametrize("case", ["c1", "cornell", "soup"])
+def test_gpu_built_scene_matches_oracle(ctx, case):
+    if case == "c1":
+        sc, rays = S.config1_scene(), S.camera_rays(512, 512)
+    elif case == "cornell":
+        sc = S.cornell_scene()
+        rays = np.concatenate([S.incoherent_rays(1 << 19, *sc.bounds, seed=1),
+                               S.camera_rays(320, 180, **S.CORNELL_CAMERA)])
+    else:
+        sc = S.soup_scene(1 << 20)
+        rays = S.incoherent_rays(1 << 18, (0, 0, 0), (1, 1, 1), seed=2)
+    b = O.OracleBVH(sc.verts, sc.idx)
+    g = ctx.upload(sc.verts, sc.idx, gpu_build=True)
+    info = g.info()
+    assert info["num_refs"] == sc.num_tris and 1 <= info["wide_depth"] <= 32
+    assert info["num_wide_nodes"] >= 1 and info["num_leaves"] >= 1
+    lo, hi = sc.verts[sc.idx.ravel()].min(0), sc.verts[sc.idx.ravel()].max(0)
+    assert np.array_equal(np.array(info["bounds_lo"], np.float32), lo)
+    assert np.array_equal(np.array(info["bounds_hi"], np.float32), hi)
+    assert_same(g.closest(rays), b.closest(rays))
+    assert np.array_equal(g.any(rays), b.any(rays))
+    g.close()
+
+
+def test_gpu_build_tiny_and_degenerate(ctx):
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 3, 4, 5, 9, 33):
+        v = rng.uniform(-1, 1, (3 * n, 3)).astype(np.float32)
+        f = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+        rays = S.incoherent_rays(4096, (-1, -1, -1), (1, 1, 1), seed=n)
+        g = ctx.upload(v, f, gpu_build=True)
+        assert_same(g.closest(rays), O.OracleBVH(v, f).closest(rays))
+        g.close()
+    # duplicates, a degenerate (zero-area) triangle, all centroids equal
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.5, 0.5, 0], [0.5, 0.5, 0], [0.5, 0.5, 0]], np.float32)
+    f = np.array([[0, 1, 2]] * 40 + [[3, 4, 5]] * 3, np.uint32)
+    rays = S.camera_rays(64, 64, eye=(0.3, 0.3, 2.0), target=(0.3, 0.3, 0.0))
+    g = ctx.upload(v, f, gpu_build=True)
+    assert_same(g.closest(rays), O.OracleBVH(v, f).closest(rays))
+    g.close()
+
+
+def test_gpu_build_rejects_bad_input(ctx):
+    import foundation_gb300 as fg
+    v = np.zeros((3, 3), np.float32)
+    with pytest.raises(fg.FndError):
+        ctx.upload(v, np.array([[0, 1, 3]], np.uint32), gpu_build=True)
+    v2 = v.copy()
+    v2[1, 0] = np.nan
+    with pytest.raises(fg.FndError):
+        ctx.upload(v2, np.array([[0, 1, 2]], np.uint32), gpu_build=True)
+    with pytest.raises(fg.FndError):
+        ctx.upload(v, np.array([[0, 1, 2]], np.uint32), gpu_build=True, spatial_splits=True)
+    g = ctx.upload(v, np.zeros((0, 3), np.uint32), gpu_build=True)  # empty scene still works
+    assert (g.closest(S.cube_camera_rays(10))["prim"] == fg.INVALID_ID).all()
+    g.close()
+
+
+def test_gpu_built_scene_renders_like_host_built(ctx):
+    cs = S.cornell_scene()
+    imgs, stats = [], []
+    for gpu in (False, True):
+        s = ctx.upload(cs.verts, cs.idx, gpu_build=gpu)
+        s.set_materials(cs.tri_material, S.material_records(cs))
+        s.set_lights(S.light_records(cs))
+        imgs.append(ctx.render(s, 96, 54, 32, S.CORNELL_CAMERA, seed=4))
+        st = ctx.render_stats()
+        stats.append((st["extension_rays"], st["shadow_rays"]))
+        s.close()
+    assert stats[0] == stats[1]
+    np.testing.assert_allclose(imgs[1], imgs[0], rtol=1e-4, atol=1e-6)
