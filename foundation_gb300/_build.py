@@ -32,7 +32,8 @@ HOST_FLAGS = ["-Xcompiler", "-ffp-contract=off"]
 # path-tracing stages: the vertex logic (pt/shade.cuh) is inlined into the
 # wavefront shade kernel, the tail megakernel and the training megakernel;
 # without contraction the three evaluate it to the same bits, so a path gives
-# the same result whichever kernel runs it
+# the same result whichever kernel runs it. The raster pass likewise keeps
+# the expression tree its scalar restatement evaluates.
 PT_FLAGS = ["-fmad=false"]
 
 
@@ -70,7 +71,7 @@ def _compile(src: str, force: bool, newest_header: float) -> tuple[str, bool]:
     cmd = [nvcc(), *ARCH, *COMMON]
     if src.endswith(".cpp"):
         cmd += HOST_FLAGS
-    elif os.path.basename(os.path.dirname(src)) == "pt":
+    elif os.path.basename(os.path.dirname(src)) in ("pt", "raster"):
         cmd += PT_FLAGS
     cmd += ["-c", src, "-o", obj + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -428,6 +428,39 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
     });
 }
 
+int fnd_rt_tonemap(fnd_rt_ctx* ctx, const float* rgb, uint32_t width, uint32_t height, int mem_in, float exposure,
+                   uint32_t mode, uint8_t* rgba, int mem_out) {
+    if (!ctx) return FND_ERR_INVALID_ARG;
+    return Guard(ctx, [&] {
+        CHECK(rgb != nullptr && rgba != nullptr);
+        CHECK((mem_in == FND_MEM_HOST || mem_in == FND_MEM_DEVICE) && (mem_out == FND_MEM_HOST || mem_out == FND_MEM_DEVICE));
+        CHECK_CODE(mode <= FND_TONEMAP_ACES, FND_ERR_INVALID_ARG, "tonemap mode %u", mode);
+        CHECK_CODE(std::isfinite(exposure) && exposure >= 0.0f, FND_ERR_INVALID_ARG, "exposure %g", (double)exposure);
+        CHECK_CODE((uint64_t)width * height <= (1ull << 28), FND_ERR_INVALID_ARG, "image %ux%u", width, height);
+        const uint32_t npix = width * height;
+        if (npix == 0) return;
+        CUDA_CHECK(cudaSetDevice(ctx->device));
+        CHECK_CODE(mem_out == FND_MEM_HOST || ((uintptr_t)rgba & 3u) == 0, FND_ERR_INVALID_ARG,
+                   "device rgba must be 4-byte aligned");
+        const float* src = rgb;
+        if (mem_in == FND_MEM_HOST) {
+            CApi::EnsureDevice(ctx->d_in, ctx->d_in_cap, 12ull * npix);
+            CUDA_CHECK(cudaMemcpyAsync(ctx->d_in, rgb, 12ull * npix, cudaMemcpyHostToDevice, ctx->stream));
+            src = static_cast<const float*>(ctx->d_in);
+        }
+        uint32_t* dst = reinterpret_cast<uint32_t*>(rgba);
+        if (mem_out == FND_MEM_HOST) {
+            CApi::EnsureDevice(ctx->d_out, ctx->d_out_cap, 4ull * npix);
+            dst = static_cast<uint32_t*>(ctx->d_out);
+        }
+        CUDA_CHECK(PT::LaunchTonemap(src, npix, exposure, mode, dst, ctx->stream));
+        if (mem_out == FND_MEM_HOST) {
+            CUDA_CHECK(cudaMemcpyAsync(rgba, dst, 4ull * npix, cudaMemcpyDeviceToHost, ctx->stream));
+            CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        }
+    });
+}
+
 int fnd_rt_render_stats_get(fnd_rt_ctx* ctx, fnd_render_stats* out) {
     if (!ctx || !out) return FND_ERR_INVALID_ARG;
     return Guard(ctx, [&] {

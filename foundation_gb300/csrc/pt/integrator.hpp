@@ -139,6 +139,9 @@ cudaError_t LaunchShade(const PathBuffers& B, const RenderParams& R, const Shade
                         uint32_t bounce, int grid, cudaStream_t s);
 cudaError_t LaunchResolve(const PathBuffers& B, int grid, cudaStream_t s);
 cudaError_t LaunchFinalize(const PathBuffers& B, float* rgb, uint32_t npix, float scale, cudaStream_t s);
+// tonemap.cu: linear RGB floats -> R8G8B8A8_UNORM words (FND_TONEMAP_* mode)
+cudaError_t LaunchTonemap(const float* rgb, uint32_t npix, float exposure, uint32_t mode, uint32_t* rgba,
+                          cudaStream_t s);
 
 }  // namespace PT
 }  // namespace Foundation

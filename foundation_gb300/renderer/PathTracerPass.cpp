@@ -100,6 +100,13 @@ void PathTracerPass::Readback(std::span<float> rgb) {
     std::memcpy(rgb.data(), m_frame, m_frame_bytes);
 }
 
+void PathTracerPass::ReadbackRGBA8(std::span<uint8_t> rgba, float exposure, uint32_t mode) {
+    CHECK(m_frame != nullptr && rgba.size() >= 4ull * m_desc.width * m_desc.height);
+    Check(fnd_rt_tonemap(m_ctx, m_frame, m_desc.width, m_desc.height, FND_MEM_HOST, exposure, mode, rgba.data(),
+                         FND_MEM_HOST),
+          "fnd_rt_tonemap");
+}
+
 void PathTracerPass::TraceClosest(std::span<const fnd_ray> rays, std::span<fnd_hit> hits) {
     CHECK(m_scene != nullptr && hits.size() >= rays.size());
     Check(fnd_rt_trace_closest(m_ctx, m_scene, rays.data(), (uint32_t)rays.size(), hits.data(), FND_MEM_HOST),

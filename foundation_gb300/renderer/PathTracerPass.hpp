@@ -58,6 +58,9 @@ public:
 
     // Mean radiance so far, width*height*3 floats (row-major from the top).
     void Readback(std::span<float> rgb);
+    // The same frame in the reference's colour-target format R8G8B8A8_UNORM
+    // (width*height*4 bytes, fnd_rt_tonemap with `mode` and `exposure`).
+    void ReadbackRGBA8(std::span<uint8_t> rgba, float exposure = 1.0f, uint32_t mode = FND_TONEMAP_ACES);
 
     void TraceClosest(std::span<const fnd_ray> rays, std::span<fnd_hit> hits);
     void TraceAny(std::span<const fnd_ray> rays, std::span<uint8_t> occluded);

@@ -1,29 +1,49 @@
 // pass_demo.cpp — drives the path-tracer pass the way the reference's Editor
 // drives its renderer (src/Editor/Editor.cpp:14-28: create, then Draw() per
-// frame), headless: loads an OBJ scene, renders, writes a PFM image.
+// frame), headless: loads an OBJ scene, renders, writes the frame to a file:
+// out.pfm keeps the linear radiance, out.png the display pixels
+// (R8G8B8A8_UNORM through fnd_rt_tonemap, ACES curve, exposure 1).
 //
-// usage: fnd_pass_demo scene.obj out.pfm width height spp_per_draw draws
+// usage: fnd_pass_demo scene.obj out.{pfm,png} width height spp_per_draw draws
 //                      eye_x eye_y eye_z target_x target_y target_z vfov_deg [sky]
 #include <cstdio>
 #include <cstdlib>
 #include <string>
 #include <vector>
 
+#include "ImageIO.hpp"
 #include "ObjLoader.hpp"
 #include "PathTracerPass.hpp"
 
 using namespace Foundation;
 
-static void WritePfm(const char* path, const std::vector<float>& rgb, uint32_t w, uint32_t h) {
-    FILE* f = std::fopen(path, "wb");
-    if (!f) Core::Fail(FND_ERR_IO, "cannot write %s", path);
-    std::fprintf(f, "PF\n%u %u\n-1.0\n", w, h);
-    for (uint32_t y = 0; y < h; ++y)  // PFM rows run bottom to top
-        std::fwrite(&rgb[3 * (size_t)(h - 1 - y) * w], sizeof(float), 3 * (size_t)w, f);
-    std::fclose(f);
+static bool EndsWith(const std::string& s, const char* suffix) {
+    const std::string x(suffix);
+    return s.size() >= x.size() && s.compare(s.size() - x.size(), x.size(), x) == 0;
 }
 
 int main(int argc, char** argv) {
+    if (argc == 3 && std::string(argv[1]) == "--write-test-png") {
+        // no GPU: a 37 x 23 gradient (r = 7x, g = 11y, b = x ^ y, a = 255 - x - y)
+        // through the PNG writer, for the CPU test of the encoder
+        const uint32_t w = 37, h = 23;
+        std::vector<uint8_t> rgba(4 * (size_t)w * h);
+        for (uint32_t y = 0; y < h; ++y)
+            for (uint32_t x = 0; x < w; ++x) {
+                uint8_t* p = &rgba[4 * ((size_t)y * w + x)];
+                p[0] = (uint8_t)(7 * x);
+                p[1] = (uint8_t)(11 * y);
+                p[2] = (uint8_t)(x ^ y);
+                p[3] = (uint8_t)(255 - x - y);
+            }
+        try {
+            Renderer::WritePng(argv[2], rgba, w, h);
+        } catch (const Core::FndError& e) {
+            std::fprintf(stderr, "error %d: %s\n", e.code(), e.what());
+            return 1;
+        }
+        return 0;
+    }
     if (argc == 3 && std::string(argv[1]) == "--parse") {
         // load only (no GPU): prints the counts the pass would upload
         try {
@@ -72,7 +92,13 @@ int main(int argc, char** argv) {
             for (int i = 0; i < draws; ++i) pass.Draw();
             std::vector<float> rgb(3 * (size_t)desc.width * desc.height);
             pass.Readback(rgb);
-            WritePfm(argv[2], rgb, desc.width, desc.height);
+            if (EndsWith(argv[2], ".png")) {
+                std::vector<uint8_t> rgba(4 * (size_t)desc.width * desc.height);
+                pass.ReadbackRGBA8(rgba);
+                Renderer::WritePng(argv[2], rgba, desc.width, desc.height);
+            } else {
+                Renderer::WritePfm(argv[2], rgb, desc.width, desc.height);
+            }
             std::printf("rendered %u x %u, %u spp, %u triangles, %zu materials, %zu lights\n", desc.width, desc.height,
                         pass.SamplesAccumulated(), pass.SceneInfo().num_tris, obj.materials.size(), obj.lights.size());
         }

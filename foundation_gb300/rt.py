@@ -46,6 +46,7 @@ BVH_GPU_BUILD = 2
 RENDER_CACHE = 2
 RENDER_WAVEFRONT = 4
 RENDER_TRAIN_ONLY = 8
+TONEMAP_CLAMP, TONEMAP_REINHARD, TONEMAP_ACES = 0, 1, 2
 CACHE_NUM_PARAMS = 22720
 CACHE_NUM_FEATURES = 96
 
@@ -105,6 +106,29 @@ class TraceConfig(C.Structure):
                     postpone_min=self.postpone_min, sort_bits=self.sort_bits)
 
 
+RASTER_VERTEX_DTYPE = np.dtype([("pos", "<f4", 2), ("color", "<f4", 3), ("uv", "<f4", 2)])
+# the reference renderer's quad (src/Renderer/Renderer.cpp:153-157, 175)
+REFERENCE_QUAD = np.array([((-0.5, -0.5), (1.0, 0.0, 0.0), (1.0, 0.0)), ((0.5, -0.5), (0.0, 1.0, 0.0), (0.0, 0.0)),
+                           ((0.5, 0.5), (0.0, 0.0, 1.0), (0.0, 1.0)), ((-0.5, 0.5), (1.0, 1.0, 1.0), (1.0, 1.0))],
+                          RASTER_VERTEX_DTYPE)
+REFERENCE_QUAD_INDICES = np.array([0, 1, 2, 2, 3, 0], np.uint16)
+
+
+class RasterDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("model", C.c_float * 16), ("view", C.c_float * 16),
+                ("proj", C.c_float * 16), ("clear", C.c_float * 4), ("cull_back", C.c_uint32)]
+
+
+def raster_uniforms(time_s: float, aspect: float = 1920.0 / 1080.0):
+    """The reference renderer's model, view and proj matrices at time t
+    (column-major float32 arrays of 16)."""
+    m, v, p = (np.zeros(16, np.float32) for _ in range(3))
+    rc = load().fnd_rt_raster_uniforms(C.c_float(time_s), C.c_float(aspect), _ptr(m), _ptr(v), _ptr(p))
+    if rc != 0:
+        raise FndError(rc, "fnd_rt_raster_uniforms: invalid arguments")
+    return m, v, p
+
+
 class TuneEntry(C.Structure):
     _fields_ = [("config", TraceConfig), ("ms", C.c_float)]
 
@@ -154,6 +178,9 @@ SIGNATURES = {
     "fnd_rt_scene_set_lights": (_I32, [_P, _P, _U32]),
     "fnd_rt_render": (_I32, [_P, _P, _P, _P, _I32]),
     "fnd_rt_render_stats_get": (_I32, [_P, _P]),
+    "fnd_rt_tonemap": (_I32, [_P, _P, _U32, _U32, _I32, C.c_float, _U32, _P, _I32]),
+    "fnd_rt_raster_uniforms": (_I32, [C.c_float, C.c_float, _P, _P, _P]),
+    "fnd_rt_raster_draw": (_I32, [_P, _P, _P, _U32, _P, _U32, _P, _U32, _U32, _P, _I32]),
     "fnd_rt_set_trace_config": (_I32, [_P, _P]),
     "fnd_rt_get_trace_config": (_I32, [_P, _P]),
     "fnd_rt_tune": (_I32, [_P, _P, _P, _U32, _U32, _U32, _P, _U32, _P, _P]),
@@ -282,6 +309,41 @@ class Context:
             return out
         img = np.empty((height, width, 3), np.float32) if out is None else out
         _check(load().fnd_rt_render(self._h, scene.handle, C.byref(d), _ptr(img), FND_MEM_HOST), self._h)
+        return img
+
+    def tonemap(self, rgb, width: int, height: int, exposure: float = 1.0, mode: int = 2, out=None):
+        """Linear RGB (host array or CUDA tensor of width*height*3 floats) to
+        R8G8B8A8_UNORM pixels: (height, width, 4) uint8 on the host, or into
+        `out` (a CUDA uint8 tensor of width*height*4), asynchronously."""
+        mem_in = FND_MEM_DEVICE if _is_device(rgb) else FND_MEM_HOST
+        if mem_in == FND_MEM_HOST:
+            rgb = np.ascontiguousarray(rgb, np.float32)
+        if out is not None and _is_device(out):
+            _check(load().fnd_rt_tonemap(self._h, _ptr(rgb), width, height, mem_in, exposure, mode, _ptr(out),
+                                         FND_MEM_DEVICE), self._h)
+            return out
+        img = np.empty((height, width, 4), np.uint8)
+        _check(load().fnd_rt_tonemap(self._h, _ptr(rgb), width, height, mem_in, exposure, mode, _ptr(img),
+                                     FND_MEM_HOST), self._h)
+        return img
+
+    def raster_draw(self, width: int, height: int, model, view, proj, texture, verts=None, indices=None,
+                    clear=(0.0, 0.0, 0.0, 1.0), cull_back: bool = True, out=None):
+        """The raster pass (the reference renderer's DrawIndexed): texture is a
+        (h, w, 4) uint8 array; verts / indices default to the reference quad.
+        Returns (height, width, 4) uint8, or fills the CUDA tensor `out`."""
+        verts = REFERENCE_QUAD if verts is None else np.ascontiguousarray(verts, RASTER_VERTEX_DTYPE)
+        indices = REFERENCE_QUAD_INDICES if indices is None else np.ascontiguousarray(indices, np.uint16)
+        tex = np.ascontiguousarray(texture, np.uint8)
+        d = RasterDesc(width, height, (C.c_float * 16)(*model), (C.c_float * 16)(*view), (C.c_float * 16)(*proj),
+                       (C.c_float * 4)(*clear), 1 if cull_back else 0)
+        args = (self._h, C.byref(d), _ptr(verts), len(verts), _ptr(indices), len(indices), _ptr(tex), tex.shape[1],
+                tex.shape[0])
+        if out is not None and _is_device(out):
+            _check(load().fnd_rt_raster_draw(*args, _ptr(out), FND_MEM_DEVICE), self._h)
+            return out
+        img = np.empty((height, width, 4), np.uint8)
+        _check(load().fnd_rt_raster_draw(*args, _ptr(img), FND_MEM_HOST), self._h)
         return img
 
     # ---- launch shape -------------------------------------------------

@@ -347,6 +347,58 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
 /* Counters of the last fnd_rt_render call (synchronises the stream). */
 int fnd_rt_render_stats_get(fnd_rt_ctx* ctx, fnd_render_stats* out);
 
+/* ---- image output ---------------------------------------------------------
+ * Linear radiance (width*height RGB floats, row-major from the top row, the
+ * layout fnd_rt_render writes) to R8G8B8A8_UNORM pixels, the format of the
+ * reference renderer's colour target (src/Renderer/Renderer.cpp:40,81):
+ * exposure, tone curve, sRGB transfer function (the target is UNORM), 8-bit
+ * rounding, alpha 255. Replaces the swapchain present of Renderer::Draw
+ * (Renderer.cpp:395-399) with a buffer the caller writes out. */
+enum { FND_TONEMAP_CLAMP = 0u, FND_TONEMAP_REINHARD = 1u, FND_TONEMAP_ACES = 2u };
+
+int fnd_rt_tonemap(fnd_rt_ctx* ctx, const float* rgb, uint32_t width, uint32_t height, int mem_in, float exposure,
+                   uint32_t mode, uint8_t* rgba, int mem_out);
+
+/* ---- raster pass -----------------------------------------------------------
+ * CUDA restatement of the reference renderer's only pass
+ * (src/Renderer/Renderer.cpp:312-366, src/Renderer/Triangle.slang): an indexed
+ * triangle list of vertex_input records (Renderer.cpp:23-27) transformed by
+ * proj * view * model, back faces culled (front faces counter-clockwise,
+ * Renderer.cpp:127-131), no depth test, fragment = texture(uv) * (colour, 1),
+ * written to an R8G8B8A8_UNORM target cleared to `clear`. Where the graphics
+ * API leaves rules to the implementation this pass fixes them: vertices
+ * snapped to 1/256 pixel, pixel centres at +0.5, the top-left fill rule,
+ * perspective-correct interpolation, bilinear filtering with repeat
+ * addressing (the reference sampler's linear filters and repeat mode on its
+ * single mip level; its anisotropic taps are implementation-defined), and
+ * no clipping: a triangle with a vertex behind the eye is skipped. */
+typedef struct fnd_raster_vertex {
+    float pos[2];
+    float color[3];
+    float uv[2];
+} fnd_raster_vertex;
+
+typedef struct fnd_raster_desc {
+    uint32_t width, height;  /* colour target (1920 x 1080 in the reference) */
+    float model[16];         /* column-major, as the uniform buffer of Renderer.cpp:28-33 */
+    float view[16];
+    float proj[16];
+    float clear[4];          /* clear colour (the reference clears to 0, 0, 0, 1) */
+    uint32_t cull_back;      /* 1: cull back faces (the reference's state) */
+} fnd_raster_desc;
+
+/* The reference's per-frame uniforms at time t seconds (Renderer.cpp:370-380):
+ * model rotates 90 degrees per second about +z, view looks from (2, 2, 2) at
+ * the origin with +z up, proj is an infinite perspective of 45 degrees and
+ * near plane 0.1 with the y axis flipped. Host-only; no context needed. */
+int fnd_rt_raster_uniforms(float time_s, float aspect, float* model, float* view, float* proj);
+
+/* Draws ni / 3 triangles (host vertex, index and RGBA8 texture arrays) into
+ * rgba (width*height*4 bytes, top row first; host or device per mem). */
+int fnd_rt_raster_draw(fnd_rt_ctx* ctx, const fnd_raster_desc* desc, const fnd_raster_vertex* verts, uint32_t nv,
+                       const uint16_t* idx, uint32_t ni, const uint8_t* texture, uint32_t tex_w, uint32_t tex_h,
+                       uint8_t* rgba, int mem);
+
 /* ---- radiance cache -----------------------------------------------------
  * An online-trained MLP (96 -> 5 x 64 ReLU -> 3, BF16 tensor cores, FP32
  * Adam) that predicts reflected radiance. With FND_RENDER_CACHE a render

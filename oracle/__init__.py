@@ -19,7 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "librt_oracle.so")
-SOURCES = ["rt_oracle.cpp", "pt_oracle.cpp", "mlp_oracle.cpp"]
+SOURCES = ["rt_oracle.cpp", "pt_oracle.cpp", "mlp_oracle.cpp", "raster_oracle.cpp"]
 HEADERS = ["rt_oracle.h", "oracle_common.hpp", "rt_oracle_internal.hpp"]
 CXXFLAGS = ["-O3", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared", "-pthread"]
 
@@ -217,4 +217,53 @@ def nrc_encode(p, wo, n, rough, albedo, lo, hi) -> np.ndarray:
     lo = np.asarray(lo, np.float32)
     hi = np.asarray(hi, np.float32)
     lib().orc_nrc_encode(_ptr(rec), _ptr(lo), _ptr(hi), _ptr(out))
+    return out
+
+
+# ---- display encoding (foundation_gb300/csrc/pt/tonemap.cu) -----------------
+def tonemap_rgba8(rgb, exposure: float = 1.0, mode: int = 2) -> np.ndarray:
+    """Linear RGB (h, w, 3) -> R8G8B8A8 (h, w, 4): exposure, tone curve (0
+    clamp, 1 Reinhard x/(1+x), 2 the ACES fit of Narkowicz 2015:
+    x(2.51x+0.03)/(x(2.43x+0.59)+0.14)), clamp to [0,1], sRGB transfer
+    function (IEC 61966-2-1), round to 8 bits; alpha 255. Float32 operations
+    in the device's order except the power, evaluated in float64 (so codes
+    agree to within one step)."""
+    f = np.float32
+    x = np.asarray(rgb, np.float32) * f(exposure)
+    pos = x > 0
+    x = np.where(pos, x, f(0))
+    if mode == 1:
+        x = x / (f(1) + x)
+    elif mode == 2:
+        x = (x * (f(2.51) * x + f(0.03))) / (x * (f(2.43) * x + f(0.59)) + f(0.14))
+    x = np.minimum(x, f(1)).astype(np.float32)
+    lin = f(12.92) * x
+    gam = (f(1.055) * np.power(x.astype(np.float64), 1.0 / 2.4).astype(np.float32) - f(0.055)).astype(np.float32)
+    s = np.where(x <= f(0.0031308), lin, gam).astype(np.float32)
+    q = np.clip(np.floor(s * f(255) + f(0.5)), 0, 255).astype(np.uint8)
+    q = np.where(pos, q, 0).astype(np.uint8)
+    a = np.full(q.shape[:-1] + (1,), 255, np.uint8)
+    return np.concatenate([q, a], -1)
+
+
+# ---- raster pass (raster_oracle.cpp) -----------------------------------------
+def raster_draw(width: int, height: int, model, view, proj, texture, verts, indices, clear=(0.0, 0.0, 0.0, 1.0),
+                cull_back: bool = True) -> np.ndarray:
+    """The scalar raster pass: verts (n, 7) float32 (pos xy, colour rgb, uv),
+    indices uint16, texture (h, w, 4) uint8 -> (height, width, 4) uint8."""
+    L = lib()
+    f = L.orc_raster_draw
+    f.restype = None
+    P = C.c_void_p
+    f.argtypes = [C.c_uint32, C.c_uint32, P, P, P, P, C.c_int, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32,
+                  C.c_uint32, P]
+    m, v, p = (np.ascontiguousarray(x, np.float32) for x in (model, view, proj))
+    cl = np.ascontiguousarray(clear, np.float32)
+    vt = np.ascontiguousarray(verts, np.float32).reshape(-1, 7)
+    ix = np.ascontiguousarray(indices, np.uint16)
+    tex = np.ascontiguousarray(texture, np.uint8)
+    out = np.zeros((height, width, 4), np.uint8)
+    ptr = lambda a: a.ctypes.data_as(P)  # noqa: E731
+    f(width, height, ptr(m), ptr(v), ptr(p), ptr(cl), 1 if cull_back else 0, ptr(vt), len(vt), ptr(ix), len(ix),
+      ptr(tex), tex.shape[1], tex.shape[0], ptr(out))
     return out

@@ -64,3 +64,24 @@ def test_cpp_pass_matches_python_binding(built, tmp_path):
     assert img.shape == (36, 64, 3)
     rel = np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2))
     assert rel < 0.05 and abs(img.mean() / ref.mean() - 1) < 0.03
+
+
+@pytest.mark.gpu
+def test_cpp_pass_png_output(built, tmp_path):
+    """The pass's display readback (PathTracerPass::ReadbackRGBA8 ->
+    fnd_rt_tonemap) written as PNG equals the display encoding of its own
+    PFM frame, computed by the oracle (one code of slack for powf)."""
+    import oracle as O
+    from foundation_gb300 import image
+    cs = S.cornell_scene(num_spheres=10, level=1)
+    p = str(tmp_path / "cornell.obj")
+    S.write_obj(cs, p)
+    cam = S.CORNELL_CAMERA
+    args = ["48", "27", "16", "2", *map(str, cam["eye"]), *map(str, cam["target"]), str(cam["vfov_deg"])]
+    for out in ("out.pfm", "out.png"):
+        r = subprocess.run([DEMO, p, str(tmp_path / out), *args], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr + r.stdout
+    png = image.read_png(str(tmp_path / "out.png"))
+    want = O.tonemap_rgba8(image.read_pfm(str(tmp_path / "out.pfm")), 1.0, 2)
+    assert png.shape == (27, 48, 4)
+    assert np.abs(png.astype(int) - want.astype(int)).max() <= 1
