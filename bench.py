@@ -430,6 +430,15 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
     for _ in range(2):
         s.closest(rd, hd)
     trace_ms = sum(timed(lambda: s.closest(rd, hd)) for _ in range(5)) / 5
+    # the same scene built on the GPU (linear BVH + device collapse)
+    t0 = time.perf_counter()
+    g = ctx.upload(tr.verts, tr.idx, gpu_build=True)
+    gpu_upload_s = time.perf_counter() - t0
+    ginfo = g.info()
+    for _ in range(2):
+        g.closest(rd, hd)
+    gpu_trace_ms = sum(timed(lambda: g.closest(rd, hd)) for _ in range(5)) / 5
+    g.close()
     del rd, hd
     ref = CV.render_reference(ctx, s, W, H, cam, ref_spp, chunk=16, seed=9001, **kw)
     out = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
@@ -452,6 +461,9 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
             "gen_s": gen_s, "upload_s": upload_s, "build_ms": info["build_ms"], "collapse_ms": info["collapse_ms"],
             "wide_nodes": info["num_wide_nodes"], "node_bytes": info["node_bytes"], "tri_bytes": info["tri_bytes"],
             "incoherent_mrays_s": n_rays / (trace_ms * 1e-3) / 1e6,
+            "gpu_build": {"upload_s": gpu_upload_s, "build_ms": ginfo["build_ms"], "collapse_ms": ginfo["collapse_ms"],
+                          "wide_nodes": ginfo["num_wide_nodes"],
+                          "incoherent_mrays_s": n_rays / (gpu_trace_ms * 1e-3) / 1e6},
             "reference_spp": ref_spp, "est_reference_relmse": r_plain * spp / ref_spp,
             "plain": {"spp": spp, "ms": plain_ms, "relmse": r_plain, "extension_rays": st["extension_rays"],
                       "shadow_rays": st["shadow_rays"],

@@ -44,14 +44,14 @@ float HalfArea(const BinaryNode& n) {
 
 }  // namespace
 
-void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out) {
+void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out, float margin_scale) {
     CHECK(!bin.nodes.empty());
     const BinaryNode& root = bin.nodes[0];
     for (int i = 0; i < 3; ++i) {
         out.lo[i] = root.lo[i];
         out.hi[i] = root.hi[i];
     }
-    const float margin = SceneMargin(root.lo, root.hi);
+    const float margin = SceneMargin(root.lo, root.hi) * margin_scale;
     out.margin = margin;
     out.nodes.clear();
     out.nodes.reserve(bin.nodes.size() / 4 + 1);

@@ -26,7 +26,10 @@ float SceneMargin(const float lo[3], const float hi[3]);
 
 // Greedy collapse (largest-surface-area internal child expanded first until 8
 // children), octant-ordered slot assignment, 8-bit outward quantisation.
-void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out);
+// margin_scale multiplies SceneMargin (a bottom-level scene whose instances
+// shrink it far below the world's size needs a wider margin: its object-space
+// ray origins lie further away, see fnd_rt_instances_upload).
+void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out, float margin_scale = 1.0f);
 
 }  // namespace RT
 }  // namespace Foundation

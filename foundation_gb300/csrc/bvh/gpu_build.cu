@@ -686,7 +686,7 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
         out.lo[a] = h_bounds[a];
         out.hi[a] = h_bounds[3 + a];
     }
-    out.margin = SceneMargin(out.lo, out.hi);
+    out.margin = SceneMargin(out.lo, out.hi) * p.margin_scale;
     morton_kernel<<<g256, 256, 0, s>>>(n, B);
     RadixSort(B, n, s);
     if (n >= 2) {

@@ -23,6 +23,7 @@ constexpr uint32_t kGpuBuildMaxTris = 1u << 27;  // radix-sort scan capacity
 struct GpuBuildParams {
     uint32_t max_leaf = 4;
     float trav_cost = 1.0f;
+    float margin_scale = 1.0f;
 };
 
 struct GpuBuildOutput {

@@ -186,6 +186,7 @@ int fnd_rt_tune(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays,
     if (!ctx) return FND_ERR_INVALID_ARG;
     return Guard(ctx, [&] {
         CHECK(scene && scene->ctx == ctx && rays && n > 0 && kind <= FND_QUERY_ANY);
+        CHECK_CODE(!scene->two_level, FND_ERR_INVALID_ARG, "two-level scenes are not tuned");
         CHECK_CODE(((uintptr_t)rays & 15u) == 0, FND_ERR_INVALID_ARG, "device rays must be 16-byte aligned");
         CUDA_CHECK(cudaSetDevice(ctx->device));
         const bool any = kind == FND_QUERY_ANY;
@@ -223,6 +224,7 @@ int fnd_rt_batch_create(fnd_rt_ctx* ctx, const fnd_rt_batch_job* jobs, uint32_t 
         for (uint32_t i = 0; i < njobs; ++i) {
             const fnd_rt_batch_job& j = jobs[i];
             CHECK_CODE(j.scene && j.scene->ctx == ctx, FND_ERR_INVALID_ARG, "job %u: scene of another context", i);
+            CHECK_CODE(!j.scene->two_level, FND_ERR_INVALID_ARG, "job %u: two-level scenes are not batched", i);
             CHECK_CODE(j.kind <= FND_QUERY_ANY, FND_ERR_INVALID_ARG, "job %u: kind %u", i, j.kind);
             CHECK_CODE(j.n == 0 || (j.rays && j.out), FND_ERR_INVALID_ARG, "job %u: null buffer", i);
             CHECK_CODE(((uintptr_t)j.rays & 15u) == 0 && ((uintptr_t)j.out & (j.kind ? 0u : 7u)) == 0,

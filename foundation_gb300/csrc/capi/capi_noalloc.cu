@@ -81,6 +81,7 @@ extern "C" int fnd_rt_trace_closest_noalloc(const fnd_rt_scene* scene, const fnd
     fnd_rt_ctx* ctx = scene->ctx;
     return CApi::Guard(ctx, [&] {
         CHECK(n == 0 || (rays != nullptr && out != nullptr));
+        CHECK_CODE(!scene->two_level, FND_ERR_INVALID_ARG, "two-level scenes are traced with fnd_rt_trace_closest");
         CHECK_CODE(n <= kNoAllocMaxRays, FND_ERR_INVALID_ARG,
                    "%u rays exceed the no-allocation limit of %u rays per call; split the batch or use "
                    "fnd_rt_trace_closest",

@@ -165,6 +165,7 @@ int fnd_rt_scene_set_materials(fnd_rt_scene* scene, const uint32_t* tri_material
     if (!scene) return FND_ERR_INVALID_ARG;
     fnd_rt_ctx* ctx = scene->ctx;
     return Guard(ctx, [&] {
+        CHECK_CODE(!scene->two_level, FND_ERR_INVALID_ARG, "two-level scenes carry no materials");
         CHECK_CODE(nt == scene->info.num_tris, FND_ERR_INVALID_ARG, "%u material ids for %u triangles", nt,
                    scene->info.num_tris);
         CHECK(nm >= 1 && materials != nullptr && (nt == 0 || tri_material != nullptr));
@@ -217,6 +218,7 @@ int fnd_rt_scene_set_lights(fnd_rt_scene* scene, const fnd_quad_light* lights, u
     if (!scene) return FND_ERR_INVALID_ARG;
     fnd_rt_ctx* ctx = scene->ctx;
     return Guard(ctx, [&] {
+        CHECK_CODE(!scene->two_level, FND_ERR_INVALID_ARG, "two-level scenes carry no lights");
         CHECK(nl == 0 || lights != nullptr);
         std::vector<PT::DevQuadLight> dl(nl);
         for (uint32_t i = 0; i < nl; ++i) {
@@ -251,6 +253,7 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
     return Guard(ctx, [&] {
         CHECK(scene != nullptr && scene->ctx == ctx && desc != nullptr);
         CHECK(mem == FND_MEM_HOST || mem == FND_MEM_DEVICE);
+        CHECK_CODE(!scene->two_level, FND_ERR_INVALID_ARG, "two-level scenes are traced, not rendered");
         const fnd_render_desc& D = *desc;
         const bool train_only = (D.flags & FND_RENDER_TRAIN_ONLY) != 0;
         CHECK_CODE(rgb != nullptr || train_only, FND_ERR_INVALID_ARG, "rgb is NULL");

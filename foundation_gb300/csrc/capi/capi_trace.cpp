@@ -116,7 +116,7 @@ void DefaultMaterial(fnd_rt_scene* scene) {
 // FND_BVH_GPU_BUILD: the vertices and indices go to the device once and the
 // tree is built there (bvh/gpu_build.cu).
 void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, uint32_t nv, const uint32_t* idx,
-                    uint32_t nt, const RT::BuildParams& bp) {
+                    uint32_t nt, const RT::BuildParams& bp, float margin_scale) {
     void *d_verts = nullptr, *d_idx = nullptr;
     RT::GpuBuildOutput go;
     try {
@@ -130,6 +130,7 @@ void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, ui
         RT::GpuBuildParams gp;
         gp.max_leaf = bp.max_leaf;
         gp.trav_cost = bp.trav_cost;
+        gp.margin_scale = margin_scale;
         RT::BuildWideGpu(static_cast<const float*>(d_verts), nv, static_cast<const uint32_t*>(d_idx), nt, gp, go,
                          ctx->stream);
         CUDA_CHECK(cudaFree(d_verts));
@@ -292,6 +293,9 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         }
         CHECK_CODE(bp.max_refs_factor >= 0.0 && bp.max_refs_factor <= 4.0, FND_ERR_INVALID_ARG,
                    "split_budget %g not in [0, 4]", bp.max_refs_factor);
+        const float margin_scale = bvh && bvh->margin_scale != 0.0f ? bvh->margin_scale : 1.0f;
+        CHECK_CODE(margin_scale >= 1.0f && margin_scale <= 65536.0f, FND_ERR_INVALID_ARG,
+                   "margin_scale %g not in [1, 65536]", (double)margin_scale);
         CHECK_CODE(bp.trav_cost > 0.0f && bp.trav_cost <= 64.0f, FND_ERR_INVALID_ARG, "traversal_cost %g not in (0, 64]",
                    (double)bp.trav_cost);
         CHECK_CODE(bp.bins >= 2 && bp.bins <= 64, FND_ERR_INVALID_ARG, "sah_bins %u not in [2, 64]", bp.bins);
@@ -312,7 +316,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             return;
         }
         if (gpu_build) {
-            UploadGpuBuilt(ctx, scene.get(), verts, nv, idx, nt, bp);
+            UploadGpuBuilt(ctx, scene.get(), verts, nv, idx, nt, bp, margin_scale);
             *out_scene = scene.release();
             ctx->live_scenes++;
             return;
@@ -380,7 +384,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         scene->info.build_ms = MsSince(t0);
         t0 = std::chrono::steady_clock::now();
         RT::WideBvh wide;
-        RT::CollapseToWide(bin, tri.data(), nt, wide);
+        RT::CollapseToWide(bin, tri.data(), nt, wide, margin_scale);
         scene->info.collapse_ms = MsSince(t0);
         CHECK_CODE(wide.depth <= (uint32_t)RT::kMaxStack / 2, FND_ERR_INVALID_SCENE,
                    "wide BVH depth %u exceeds the traversal stack bound %d", wide.depth, RT::kMaxStack / 2);
@@ -443,9 +447,16 @@ int fnd_rt_scene_info_get(const fnd_rt_scene* scene, fnd_rt_scene_info* out_info
 int fnd_rt_scene_destroy(fnd_rt_scene* scene) {
     if (!scene) return FND_ERR_INVALID_ARG;
     fnd_rt_ctx* ctx = scene->ctx;
+    if (scene->users > 0) {
+        if (ctx) ctx->last_error = "scene is instanced by a live two-level scene";
+        return FND_ERR_INVALID_ARG;
+    }
     const int rc = Guard(ctx, [&] {
         UseDevice(ctx);
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        for (fnd_rt_scene* b : scene->blas) b->users--;
+        scene->blas.clear();
+        if (scene->d_instances) CUDA_CHECK(cudaFree(scene->d_instances));
         if (scene->d_nodes) CUDA_CHECK(cudaFree(scene->d_nodes));
         if (scene->d_tris) CUDA_CHECK(cudaFree(scene->d_tris));
         if (scene->d_tri_shade) CUDA_CHECK(cudaFree(scene->d_tri_shade));
@@ -497,10 +508,31 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
             else
                 L.hits = ctx->d_out;
         }
-        if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
-        const int variant = (any ? 1 : 0) + (stats ? 2 : 0);
-        const int grid = TraceGrid(ctx, ctx->trace_cfg, variant);
-        CUDA_CHECK(LaunchTraceOrdered(ctx, scene, L, any, stats != nullptr, ctx->trace_cfg, grid));
+        if (scene->two_level) {
+            CHECK_CODE(stats == nullptr, FND_ERR_INVALID_ARG, "trace statistics are not kept for two-level scenes");
+            RT::InstancedLaunch I{};
+            I.tlas = scene->view;
+            I.inst = static_cast<const RT::InstanceRec*>(scene->d_instances);
+            I.num_inst = scene->num_instances;
+            I.rays = L.rays;
+            I.n = n;
+            I.hits = L.hits;
+            I.occluded = L.occluded;
+            I.counter = ctx->d_counter;
+            I.status = ctx->d_status;
+            if (scene->num_instances == 0) {
+                RT::TraceLaunch E = L;  // no instances: every ray misses
+                E.scene = RT::DeviceScene{};
+                CUDA_CHECK(RT::LaunchTraceConfigured(E, any, false, ctx->trace_cfg, 1, ctx->stream));
+            } else {
+                CUDA_CHECK(RT::LaunchInstanced(I, any, ctx->sm_count, ctx->stream));
+            }
+        } else {
+            if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+            const int variant = (any ? 1 : 0) + (stats ? 2 : 0);
+            const int grid = TraceGrid(ctx, ctx->trace_cfg, variant);
+            CUDA_CHECK(LaunchTraceOrdered(ctx, scene, L, any, stats != nullptr, ctx->trace_cfg, grid));
+        }
         if (stats) {
             unsigned long long h[2] = {0, 0};
             CUDA_CHECK(cudaMemcpyAsync(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));

@@ -85,6 +85,13 @@ struct fnd_rt_scene {
     uint32_t num_materials = 0;
     void* d_lights = nullptr;
     uint32_t num_lights = 0;
+    // two-level scenes (fnd_rt_instances_upload): d_nodes / d_tris hold the
+    // top level over the instances' world boxes
+    bool two_level = false;
+    void* d_instances = nullptr;  // RT::InstanceRec[num_instances]
+    uint32_t num_instances = 0;
+    std::vector<fnd_rt_scene*> blas;  // the bottom levels (each counts this scene in `users`)
+    int users = 0;                    // two-level scenes that instance this one
 };
 
 namespace Foundation {

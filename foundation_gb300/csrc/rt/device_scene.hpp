@@ -24,5 +24,16 @@ struct DeviceScene {
     uint32_t num_tris;
 };
 
+// One instance of a two-level scene (104 bytes): its bottom-level scene, the
+// world-to-object transform (row-major 3x4, FP32 rounding of the FP64
+// inverse of the instance transform) and the hit id of its triangle 0.
+struct InstanceRec {
+    DeviceScene blas;
+    float inv[12];
+    uint32_t prim_offset;
+    uint32_t pad[3];
+};
+static_assert(sizeof(InstanceRec) == 104, "instance record layout");
+
 }  // namespace RT
 }  // namespace Foundation

@@ -279,5 +279,99 @@ __device__ __forceinline__ bool trace_single(const DeviceScene& sc, const RaySta
     return best_p != FND_INVALID_ID;
 }
 
+// World ray -> object space of an instance: o' = inv * (o, 1), d' = inv * (d, 0),
+// each component summed left to right with round-to-nearest operations (the
+// oracle evaluates the same expression); t is the same parameter in both
+// spaces, so tmin / tmax carry over.
+__device__ __forceinline__ void instance_ray(const float* inv, float4 r0, float4 r1, float4& o0, float4& o1) {
+    float o[3], d[3];
+    for (int i = 0; i < 3; ++i) {
+        const float* m = inv + 4 * i;
+        o[i] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], r0.x), __fmul_rn(m[1], r0.y)), __fmul_rn(m[2], r0.z)), m[3]);
+        d[i] = __fadd_rn(__fadd_rn(__fmul_rn(m[0], r1.x), __fmul_rn(m[1], r1.y)), __fmul_rn(m[2], r1.z));
+    }
+    o0 = make_float4(o[0], o[1], o[2], r0.w);
+    o1 = make_float4(d[0], d[1], d[2], r1.w);
+}
+
+// Two-level traversal: the top-level tree's leaves are instances (the plane
+// record's index word holds the instance id); each instance's bottom level
+// is traversed in object space with trace_single. Ties across instances
+// break by the global id (prim_offset + bottom-level id), as within a scene.
+template <bool kAny>
+__device__ __forceinline__ bool trace_two_level(const DeviceScene& tlas, const InstanceRec* __restrict__ inst,
+                                                uint32_t num_inst, float4 r0, float4 r1, float& best_t,
+                                                uint32_t& best_p, uint32_t* status) {
+    best_p = FND_INVALID_ID;
+    if (tlas.num_nodes == 0) return false;
+    const RayState r = setup_ray(r0, r1);
+    uint2 stack[kMaxStack];
+    int sp = 0;
+    uint32_t ng_base = 0, ng_group = (1u << 8) | (1u << r.oct), tg_base = 0, tg_mask = 0;
+    for (;;) {
+        if (ng_group & 0xFFu) {
+            const uint32_t b = (uint32_t)__ffs(ng_group & 0xFFu) - 1u;
+            ng_group &= ~(1u << b);
+            const uint32_t slot = b ^ r.oct;
+            const uint32_t child = ng_base + (uint32_t)__popc((ng_group >> 8) & ((1u << slot) - 1u));
+            if (ng_group & 0xFFu) {
+                if (sp >= kMaxStack) {
+                    atomicOr(status, kStatusStackOverflow);
+                    break;
+                }
+                stack[sp++] = make_uint2(ng_base, ng_group);
+            }
+            if (child >= tlas.num_nodes) {
+                atomicOr(status, kStatusBadIndex);
+                break;
+            }
+            const NodeHits h = intersect_node(r, tlas.nodes, child, best_t);
+            ng_base = h.child_base;
+            ng_group = h.group;
+            tg_base = h.tri_base;
+            tg_mask = h.tris;
+            if (tg_mask && (uint64_t)tg_base + (uint64_t)(32 - __clz(tg_mask)) > tlas.num_tris) {
+                atomicOr(status, kStatusBadIndex);
+                break;
+            }
+        }
+        while (tg_mask) {
+            const uint32_t k = (uint32_t)__ffs(tg_mask) - 1u;
+            tg_mask &= tg_mask - 1u;
+            const uint32_t id = __float_as_uint(__ldg(tlas.v0 + tg_base + k).w);
+            if (id >= num_inst) {
+                atomicOr(status, kStatusBadIndex);
+                continue;
+            }
+            const InstanceRec& I = inst[id];
+            float inv[12];
+            for (int q = 0; q < 12; ++q) inv[q] = __ldg(I.inv + q);
+            float4 o0, o1;
+            instance_ray(inv, r0, r1, o0, o1);
+            const DeviceScene blas = I.blas;
+            float t = best_t;
+            uint32_t p;
+            if (trace_single<kAny>(blas, setup_ray(o0, o1), t, p, status)) {
+                const uint32_t gid = __ldg(&I.prim_offset) + p;
+                if (kAny) {
+                    best_t = t;
+                    best_p = gid;
+                    return true;
+                }
+                if (best_p == FND_INVALID_ID || t < best_t || (t == best_t && gid < best_p)) {
+                    best_t = t;
+                    best_p = gid;
+                }
+            }
+        }
+        if (ng_group & 0xFFu) continue;
+        if (sp == 0) break;
+        const uint2 e = stack[--sp];
+        ng_base = e.x;
+        ng_group = e.y;
+    }
+    return best_p != FND_INVALID_ID;
+}
+
 }  // namespace RT
 }  // namespace Foundation

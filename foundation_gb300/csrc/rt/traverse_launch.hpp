@@ -60,6 +60,20 @@ struct BatchLaunch {
     uint32_t postpone_min;
 };
 
+// Rays against a two-level scene (instances.cu).
+struct InstancedLaunch {
+    DeviceScene tlas;            // leaves' index words hold instance ids
+    const InstanceRec* inst;
+    uint32_t num_inst;
+    const float4* rays;
+    uint32_t n;
+    void* hits;                  // fnd_hit[n] (closest)
+    uint8_t* occluded;           // uint8[n]   (any)
+    uint32_t* counter;
+    uint32_t* status;
+};
+cudaError_t LaunchInstanced(const InstancedLaunch& L, bool any, int sm_count, cudaStream_t stream);
+
 // variant: 0 closest, 1 any, 2 closest+stats, 3 any+stats, 4 batch
 cudaError_t TraceOccupancy(int variant, int* blocks_per_sm);
 cudaError_t TraceOccupancyFor(const TraceConfig& c, int variant, int* blocks_per_sm);

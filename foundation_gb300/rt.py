@@ -63,7 +63,8 @@ class _Desc(C.Structure):
 
 class _BvhDesc(C.Structure):
     _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("build_threads", C.c_uint32),
-                ("flags", C.c_uint32), ("traversal_cost", C.c_float), ("split_budget", C.c_float)]
+                ("flags", C.c_uint32), ("traversal_cost", C.c_float), ("split_budget", C.c_float),
+                ("margin_scale", C.c_float)]
 
 
 class SceneInfo(C.Structure):
@@ -180,6 +181,7 @@ SIGNATURES = {
     "fnd_rt_render_stats_get": (_I32, [_P, _P]),
     "fnd_rt_tonemap": (_I32, [_P, _P, _U32, _U32, _I32, C.c_float, _U32, _P, _I32]),
     "fnd_rt_raster_uniforms": (_I32, [C.c_float, C.c_float, _P, _P, _P]),
+    "fnd_rt_instances_upload": (_I32, [_P, _P, _U32, _P]),
     "fnd_rt_raster_draw": (_I32, [_P, _P, _P, _U32, _P, _U32, _P, _U32, _U32, _P, _I32]),
     "fnd_rt_set_trace_config": (_I32, [_P, _P]),
     "fnd_rt_get_trace_config": (_I32, [_P, _P]),
@@ -265,7 +267,8 @@ class Context:
     def close(self):
         """Destroys the scenes still open on this context, then the context."""
         if self._h is not None:
-            for sc in list(self._scenes):
+            # two-level scenes first: they hold their bottom levels
+            for sc in sorted(self._scenes, key=lambda x: not getattr(x, "two_level", False)):
                 sc.close()
             rc = load().fnd_rt_destroy(self._h)
             if rc == -1:  # refused (scenes still alive): the context is intact
@@ -279,11 +282,15 @@ class Context:
     def __exit__(self, *a):
         self.close()
 
+    def instances(self, instances) -> "InstanceScene":
+        """Two-level scene: instances = [(scene, transform (3, 4) object->world, prim_offset)]."""
+        return InstanceScene(self, instances)
+
     def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0,
                spatial_splits: bool = False, traversal_cost: float = 0.0, gpu_build: bool = False,
-               split_budget: float = 0.0) -> "Scene":
+               split_budget: float = 0.0, margin_scale: float = 0.0) -> "Scene":
         return Scene(self, verts, idx, bins, max_leaf, threads, spatial_splits, traversal_cost, gpu_build,
-                     split_budget)
+                     split_budget, margin_scale)
 
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
@@ -430,13 +437,13 @@ class Context:
 
 class Scene:
     def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0, spatial_splits=False,
-                 traversal_cost=0.0, gpu_build=False, split_budget=0.0):
+                 traversal_cost=0.0, gpu_build=False, split_budget=0.0, margin_scale=0.0):
         self._h = None
         self.ctx = ctx
         v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
         flags = (BVH_SPATIAL_SPLITS if spatial_splits else 0) | (BVH_GPU_BUILD if gpu_build else 0)
-        bd = _BvhDesc(bins, max_leaf, threads, flags, traversal_cost, split_budget)
+        bd = _BvhDesc(bins, max_leaf, threads, flags, traversal_cost, split_budget, margin_scale)
         h = C.c_void_p()
         _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),
                ctx.handle)
@@ -531,6 +538,31 @@ class PinnedBuffer:
         if getattr(self, "_p", None):
             load().fnd_rt_host_free(self._p)
             self._p = None
+
+
+class _Instance(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("transform", C.c_float * 12), ("prim_offset", C.c_uint32)]
+
+
+class InstanceScene(Scene):
+    """Instances of uploaded scenes under a top-level tree (fnd_rt_instances_upload).
+    Traced with closest() / any(); hit ids are prim_offset + bottom-level ids."""
+
+    two_level = True
+
+    def __init__(self, ctx: Context, instances):
+        self.ctx = ctx
+        self._h = None
+        arr = (_Instance * max(1, len(instances)))()
+        self._blas = []
+        for i, (scene, m, off) in enumerate(instances):
+            m = np.asarray(m, np.float32).reshape(3, 4)
+            arr[i] = _Instance(scene.handle.value, (C.c_float * 12)(*m.ravel()), int(off))
+            self._blas.append(scene)
+        h = C.c_void_p()
+        _check(load().fnd_rt_instances_upload(ctx.handle, arr, len(instances), C.byref(h)), ctx.handle)
+        self._h = h
+        ctx._scenes.add(self)
 
 
 class Batch:

@@ -91,6 +91,9 @@ typedef struct fnd_rt_bvh_desc {
                                test, (0, 64]; 0: default 1 (the reference tree) */
     float split_budget;     /* FND_BVH_SPATIAL_SPLITS: references the splits may add,
                                per triangle, [0, 4]; 0: default 2 */
+    float margin_scale;     /* box inflation relative to the default (2^-16 of the scene
+                               size), [1, 2^16]; 0: 1. A scene instanced at a scale far below
+                               the world's needs more (fnd_rt_instances_upload checks it) */
 } fnd_rt_bvh_desc;
 
 /* Spatial splits (Stich et al. 2009): references of triangles that straddle
@@ -346,6 +349,31 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
 
 /* Counters of the last fnd_rt_render call (synchronises the stream). */
 int fnd_rt_render_stats_get(fnd_rt_ctx* ctx, fnd_render_stats* out);
+
+/* ---- instancing -------------------------------------------------------------
+ * A two-level scene: instances of uploaded triangle scenes (bottom levels)
+ * placed by affine transforms, under a top-level tree over their world
+ * boxes. Traced with fnd_rt_trace_closest / fnd_rt_trace_any like any scene:
+ * a hit reports prim = prim_offset of the instance + the bottom-level
+ * triangle index, and t, the ray parameter (the same in world and object
+ * space). Each instance's bottom level is intersected with the ray mapped by
+ * the inverse transform (computed in FP64, rounded to FP32): o' = Minv (o, 1),
+ * d' = Minv (d, 0), sums left to right. Ties break by the reported id.
+ * A bottom level must stay alive while instanced, and its box margin must
+ * cover the object-space ray origins its instances produce: an instance
+ * scaled far below the world needs the bottom level uploaded with a larger
+ * margin_scale (the call fails with FND_ERR_INVALID_SCENE naming the value).
+ * Two-level scenes are traced only: not rendered, batched, tuned or traced
+ * through the no-allocation entry point. Reference counterpart: none (the
+ * reference draws one hard-coded quad). */
+typedef struct fnd_rt_instance {
+    const fnd_rt_scene* scene;  /* bottom level: a triangle scene of the same context */
+    float transform[12];        /* object -> world, row-major 3x4: x' = M (x, y, z, 1) */
+    uint32_t prim_offset;       /* hit id of the instance's triangle 0 */
+} fnd_rt_instance;
+
+int fnd_rt_instances_upload(fnd_rt_ctx* ctx, const fnd_rt_instance* instances, uint32_t n,
+                            fnd_rt_scene** out_scene);
 
 /* ---- image output ---------------------------------------------------------
  * Linear radiance (width*height RGB floats, row-major from the top row, the

@@ -267,3 +267,41 @@ def raster_draw(width: int, height: int, model, view, proj, texture, verts, indi
     f(width, height, ptr(m), ptr(v), ptr(p), ptr(cl), 1 if cull_back else 0, ptr(vt), len(vt), ptr(ix), len(ix),
       ptr(tex), tex.shape[1], tex.shape[0], ptr(out))
     return out
+
+
+# ---- two-level scenes (rt_oracle.cpp orc_instances_trace) ---------------------
+def instances_trace(levels, instances, rays, any_hit: bool = False, threads: int = 0):
+    """levels: [(verts (nv, 3) float32, idx (nt, 3) uint32)]; instances:
+    [(level index, transform (3, 4) object->world, prim_offset)]. Returns the
+    closest-hit records (prim, t) or the occlusion flags, brute force."""
+    L = lib()
+    f = L.orc_instances_trace
+    f.restype = None
+    P = C.c_void_p
+    f.argtypes = [P, P, P, P, P, P, P, C.c_uint32, P, C.c_uint64, P, P, C.c_int, C.c_uint32]
+    verts, idx, base, count, vb = [], [], [], [], 0
+    tb = 0
+    for v, ix in levels:
+        v = np.asarray(v, np.float32).reshape(-1, 3)
+        ix = np.asarray(ix, np.uint32).reshape(-1, 3)
+        verts.append(v)
+        idx.append(ix + np.uint32(vb))
+        base.append(tb)
+        count.append(len(ix))
+        vb += len(v)
+        tb += len(ix)
+    verts = np.ascontiguousarray(np.concatenate(verts), np.float32)
+    idx = np.ascontiguousarray(np.concatenate(idx), np.uint32)
+    base = np.asarray(base, np.uint32)
+    count = np.asarray(count, np.uint32)
+    lev = np.asarray([i[0] for i in instances], np.uint32)
+    tr = np.ascontiguousarray(np.stack([np.asarray(i[1], np.float32).reshape(12) for i in instances]), np.float32)
+    off = np.asarray([i[2] for i in instances], np.uint32)
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = len(rays)
+    hits = np.zeros(n, HIT_DTYPE) if not any_hit else None
+    occ = np.zeros(n, np.uint8) if any_hit else None
+    ptr = lambda a: a.ctypes.data_as(P) if a is not None else None  # noqa: E731
+    f(ptr(verts), ptr(idx), ptr(base), ptr(count), ptr(lev), ptr(tr), ptr(off), len(instances), ptr(rays), n,
+      ptr(hits), ptr(occ), 1 if any_hit else 0, threads)
+    return occ if any_hit else hits

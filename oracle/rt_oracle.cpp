@@ -466,6 +466,79 @@ void orc_brute_any(const float* verts, uint32_t nv, const uint32_t* idx, uint32_
     });
 }
 
+// Two-level scenes (fnd_rt_instances_upload): every instance's bottom level
+// brute-forced in object space. The ray is mapped by the FP32 rounding of
+// the FP64 inverse transform (adjugate / determinant, translation
+// -inv(A) b), o' = ((m0 ox + m1 oy) + m2 oz) + m3, d' = (m0 dx + m1 dy) + m2 dz
+// in FP32; a hit's id is the instance's prim offset plus the bottom-level
+// triangle index, ties broken by that id.
+// Geometry: bottom level k owns triangles [tri_base[k], tri_base[k] + tri_count[k])
+// of idx (indices into verts); instance i uses level inst_level[i].
+static void inverse34(const float* m, float* out) {
+    const double a00 = m[0], a01 = m[1], a02 = m[2], a10 = m[4], a11 = m[5], a12 = m[6];
+    const double a20 = m[8], a21 = m[9], a22 = m[10];
+    const double c00 = a11 * a22 - a12 * a21, c01 = a10 * a22 - a12 * a20, c02 = a10 * a21 - a11 * a20;
+    const double det = a00 * c00 - a01 * c01 + a02 * c02;
+    double inv[12];
+    inv[0] = c00 / det;
+    inv[1] = (a02 * a21 - a01 * a22) / det;
+    inv[2] = (a01 * a12 - a02 * a11) / det;
+    inv[4] = (a12 * a20 - a10 * a22) / det;
+    inv[5] = (a00 * a22 - a02 * a20) / det;
+    inv[6] = (a02 * a10 - a00 * a12) / det;
+    inv[8] = c02 / det;
+    inv[9] = (a01 * a20 - a00 * a21) / det;
+    inv[10] = (a00 * a11 - a01 * a10) / det;
+    for (int i = 0; i < 3; ++i)
+        inv[4 * i + 3] = -((inv[4 * i] * (double)m[3] + inv[4 * i + 1] * (double)m[7]) + inv[4 * i + 2] * (double)m[11]);
+    for (int k = 0; k < 12; ++k) out[k] = (float)inv[k];
+}
+
+static Ray instance_ray(const float* inv, const Ray& r) {
+    Ray o = r;
+    for (int i = 0; i < 3; ++i) {
+        const float* m = inv + 4 * i;
+        o.org[i] = ((m[0] * r.org[0] + m[1] * r.org[1]) + m[2] * r.org[2]) + m[3];
+        o.dir[i] = (m[0] * r.dir[0] + m[1] * r.dir[1]) + m[2] * r.dir[2];
+    }
+    return o;
+}
+
+void orc_instances_trace(const float* verts, const uint32_t* idx, const uint32_t* tri_base, const uint32_t* tri_count,
+                         const uint32_t* inst_level, const float* inst_transform, const uint32_t* inst_offset,
+                         uint32_t n_inst, const void* rays, uint64_t n, void* hits, uint8_t* occluded, int any,
+                         uint32_t threads) {
+    const Ray* R = (const Ray*)rays;
+    std::vector<float> invs(12 * (size_t)n_inst);
+    for (uint32_t i = 0; i < n_inst; ++i) inverse34(inst_transform + 12 * (size_t)i, &invs[12 * (size_t)i]);
+    parallel_chunks(n, threads, [&](uint32_t, uint64_t s, uint64_t e) {
+        for (uint64_t q = s; q < e; ++q) {
+            float best_t = INFINITY;
+            uint32_t best_p = kInvalid;
+            for (uint32_t i = 0; i < n_inst && !(any && best_p != kInvalid); ++i) {
+                const RayPre rp = precompute(instance_ray(&invs[12 * (size_t)i], R[q]));
+                const uint32_t lv = inst_level[i];
+                for (uint32_t t = 0; t < tri_count[lv]; ++t) {
+                    const uint32_t* f = idx + 3 * ((size_t)tri_base[lv] + t);
+                    float th;
+                    if (!intersect(rp, verts + 3 * (size_t)f[0], verts + 3 * (size_t)f[1], verts + 3 * (size_t)f[2], th))
+                        continue;
+                    const uint32_t gid = inst_offset[i] + t;
+                    if (best_p == kInvalid || closer(th, gid, best_t, best_p)) {
+                        best_t = th;
+                        best_p = gid;
+                    }
+                    if (any) break;
+                }
+            }
+            if (any)
+                occluded[q] = best_p != kInvalid ? 1 : 0;
+            else
+                ((Hit*)hits)[q] = Hit{best_p, best_p == kInvalid ? INFINITY : best_t};
+        }
+    });
+}
+
 int orc_intersect1(const float* ray8, const float* v9, float* out5) {
     Ray r;
     std::memcpy(&r, ray8, sizeof(Ray));
