@@ -245,7 +245,7 @@ def path_tracer_block(fg, torch, stream, local):
 
 
 def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
-    """Spec target workload: a 1,048,576-triangle soup in the unit cube
+    """The 1.5 Grays/s target workload: a 1,048,576-triangle soup in the unit cube
     (edge lengths log-uniform in [1e-3, 0.1], seed 2) and 8,388,608 rays with
     origins uniform in the cube and directions uniform on the sphere. Timed
     on the reference tree (binned SAH, default launch shape) and on the

@@ -18,8 +18,10 @@
 //    host at scene upload and again on every push (a failed push latches
 //    kStatusStackOverflow and ends the ray instead of writing out of bounds).
 // Block size, short-stack depth and the refill threshold are launch
-// parameters chosen by the autotuner (tune.cpp); every combination below is
-// compiled.
+// parameters chosen by the autotuner (capi/capi_batch.cpp); every
+// combination below is compiled. Two-level scenes (instances) run the same
+// loop with kTwoLevel: a lane descending into an instance pushes a return
+// marker and swaps its ray and node arrays to the instance's object space.
 #include <cfloat>
 
 #include "traverse.cuh"
@@ -113,9 +115,40 @@ struct BatchSource {
     }
 };
 
+// Rays against a two-level scene: the top level's leaves are instances.
+struct InstancedSource {
+    DeviceScene scene;  // the top level
+    const InstanceRec* inst;
+    uint32_t num_inst;
+    const float4* rays;
+    void* hits;
+    uint8_t* occluded;
+    uint32_t n;
+    struct Lane {};
+    __device__ __forceinline__ uint32_t map(uint32_t pos) const { return pos; }
+    __device__ __forceinline__ void load(uint32_t id, float4& r0, float4& r1, Lane&) const {
+        r0 = __ldg(rays + 2 * (size_t)id);
+        r1 = __ldg(rays + 2 * (size_t)id + 1);
+    }
+    __device__ __forceinline__ const DeviceScene& scene_of(const Lane&) const { return scene; }
+    __device__ __forceinline__ bool any_of(const Lane&, bool dflt) const { return dflt; }
+    __device__ __forceinline__ void store(uint32_t id, const Lane&, bool any, uint32_t prim, float t) const {
+        if (any) {
+            __stcs(occluded + id, (uint8_t)(prim != FND_INVALID_ID ? 1 : 0));
+        } else {
+            const uint2 o = make_uint2(prim, prim == FND_INVALID_ID ? 0x7F800000u : __float_as_uint(t));
+            __stcs(reinterpret_cast<uint2*>(hits) + id, o);
+        }
+    }
+};
+
+constexpr uint32_t kInstanceMarker = 0xFFFFFFFFu;  // stack entry: return to the top level
+
 // ---- the persistent traversal loop ----------------------------------------
-// kKind: 0 closest, 1 any, 2 per-lane (from the source).
-template <class Src, int kKind, bool kStats, int kShort, int kBlock>
+// kKind: 0 closest, 1 any, 2 per-lane (from the source). kTwoLevel: the
+// source is an InstancedSource (triangle leaves of the top level are
+// instances; per-lane node / triangle arrays).
+template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLevel = false>
 __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack) {
     static_assert((kShort & (kShort - 1)) == 0, "short stack size must be a power of two");
     uint2 l_stack[kMaxStack - kShort];
@@ -132,6 +165,19 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
     uint32_t ng_base = 0, ng_group = 0, tg_base = 0, tg_mask = 0;
     int sp = 0;
     unsigned long long st_nodes = 0, st_tris = 0;
+    // two-level state: the arrays the lane traverses now, and its instance
+    bool in_blas = false;
+    DeviceScene cur{};
+    uint32_t prim_off = 0;
+
+    auto push = [&](uint2 e) -> bool {
+        if (sp >= kMaxStack) return false;
+        const int s = (sp & (kShort - 1)) * kBlock + tid;
+        if (sp >= kShort) l_stack[sp - kShort] = s_stack[s];
+        s_stack[s] = e;
+        sp++;
+        return true;
+    };
 
     for (;;) {
         // ---- dynamic fetch -------------------------------------------------
@@ -159,6 +205,11 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                     tg_mask = 0;
                     sp = 0;
                     active = true;
+                    if constexpr (kTwoLevel) {
+                        in_blas = false;
+                        cur = src.scene;
+                        prim_off = 0;
+                    }
                 }
             }
         }
@@ -168,7 +219,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
         }
         if (!active) continue;
 
-        const DeviceScene& sc = src.scene_of(ln);
+        const DeviceScene& sc = kTwoLevel ? cur : src.scene_of(ln);
         bool overflow = false;
         // ---- one node --------------------------------------------------------
         if (ng_group & 0xFFu) {
@@ -176,17 +227,9 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
             ng_group &= ~(1u << b);
             const uint32_t slot = b ^ r.oct;
             const uint32_t child = ng_base + (uint32_t)__popc((ng_group >> 8) & ((1u << slot) - 1u));
-            if (ng_group & 0xFFu) {
-                if (sp >= kMaxStack) {
-                    overflow = true;
-                } else {
-                    const int s = (sp & (kShort - 1)) * kBlock + tid;
-                    if (sp >= kShort) l_stack[sp - kShort] = s_stack[s];
-                    s_stack[s] = make_uint2(ng_base, ng_group);
-                    sp++;
-                }
-            }
-            if (child < sc.num_nodes) {
+            if (ng_group & 0xFFu) overflow = !push(make_uint2(ng_base, ng_group));
+            if (overflow) {
+            } else if (child < sc.num_nodes) {
                 const NodeHits h = intersect_node(r, sc.nodes, child, best_t);
                 if (kStats) st_nodes++;
                 ng_base = h.child_base;
@@ -203,16 +246,11 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                 // triangle postponement (Ylitie et al. 2017): when only a few
                 // lanes of the warp have triangles to test, keep traversing
                 // nodes with the rest and test the triangles later
-                if (C.postpone_min) {
+                if (!kTwoLevel && C.postpone_min) {
                     const uint32_t tri_lanes = __ballot_sync(__activemask(), tg_mask != 0u);
                     if (tg_mask && (ng_group & 0xFFu) && (uint32_t)__popc(tri_lanes) < C.postpone_min &&
-                        sp < kMaxStack) {
-                        const int s = (sp & (kShort - 1)) * kBlock + tid;
-                        if (sp >= kShort) l_stack[sp - kShort] = s_stack[s];
-                        s_stack[s] = make_uint2(tg_base | kTriGroupFlag, tg_mask);
-                        sp++;
+                        push(make_uint2(tg_base | kTriGroupFlag, tg_mask)))
                         tg_mask = 0;
-                    }
                 }
             } else {
                 atomicOr(C.status, kStatusBadIndex);
@@ -221,18 +259,47 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                 sp = 0;
             }
         }
-        // ---- its triangles ---------------------------------------------------
-        while (tg_mask) {
+        // ---- its triangles (or, on the top level, its instances) ------------
+        while (tg_mask && !overflow) {
             const uint32_t k = (uint32_t)__ffs(tg_mask) - 1u;
             tg_mask &= tg_mask - 1u;
             const uint32_t ti = tg_base + k;
+            if constexpr (kTwoLevel) {
+                if (!in_blas) {
+                    const uint32_t iid = __float_as_uint(__ldg(sc.v0 + ti).w);
+                    if (iid >= src.num_inst) {
+                        atomicOr(C.status, kStatusBadIndex);
+                        continue;
+                    }
+                    // resume order after the instance: this leaf's other
+                    // instances, then the node's other children
+                    overflow = ((ng_group & 0xFFu) && !push(make_uint2(ng_base, ng_group))) ||
+                               (tg_mask && !push(make_uint2(tg_base | kTriGroupFlag, tg_mask))) ||
+                               !push(make_uint2(kInstanceMarker, 0u));
+                    if (overflow) break;
+                    const InstanceRec& I = src.inst[iid];
+                    float inv[12];
+                    for (int q = 0; q < 12; ++q) inv[q] = __ldg(I.inv + q);
+                    float4 r0, r1, o0, o1;
+                    src.load(ray_id, r0, r1, ln);
+                    instance_ray(inv, r0, r1, o0, o1);
+                    r = setup_ray(o0, o1);
+                    cur = I.blas;
+                    prim_off = __ldg(&I.prim_offset);
+                    in_blas = true;
+                    ng_base = 0;
+                    ng_group = cur.num_nodes ? (1u << 8) | (1u << r.oct) : 0u;
+                    tg_mask = 0;
+                    break;
+                }
+            }
             const float4 v0 = __ldg(sc.v0 + ti);
             const float4 v1 = __ldg(sc.v1 + ti);
             const float4 v2 = __ldg(sc.v2 + ti);
             if (kStats) st_tris++;
             float t;
             if (intersect_tri(r, v0, v1, v2, best_t, t)) {
-                const uint32_t pid = __float_as_uint(v0.w);
+                const uint32_t pid = __float_as_uint(v0.w) + (kTwoLevel ? prim_off : 0u);
                 if (any_hit) {
                     best_t = t;
                     best_p = pid;
@@ -246,13 +313,29 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
             }
         }
         // ---- next group or done ------------------------------------------
-        if ((ng_group & 0xFFu) == 0u && !overflow) {
+        if ((ng_group & 0xFFu) == 0u && tg_mask == 0u && !overflow) {
             if (sp > 0) {
                 sp--;
                 const int s = (sp & (kShort - 1)) * kBlock + tid;
                 const uint2 e = s_stack[s];
                 if (sp >= kShort) s_stack[s] = l_stack[sp - kShort];
-                if (e.x & kTriGroupFlag) {
+                bool marker = false;
+                if constexpr (kTwoLevel) {
+                    if (e.x == kInstanceMarker) {
+                        // back to the top level: the world ray again
+                        float4 r0, r1;
+                        src.load(ray_id, r0, r1, ln);
+                        r = setup_ray(r0, r1);
+                        cur = src.scene;
+                        prim_off = 0;
+                        in_blas = false;
+                        ng_group = 0;
+                        tg_mask = 0;
+                        marker = true;
+                    }
+                }
+                if (marker) {
+                } else if (e.x & kTriGroupFlag) {
                     tg_base = e.x & ~kTriGroupFlag;
                     tg_mask = e.y;
                     ng_group = 0;
@@ -311,6 +394,21 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) batch_kernel(const 
     src.n = B.total;
     const Common C{B.counter, B.status, nullptr, B.refill_min, B.postpone_min};
     persistent_trace<BatchSource, 2, false, kShort, kBlock>(src, C, s_stack);
+}
+
+template <bool kAny>
+__global__ void __launch_bounds__(128, 6) instanced_trace_kernel(const InstancedLaunch L) {
+    __shared__ uint2 s_stack[8 * 128];
+    InstancedSource src;
+    src.scene = L.tlas;
+    src.inst = L.inst;
+    src.num_inst = L.num_inst;
+    src.rays = L.rays;
+    src.hits = L.hits;
+    src.occluded = L.occluded;
+    src.n = L.n;
+    const Common C{L.counter, L.status, nullptr, 8u, 0u};
+    persistent_trace<InstancedSource, kAny ? 1 : 0, false, 8, 128, true>(src, C, s_stack);
 }
 
 __global__ void fill_miss_kernel(uint2* hits, uint8_t* occluded, uint32_t cap, const uint32_t* n_dev) {
@@ -397,6 +495,20 @@ cudaError_t LaunchTrace(const TraceLaunch& L, bool any, bool stats, int grid, cu
     TraceConfig c{};
     c.refill_min = L.refill_min;
     return LaunchTraceConfigured(L, any, stats, c, grid, stream);
+}
+
+cudaError_t LaunchInstanced(const InstancedLaunch& L, bool any, int sm_count, cudaStream_t stream) {
+    if (L.n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(L.counter, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+    const void* fn = any ? reinterpret_cast<const void*>(&instanced_trace_kernel<true>)
+                         : reinterpret_cast<const void*>(&instanced_trace_kernel<false>);
+    int blocks = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 128, 0);
+    if (e != cudaSuccess) return e;
+    InstancedLaunch arg = L;
+    void* params[] = {&arg};
+    return cudaLaunchKernel(fn, dim3(sm_count * (blocks > 0 ? blocks : 1)), dim3(128), params, 0, stream);
 }
 
 cudaError_t LaunchBatch(const BatchLaunch& B, const TraceConfig& c, int grid, cudaStream_t stream) {

@@ -232,11 +232,13 @@ def tonemap_rgba8(rgb, exposure: float = 1.0, mode: int = 2) -> np.ndarray:
     x = np.asarray(rgb, np.float32) * f(exposure)
     pos = x > 0
     x = np.where(pos, x, f(0))
-    if mode == 1:
-        x = x / (f(1) + x)
-    elif mode == 2:
-        x = (x * (f(2.51) * x + f(0.03))) / (x * (f(2.43) * x + f(0.59)) + f(0.14))
-    x = np.minimum(x, f(1)).astype(np.float32)
+    with np.errstate(invalid="ignore", over="ignore"):
+        if mode == 1:
+            x = x / (f(1) + x)
+        elif mode == 2:
+            x = (x * (f(2.51) * x + f(0.03))) / (x * (f(2.43) * x + f(0.59)) + f(0.14))
+    with np.errstate(invalid="ignore"):
+        x = np.fmin(x, f(1)).astype(np.float32)  # drops NaN (inf / inf of the curves) like fminf
     lin = f(12.92) * x
     gam = (f(1.055) * np.power(x.astype(np.float64), 1.0 / 2.4).astype(np.float32) - f(0.055)).astype(np.float32)
     s = np.where(x <= f(0.0031308), lin, gam).astype(np.float32)
