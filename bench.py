@@ -56,6 +56,9 @@ def parse_args():
     p.add_argument("--workload", default="cornell", choices=["cornell", "soup1m"],
                    help="traversal workload of the timed steps (cornell: the headline)")
     p.add_argument("--spatial-splits", action="store_true", help="build the scene with spatial splits")
+    p.add_argument("--extra", default="path_tracer,incoherent_1m_tris,time_to_relmse_1080p,batched_256_scenes,"
+                                      "large_scene_4k",
+                   help="comma-separated extra blocks to run (also: cache_frames)")
     return p.parse_args()
 
 
@@ -296,6 +299,40 @@ def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
                                "wide_nodes": info["num_wide_nodes"], "wide_depth": info["wide_depth"],
                                "build_ms": info["build_ms"]},
             "best": best, "target_mrays_s": 1500.0}
+
+
+def cache_frames_block(fg, torch, stream, local, frames: int = 8):
+    """Radiance-cache frames at 1920x1080 on the Cornell scene (65,536
+    training paths and 4 Adam steps of 16,384 per frame): `frames`
+    training-only frames, then `frames` 1-spp cache frames, each timed with
+    CUDA events (the per-frame costs behind the time-to-relMSE block)."""
+    from foundation_gb300 import scenes
+    cs = scenes.cornell_scene()
+    ctx = fg.Context(local, stream=stream.cuda_stream)
+    s = ctx.upload(cs.verts, cs.idx)
+    s.set_materials(cs.tri_material, scenes.material_records(cs))
+    s.set_lights(scenes.light_records(cs))
+    out = torch.empty(1920 * 1080 * 3, dtype=torch.float32, device="cuda")
+    ctx.cache_create(s, train_paths=65536, train_steps=4, batch=16384, learning_rate=1e-2, seed=1)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        ctx.sync()
+        return e0.elapsed_time(e1)
+
+    cam = scenes.CORNELL_CAMERA
+    train = [timed(lambda: ctx.render(s, 1920, 1080, 1, cam, seed=f, cache=True, train_only=True))
+             for f in range(frames)]
+    render = [timed(lambda: ctx.render(s, 1920, 1080, 1, cam, seed=100 + f, cache=True, accumulate=f > 0, out=out))
+              for f in range(frames)]
+    st = ctx.render_stats()
+    ctx.close()
+    return {"workload": "cornell200 1920x1080, cache frames (65,536 training paths, 4 x 16,384-sample steps)",
+            "train_only_ms": float(np.median(train)), "cache_frame_ms": float(np.median(render)),
+            "extension_rays_last": st["extension_rays"], "shadow_rays_last": st["shadow_rays"]}
 
 
 def time_to_relmse_block(fg, torch, stream, local, ref_spp: int = 8192):
@@ -631,11 +668,11 @@ def main():
                                                 "build_ms", "collapse_ms")},
         }
         if not args.no_extra:
-            line["path_tracer"] = path_tracer_block(fg, torch, stream, local)
-            line["incoherent_1m_tris"] = incoherent_1m_block(fg, torch, stream, local)
-            line["time_to_relmse_1080p"] = time_to_relmse_block(fg, torch, stream, local)
-            line["batched_256_scenes"] = batched_block(fg, torch, stream, local)
-            line["large_scene_4k"] = large_scene_block(fg, torch, stream, local)
+            blocks = {"path_tracer": path_tracer_block, "incoherent_1m_tris": incoherent_1m_block,
+                      "time_to_relmse_1080p": time_to_relmse_block, "batched_256_scenes": batched_block,
+                      "large_scene_4k": large_scene_block, "cache_frames": cache_frames_block}
+            for name in [x for x in args.extra.split(",") if x]:
+                line[name] = blocks[name](fg, torch, stream, local)
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, rays)
         print(json.dumps(line), flush=True)

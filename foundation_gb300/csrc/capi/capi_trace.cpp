@@ -62,7 +62,7 @@ cudaError_t LaunchTraceOrdered(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, RT::T
     L.order = nullptr;
     if (cfg.sort_bits && L.n > 1 && scene->view.num_nodes) {
         const size_t m = size_t(1) << cfg.sort_bits;
-        const size_t need = sizeof(uint32_t) * (2 * (size_t)L.n + m + RT::kMaxSortTiles) + 1024;
+        const size_t need = RT::RaySortScratchBytes(L.n, cfg.sort_bits) + 1024;  // + alignment of the parts
         EnsureDevice(ctx->d_sort, ctx->d_sort_cap, need);
         auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
         char* p = static_cast<char*>(ctx->d_sort);

@@ -104,9 +104,10 @@ cudaError_t LaunchTrainingPaths(const TrainPathsArgs& A, cudaStream_t s);
 
 constexpr uint32_t kQueryNextFlag = 0x80000000u;  // in PathBuffers::rng.w
 
-// Statistics counters appended after the queue counts; the tail kernel's
-// block-completion and path-fetch counters (reset by generate).
-constexpr int kCountExt0 = 0, kCountExt1 = 1, kCountShadow = 2, kStatExt = 4, kStatShadow = 6;  // 64-bit at 4, 6
+// Device counters of a wave (PathBuffers::counts): the two extension queue
+// lengths, the shadow queue length, and the tail kernel's block-completion
+// and path-fetch counters (all reset by generate).
+constexpr int kCountExt0 = 0, kCountExt1 = 1, kCountShadow = 2;
 constexpr int kCountTailDone = 8, kCountTailFetch = 9;
 
 // The tail of a wave: once the extension queue `q` (the paths that continue
