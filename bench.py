@@ -373,6 +373,7 @@ def time_to_relmse_block(fg, torch, stream, local, ref_spp: int = 8192):
             "cache": {k: cache[k] for k in ("reached", "time_ms", "frames", "spp", "relmse")},
             "speedup_cache_vs_plain": speedup, "target_speedup": 3.0,
             "cache_relmse_after_512_frames": long["relmse"],
+            "relmse_per_channel": {"plain": plain.get("relmse_rgb"), "cache": cache.get("relmse_rgb")},
             "cache_loss_last": st["loss_last"]}
 
 
@@ -521,9 +522,20 @@ def cpu_baseline(sc, rays):
     t0 = time.perf_counter()
     b.closest(rays[:n1], threads=1)
     dt1 = time.perf_counter() - t0
+    # the integrator: the FP64 oracle path tracer on a crop of the 1080p frame
+    integ = None
+    if hasattr(sc, "materials") and sc.materials is not None:
+        from foundation_gb300 import scenes
+        crop, spp = (896, 476, 128, 128), 16
+        t0 = time.perf_counter()
+        oracle.pt_render(b, sc.tri_material, scenes.material_records(sc), scenes.light_records(sc),
+                         scenes.CORNELL_CAMERA, 1920, 1080, spp, crop=crop, threads=cores)
+        dt2 = time.perf_counter() - t0
+        integ = {"paths_per_s": crop[2] * crop[3] * spp / dt2, "sample": f"{crop[2]}x{crop[3]} crop x {spp} spp of "
+                 "the 1920x1080 Cornell frame, FP64 path tracer, max depth 8", "cores": cores}
     return {"value": len(rays) / dt / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"all {len(rays)} rays of one step, scalar C++ oracle on {cores} threads",
-            "single_core_mrays_s": n1 / dt1 / 1e6, "bvh_build_s": build_s}
+            "single_core_mrays_s": n1 / dt1 / 1e6, "bvh_build_s": build_s, "integrator": integ}
 
 
 # ---------------------------------------------------------------------------

@@ -12,12 +12,18 @@ and keeps the winners in a JSON file keyed by
 where the size bucket is floor(log2(triangles)), coherence is "coherent"
 (camera rays) or "incoherent", and the kind is "closest" or "any".
 `apply` selects the entry of the nearest size bucket for a workload.
+
+The path tracer's queue widths — paths in flight per wave and the queue
+length below which the tail megakernel finishes a wave — are tuned per image
+size and mode by `tune_render` (key "render:<w>x<h>:<plain|cache>") and read
+back with `render_options`.
 """
 from __future__ import annotations
 
 import json
 import math
 import os
+import time
 
 from . import rt
 
@@ -77,3 +83,39 @@ def tune_workload(ctx: "rt.Context", table: TuneTable, scene: "rt.Scene", rays_d
                   kind: int = rt.QUERY_CLOSEST, reps: int = 3) -> dict:
     best, entries = ctx.tune(scene, rays_dev, kind=kind, reps=reps)
     return table.record(scene.info()["num_tris"], coherence, kind, best, entries)
+
+
+def render_key(width: int, height: int, cache: bool) -> str:
+    return f"render:{width}x{height}:{'cache' if cache else 'plain'}"
+
+
+def tune_render(ctx: "rt.Context", table: TuneTable, scene: "rt.Scene", width: int, height: int, camera: dict, *,
+                spp: int = 2, cache: bool = False, waves=(1 << 20, 1 << 21, 1 << 22, 1 << 23),
+                tails=(0, 1 << 16, 1 << 18, 1 << 20), reps: int = 2, **render_kw) -> dict:
+    """Times `reps` render calls of `spp` samples per pixel for every wave
+    size x tail threshold (0: automatic) and records the fastest. With
+    cache=True the calls render with the radiance cache (the cache must
+    exist)."""
+    results = []
+    for w in waves:
+        for tp in tails:
+            ctx.render(scene, width, height, spp, camera, wave_paths=w, tail_paths=tp, cache=cache, **render_kw)
+            ctx.sync()
+            best = math.inf
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                ctx.render(scene, width, height, spp, camera, wave_paths=w, tail_paths=tp, cache=cache, **render_kw)
+                ctx.sync()
+                best = min(best, (time.perf_counter() - t0) * 1e3)
+            results.append(dict(wave_paths=w, tail_paths=tp, ms=best))
+    win = min(results, key=lambda e: e["ms"])
+    default = next((e["ms"] for e in results if e["wave_paths"] == (1 << 22) and e["tail_paths"] == 0), None)
+    entry = dict(win, default_ms=default, spp=spp)
+    table.entries[render_key(width, height, cache)] = entry
+    return entry
+
+
+def render_options(table: TuneTable, width: int, height: int, cache: bool = False) -> dict:
+    """Keyword arguments for Context.render from a tuned entry ({} if none)."""
+    e = table.entries.get(render_key(width, height, cache))
+    return {} if e is None else dict(wave_paths=e["wave_paths"], tail_paths=e["tail_paths"])

@@ -19,10 +19,16 @@ import math
 
 
 def relmse(img, ref, eps: float = 1e-2) -> float:
-    import torch
     a = img.double()
     r = ref.double()
     return float(((a - r) ** 2 / (r * r + eps)).mean().item())
+
+
+def relmse_rgb(img, ref, eps: float = 1e-2) -> list:
+    """relMSE of each channel (images of interleaved RGB floats)."""
+    a = img.double().reshape(-1, 3)
+    r = ref.double().reshape(-1, 3)
+    return [float(x) for x in ((a - r) ** 2 / (r * r + eps)).mean(0).tolist()]
 
 
 def render_reference(ctx, scene, width, height, camera, spp_total: int, chunk: int = 256, seed: int = 9001, **kw):
@@ -62,6 +68,7 @@ def time_to_relmse(ctx, scene, ref, width, height, camera, *, mode: str = "plain
         r = relmse(out, ref)
         curve.append((round(t_ms, 3), spp, r))
         if r <= target:
-            return {"reached": True, "time_ms": t_ms, "frames": f + 1, "spp": spp, "relmse": r, "curve": curve[-8:]}
+            return {"reached": True, "time_ms": t_ms, "frames": f + 1, "spp": spp, "relmse": r,
+                    "relmse_rgb": relmse_rgb(out, ref), "curve": curve[-8:]}
     return {"reached": False, "time_ms": t_ms, "frames": max_frames, "spp": spp,
-            "relmse": curve[-1][2] if curve else math.nan, "curve": curve[-8:]}
+            "relmse": curve[-1][2] if curve else math.nan, "relmse_rgb": relmse_rgb(out, ref), "curve": curve[-8:]}

@@ -2,9 +2,10 @@
 //
 //  1. prep: per triangle its box, its shading normal, input validation, and
 //     the scene box / centroid box (warp-reduced float atomics);
-//  2. 30-bit Morton code of each centroid on a 1024^3 grid over the centroid
-//     box;
-//  3. stable LSD radix sort of (code, triangle) in four 8-bit passes: per
+//  2. 63-bit Morton code of each centroid on a 2^21 x 2^21 x 2^21 grid over
+//     the centroid box (dense scenes keep a spatial order far below the
+//     triangle size);
+//  3. stable LSD radix sort of (code, triangle) in eight 8-bit passes: per
 //     2,048-element warp tile a digit histogram, one exclusive scan over the
 //     digit-major counts, then a scatter in which each warp ranks its
 //     elements in order with __match_any_sync;
@@ -46,8 +47,10 @@ constexpr uint32_t kPrepBadIndex = 1u, kPrepNonFinite = 2u;
 
 struct Buffers {
     float4 *blo, *bhi;            // triangle boxes (original order)
-    uint32_t *keys, *vals;        // sorted codes / triangle ids
-    uint32_t *keys2, *vals2;      // radix-sort ping-pong
+    unsigned long long *keys;     // sorted codes
+    uint32_t* vals;               // triangle ids
+    unsigned long long* keys2;    // radix-sort ping-pong
+    uint32_t* vals2;
     uint32_t* cnt;                // digit-major tile counts
     uint32_t* sums;               // scan tile sums
     uint32_t *left, *right;       // internal node children (kLeafRef | sorted index for leaves)
@@ -151,12 +154,14 @@ __global__ void __launch_bounds__(256) prep_kernel(const float* __restrict__ ver
     }
 }
 
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-    v &= 0x3FFu;
-    v = (v | (v << 16)) & 0x030000FFu;
-    v = (v | (v << 8)) & 0x0300F00Fu;
-    v = (v | (v << 4)) & 0x030C30C3u;
-    v = (v | (v << 2)) & 0x09249249u;
+// bits 0..20 of v to positions 0, 3, 6, ... 60
+__device__ __forceinline__ unsigned long long spread3(unsigned long long v) {
+    v &= 0x1FFFFFull;
+    v = (v | (v << 32)) & 0x1F00000000FFFFull;
+    v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
     return v;
 }
 
@@ -166,11 +171,11 @@ __global__ void __launch_bounds__(256) morton_kernel(uint32_t nt, Buffers B) {
     const float4 lo = B.blo[t], hi = B.bhi[t];
     const float c[3] = {__fmul_rn(0.5f, __fadd_rn(lo.x, hi.x)), __fmul_rn(0.5f, __fadd_rn(lo.y, hi.y)),
                         __fmul_rn(0.5f, __fadd_rn(lo.z, hi.z))};
-    uint32_t q[3];
+    unsigned long long q[3];
     for (int a = 0; a < 3; ++a) {
         const float e = B.bounds[9 + a] - B.bounds[6 + a];
-        const float u = e > 0.0f ? (c[a] - B.bounds[6 + a]) * (1024.0f / e) : 0.0f;
-        q[a] = (uint32_t)fminf(fmaxf(u, 0.0f), 1023.0f);
+        const float u = e > 0.0f ? (c[a] - B.bounds[6 + a]) * (2097152.0f / e) : 0.0f;
+        q[a] = (unsigned long long)fminf(fmaxf(u, 0.0f), 2097151.0f);
     }
     B.keys[t] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
     B.vals[t] = t;
@@ -185,7 +190,7 @@ constexpr uint32_t kScanItems = 16;
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096 counters per scan tile
 constexpr int kTopThreads = 1024;                           // scans up to 4 * 1024 tile sums
 
-__global__ void __launch_bounds__(32 * kSortWarps) hist_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+__global__ void __launch_bounds__(32 * kSortWarps) hist_kernel(const unsigned long long* __restrict__ keys, uint32_t n,
                                                                uint32_t shift, uint32_t units, uint32_t* cnt) {
     __shared__ uint32_t s_cnt[kSortWarps][256];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -196,7 +201,7 @@ __global__ void __launch_bounds__(32 * kSortWarps) hist_kernel(const uint32_t* _
     const uint32_t base = u * kSortTile;
     for (uint32_t it = 0; it < kSortIters; ++it) {
         const uint32_t i = base + it * 32 + lane;
-        if (i < n) atomicAdd(&s_cnt[warp][(keys[i] >> shift) & 255u], 1u);
+        if (i < n) atomicAdd(&s_cnt[warp][(uint32_t)(keys[i] >> shift) & 255u], 1u);
     }
     __syncwarp();
     for (uint32_t d = lane; d < 256; d += 32) cnt[(size_t)d * units + u] = s_cnt[warp][d];
@@ -269,10 +274,11 @@ __global__ void __launch_bounds__(kScanThreads) scan_tile_kernel(uint32_t* a, ui
     }
 }
 
-__global__ void __launch_bounds__(32 * kSortWarps) scatter_kernel(const uint32_t* __restrict__ keys,
+__global__ void __launch_bounds__(32 * kSortWarps) scatter_kernel(const unsigned long long* __restrict__ keys,
                                                                   const uint32_t* __restrict__ vals, uint32_t n,
                                                                   uint32_t shift, uint32_t units,
-                                                                  const uint32_t* __restrict__ cnt, uint32_t* ok_,
+                                                                  const uint32_t* __restrict__ cnt,
+                                                                  unsigned long long* ok_,
                                                                   uint32_t* ov) {
     __shared__ uint32_t s_run[kSortWarps][256];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -284,8 +290,8 @@ __global__ void __launch_bounds__(32 * kSortWarps) scatter_kernel(const uint32_t
     for (uint32_t it = 0; it < kSortIters; ++it) {
         const uint32_t i = base + it * 32 + lane;
         const bool ok = i < n;
-        const uint32_t k = ok ? keys[i] : 0u;
-        const uint32_t d = ok ? ((k >> shift) & 255u) : 256u;
+        const unsigned long long k = ok ? keys[i] : 0ull;
+        const uint32_t d = ok ? ((uint32_t)(k >> shift) & 255u) : 256u;
         const uint32_t peers = __match_any_sync(kFull, d);
         const uint32_t rank = (uint32_t)__popc(peers & ((1u << lane) - 1u));
         const uint32_t start = ok ? s_run[warp][d] : 0u;
@@ -300,17 +306,17 @@ __global__ void __launch_bounds__(32 * kSortWarps) scatter_kernel(const uint32_t
 }
 
 // ---- hierarchy (Karras 2012) -------------------------------------------------
-__device__ __forceinline__ int prefix(const uint32_t* k, int n, int i, int j) {
+__device__ __forceinline__ int prefix(const unsigned long long* k, int n, int i, int j) {
     if (j < 0 || j >= n) return -1;
-    const uint32_t a = k[i], b = k[j];
-    if (a != b) return __clz(a ^ b);
-    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+    const unsigned long long a = k[i], b = k[j];
+    if (a != b) return __clzll(a ^ b);
+    return 64 + __clz((uint32_t)i ^ (uint32_t)j);
 }
 
 __global__ void __launch_bounds__(256) hierarchy_kernel(int n, Buffers B) {
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= n - 1) return;
-    const uint32_t* k = B.keys;
+    const unsigned long long* k = B.keys;
     const int d = prefix(k, n, i, i + 1) - prefix(k, n, i, i - 1) > 0 ? 1 : -1;
     const int dmin = prefix(k, n, i, i - d);
     int lmax = 2;
@@ -611,8 +617,9 @@ void RadixSort(Buffers& B, uint32_t n, cudaStream_t s) {
     const uint32_t m = 256u * units;
     const uint32_t tiles = (m + kScanTile - 1) / kScanTile;
     const uint32_t blocks = (units + kSortWarps - 1) / kSortWarps;
-    uint32_t *k_in = B.keys, *v_in = B.vals, *k_out = B.keys2, *v_out = B.vals2;
-    for (uint32_t shift = 0; shift < 32; shift += 8) {
+    unsigned long long *k_in = B.keys, *k_out = B.keys2;
+    uint32_t *v_in = B.vals, *v_out = B.vals2;
+    for (uint32_t shift = 0; shift < 64; shift += 8) {
         hist_kernel<<<blocks, 32 * kSortWarps, 0, s>>>(k_in, n, shift, units, B.cnt);
         scan_tile_sum_kernel<<<tiles, kScanThreads, 0, s>>>(B.cnt, m, B.sums);
         scan_top_kernel<<<1, kTopThreads, 0, s>>>(B.sums, tiles);
@@ -622,7 +629,7 @@ void RadixSort(Buffers& B, uint32_t n, cudaStream_t s) {
         std::swap(v_in, v_out);
     }
     Check(cudaGetLastError(), "radix sort launch");
-    // four passes: the sorted data is back in keys / vals
+    // eight passes: the sorted data is back in keys / vals
 }
 
 }  // namespace
@@ -643,9 +650,9 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     const uint32_t units = (n + kSortTile - 1) / kSortTile;
     B.blo = S.get<float4>(n);
     B.bhi = S.get<float4>(n);
-    B.keys = S.get<uint32_t>(n);
+    B.keys = S.get<unsigned long long>(n);
     B.vals = S.get<uint32_t>(n);
-    B.keys2 = S.get<uint32_t>(n);
+    B.keys2 = S.get<unsigned long long>(n);
     B.vals2 = S.get<uint32_t>(n);
     B.cnt = S.get<uint32_t>(256ull * units);
     B.sums = S.get<uint32_t>(4 * kTopThreads);

@@ -37,3 +37,26 @@ def test_tune_pass_on_gpu(built, tmp_path):
         cfg = t.apply(ctx, s.info()["num_tris"], "incoherent")
         assert ctx.trace_config() == cfg
         t.save(str(tmp_path / "t.json"))
+
+
+@pytest.mark.gpu
+def test_render_queue_widths_tuned(built, tmp_path):
+    import foundation_gb300 as fg
+    from foundation_gb300 import scenes as S
+    cs = S.cornell_scene(num_spheres=30, level=2)
+    with fg.Context(0) as ctx:
+        s = ctx.upload(cs.verts, cs.idx)
+        s.set_materials(cs.tri_material, S.material_records(cs))
+        s.set_lights(S.light_records(cs))
+        t = AT.TuneTable()
+        e = AT.tune_render(ctx, t, s, 320, 180, S.CORNELL_CAMERA, spp=4, waves=(1 << 16, 1 << 18), tails=(0, 4096),
+                           reps=1)
+        assert e["ms"] <= e["default_ms"] if e["default_ms"] else True
+        opts = AT.render_options(t, 320, 180)
+        assert opts == dict(wave_paths=e["wave_paths"], tail_paths=e["tail_paths"])
+        img = ctx.render(s, 320, 180, 4, S.CORNELL_CAMERA, **opts)
+        assert np.isfinite(img).all()
+        p = str(tmp_path / "t.json")
+        t.save(p)
+        assert AT.render_options(AT.TuneTable.load(p), 320, 180) == opts
+        assert AT.render_options(t, 64, 64) == {}
