@@ -493,6 +493,11 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
                                             out=out, **kw))
         frames += 1
     r_cache = CV.relmse(out, ref)
+    # bias floor: the same cache accumulated over 128 more frames
+    for f in range(128):
+        ctx.render(s, W, H, 1, cam, seed=5000 + f, cache=True, accumulate=True, out=out, **kw)
+    ctx.sync()
+    r_bias = CV.relmse(out, ref)
     ctx.close()
     return {"workload": f"terrain 2237^2 + 4096 level-4 icospheres ({tr.num_tris} tris), sun + sky, "
                         f"{W}x{H}, max depth 6",
@@ -506,7 +511,9 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
             "plain": {"spp": spp, "ms": plain_ms, "relmse": r_plain, "extension_rays": st["extension_rays"],
                       "shadow_rays": st["shadow_rays"],
                       "grays_s_incl_shading": (st["extension_rays"] + st["shadow_rays"]) / (plain_ms * 1e-3) / 1e9},
-            "cache_same_time": {"ms": t_cache, "warmup_frames": warmup_frames, "frames": frames, "relmse": r_cache}}
+            "cache_same_time": {"ms": t_cache, "warmup_frames": warmup_frames, "frames": frames, "relmse": r_cache},
+            "cache_relmse_after_more_frames": {"frames": frames + 128, "relmse": r_bias,
+                                               "note": "bias + reference noise floor"}}
 
 
 def cpu_baseline(sc, rays):
