@@ -582,6 +582,29 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
     }
 }
 
+__global__ void instance_shade_kernel(const float* __restrict__ inv, const uint32_t* __restrict__ prefix,
+                                      const uint32_t* __restrict__ off, const float4* const* __restrict__ blas,
+                                      uint32_t n_inst, uint32_t total, float4* __restrict__ out) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    uint32_t lo = 0, hi = n_inst;  // prefix[lo] <= g < prefix[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= g)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const uint32_t t = g - prefix[lo];
+    const float4 n = blas[lo][t];
+    const float* m = inv + 12 * (size_t)lo;
+    float w[3];
+    for (int j = 0; j < 3; ++j) w[j] = m[j] * n.x + m[4 + j] * n.y + m[8 + j] * n.z;
+    const float l = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    const float k = l > 0.0f ? 1.0f / l : 0.0f;
+    out[(size_t)off[lo] + t] = l > 0.0f ? make_float4(w[0] * k, w[1] * k, w[2] * k, 0.0f) : make_float4(0, 0, 1, 0);
+}
+
 __global__ void write_ids_kernel(float4* shade, const uint32_t* ids, uint32_t nt) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < nt) reinterpret_cast<uint32_t*>(shade + t)[3] = ids[t];
@@ -765,6 +788,15 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     Check(cudaStreamSynchronize(s), "node copy");
     out.d_nodes = exact;
     out.collapse_ms = Ms(t1);
+}
+
+cudaError_t InstanceShade(const float* d_inv, const uint32_t* d_prefix, const uint32_t* d_prim_offset,
+                          const float4* const* d_blas_shade, uint32_t n_inst, uint32_t total, float4* d_out,
+                          cudaStream_t s) {
+    if (total == 0 || n_inst == 0) return cudaSuccess;
+    instance_shade_kernel<<<(total + 255) / 256, 256, 0, s>>>(d_inv, d_prefix, d_prim_offset, d_blas_shade, n_inst,
+                                                                total, d_out);
+    return cudaGetLastError();
 }
 
 cudaError_t WriteMaterialIds(float4* d_tri_shade, const uint32_t* d_ids, uint32_t nt, cudaStream_t s) {

@@ -47,5 +47,14 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
 // tri_shade[t].w = material id bits of triangle t.
 cudaError_t WriteMaterialIds(float4* d_tri_shade, const uint32_t* d_ids, uint32_t nt, cudaStream_t s);
 
+// Shading records of a two-level scene: for instance i (prefix[i] .. prefix[i+1]
+// of the flat triangle range) and its triangle t, the world-space normal
+// normalize(inv(A)^T n) of the bottom level's normal n (inv: the instance's
+// world-to-object rows, row-major 3x4), written at prim_offset[i] + t with
+// material 0.
+cudaError_t InstanceShade(const float* d_inv, const uint32_t* d_prefix, const uint32_t* d_prim_offset,
+                          const float4* const* d_blas_shade, uint32_t n_inst, uint32_t total, float4* d_out,
+                          cudaStream_t s);
+
 }  // namespace RT
 }  // namespace Foundation

@@ -11,6 +11,7 @@
 
 #include "../bvh/bvh_build.hpp"
 #include "../bvh/collapse.hpp"
+#include "../bvh/gpu_build.hpp"
 #include "context.hpp"
 
 using namespace Foundation;
@@ -174,6 +175,50 @@ int fnd_rt_instances_upload(fnd_rt_ctx* ctx, const fnd_rt_instance* instances, u
             scene->view.v2 = reinterpret_cast<const float4*>(tris + 32ull * n);
             scene->view.num_nodes = I.num_wide_nodes;
             scene->view.num_tris = n;
+        }
+        // shading records by global id: world normals of every instance's triangles
+        {
+            std::vector<uint32_t> prefix(n + 1, 0), offs(n);
+            std::vector<float> inv(12 * (size_t)n);
+            std::vector<const float4*> shade(n);
+            for (uint32_t i = 0; i < n; ++i) {
+                prefix[i + 1] = prefix[i] + instances[i].scene->info.num_tris;
+                CHECK_CODE((uint64_t)prefix[i] + instances[i].scene->info.num_tris < (1ull << 32), FND_ERR_INVALID_ARG,
+                           "instances hold more than 2^32 triangles");
+                offs[i] = instances[i].prim_offset;
+                std::copy(recs[i].inv, recs[i].inv + 12, inv.begin() + 12 * (size_t)i);
+                shade[i] = static_cast<const float4*>(instances[i].scene->d_tri_shade);
+            }
+            const uint32_t total = prefix[n];
+            const size_t nshade = std::max<size_t>(1, scene->info.num_tris);
+            void *d_prefix = nullptr, *d_offs = nullptr, *d_inv = nullptr, *d_ptrs = nullptr;
+            try {
+                CUDA_CHECK(cudaMalloc(&scene->d_tri_shade, 16 * nshade));
+                CUDA_CHECK(cudaMemset(scene->d_tri_shade, 0, 16 * nshade));
+                if (total) {
+                    CUDA_CHECK(cudaMalloc(&d_prefix, 4ull * (n + 1)));
+                    CUDA_CHECK(cudaMalloc(&d_offs, 4ull * n));
+                    CUDA_CHECK(cudaMalloc(&d_inv, 48ull * n));
+                    CUDA_CHECK(cudaMalloc(&d_ptrs, sizeof(void*) * n));
+                    CUDA_CHECK(cudaMemcpy(d_prefix, prefix.data(), 4ull * (n + 1), cudaMemcpyHostToDevice));
+                    CUDA_CHECK(cudaMemcpy(d_offs, offs.data(), 4ull * n, cudaMemcpyHostToDevice));
+                    CUDA_CHECK(cudaMemcpy(d_inv, inv.data(), 48ull * n, cudaMemcpyHostToDevice));
+                    CUDA_CHECK(cudaMemcpy(d_ptrs, shade.data(), sizeof(void*) * n, cudaMemcpyHostToDevice));
+                    CUDA_CHECK(RT::InstanceShade(static_cast<const float*>(d_inv), static_cast<const uint32_t*>(d_prefix),
+                                                 static_cast<const uint32_t*>(d_offs),
+                                                 static_cast<const float4* const*>(d_ptrs), n, total,
+                                                 static_cast<float4*>(scene->d_tri_shade), ctx->stream));
+                    CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+                }
+                CApi::DefaultMaterial(scene.get());
+            } catch (...) {
+                for (void* p : {d_prefix, d_offs, d_inv, d_ptrs, scene->d_tri_shade, scene->d_nodes, scene->d_tris,
+                                scene->d_instances, scene->d_materials})
+                    if (p) cudaFree(p);
+                throw;
+            }
+            for (void* p : {d_prefix, d_offs, d_inv, d_ptrs})
+                if (p) cudaFree(p);
         }
         for (uint32_t i = 0; i < n; ++i) {
             fnd_rt_scene* b = const_cast<fnd_rt_scene*>(instances[i].scene);

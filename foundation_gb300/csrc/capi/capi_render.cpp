@@ -97,10 +97,34 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
                 uint32_t tail_paths) {
     const int g_closest = CApi::TraceGrid(ctx, ctx->trace_cfg, 0);
     const int g_any = CApi::TraceGrid(ctx, ctx->trace_cfg, 1);
-    if (tail_paths && ctx->tail_blocks_per_sm == 0) ctx->tail_blocks_per_sm = PT::TailBlocksPerSm();
-    const int g_tail = ctx->sm_count * std::max(1, ctx->tail_blocks_per_sm);
+    const bool two = scene->two_level;
+    int& tail_occ = ctx->tail_blocks_per_sm[two ? 1 : 0];
+    if (tail_paths && tail_occ == 0) tail_occ = PT::TailBlocksPerSm(two);
+    const int g_tail = ctx->sm_count * std::max(1, tail_occ);
     RT::TraceConfig cfg0 = ctx->trace_cfg;
     cfg0.sort_bits = 0;
+    // two-level scenes: the instanced persistent kernel on the device queues
+    auto trace = [&](RT::TraceLaunch& L, bool any, const RT::TraceConfig& cfg, int grid) -> cudaError_t {
+        if (!two) return CApi::LaunchTraceOrdered(ctx, scene, L, any, false, cfg, grid);
+        if (scene->num_instances == 0) {
+            RT::TraceLaunch E = L;
+            E.scene = RT::DeviceScene{};
+            return RT::LaunchTraceConfigured(E, any, false, cfg, 1, ctx->stream);
+        }
+        RT::InstancedLaunch I{};
+        I.tlas = scene->view;
+        I.inst = static_cast<const RT::InstanceRec*>(scene->d_instances);
+        I.num_inst = scene->num_instances;
+        I.rays = L.rays;
+        I.n = L.n;
+        I.n_dev = L.n_dev;
+        I.ray_total = L.ray_total;
+        I.hits = L.hits;
+        I.occluded = L.occluded;
+        I.counter = L.counter;
+        I.status = L.status;
+        return RT::LaunchInstanced(I, any, ctx->sm_count, ctx->stream);
+    };
     for (uint32_t b = 0; b < max_depth; ++b) {
         const int cur = (int)(b & 1u), nxt = cur ^ 1;
         RT::TraceLaunch L{};
@@ -115,7 +139,7 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
         L.refill_min = ctx->refill_min;
         // camera rays keep their (already coherent) order; later bounces and
         // shadow rays take the context's coherence ordering, if any
-        CUDA_CHECK(CApi::LaunchTraceOrdered(ctx, scene, L, false, false, b == 0 ? cfg0 : ctx->trace_cfg, g_closest));
+        CUDA_CHECK(trace(L, false, b == 0 ? cfg0 : ctx->trace_cfg, g_closest));
         CUDA_CHECK(cudaMemsetAsync(B.counts + nxt, 0, sizeof(uint32_t), ctx->stream));
         CUDA_CHECK(cudaMemsetAsync(B.counts + PT::kCountShadow, 0, sizeof(uint32_t), ctx->stream));
         CUDA_CHECK(PT::LaunchShade(B, R, S, C, cur, b, grid_shade, ctx->stream));
@@ -129,11 +153,13 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
         A.counter = ctx->d_counter;
         A.status = ctx->d_status;
         A.refill_min = ctx->refill_min;
-        CUDA_CHECK(CApi::LaunchTraceOrdered(ctx, scene, A, true, false, ctx->trace_cfg, g_any));
+        CUDA_CHECK(trace(A, true, ctx->trace_cfg, g_any));
         CUDA_CHECK(PT::LaunchResolve(B, grid_shade, ctx->stream));
         if (tail_paths && b + 1 < max_depth) {
             PT::TailArgs T{};
             T.scene = scene->view;
+            T.inst = two && scene->num_instances ? static_cast<const RT::InstanceRec*>(scene->d_instances) : nullptr;
+            T.num_inst = scene->num_instances;
             T.B = B;
             T.R = R;
             T.S = S;
@@ -165,7 +191,6 @@ int fnd_rt_scene_set_materials(fnd_rt_scene* scene, const uint32_t* tri_material
     if (!scene) return FND_ERR_INVALID_ARG;
     fnd_rt_ctx* ctx = scene->ctx;
     return Guard(ctx, [&] {
-        CHECK_CODE(!scene->two_level, FND_ERR_INVALID_ARG, "two-level scenes carry no materials");
         CHECK_CODE(nt == scene->info.num_tris, FND_ERR_INVALID_ARG, "%u material ids for %u triangles", nt,
                    scene->info.num_tris);
         CHECK(nm >= 1 && materials != nullptr && (nt == 0 || tri_material != nullptr));
@@ -218,7 +243,6 @@ int fnd_rt_scene_set_lights(fnd_rt_scene* scene, const fnd_quad_light* lights, u
     if (!scene) return FND_ERR_INVALID_ARG;
     fnd_rt_ctx* ctx = scene->ctx;
     return Guard(ctx, [&] {
-        CHECK_CODE(!scene->two_level, FND_ERR_INVALID_ARG, "two-level scenes carry no lights");
         CHECK(nl == 0 || lights != nullptr);
         std::vector<PT::DevQuadLight> dl(nl);
         for (uint32_t i = 0; i < nl; ++i) {
@@ -253,7 +277,6 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
     return Guard(ctx, [&] {
         CHECK(scene != nullptr && scene->ctx == ctx && desc != nullptr);
         CHECK(mem == FND_MEM_HOST || mem == FND_MEM_DEVICE);
-        CHECK_CODE(!scene->two_level, FND_ERR_INVALID_ARG, "two-level scenes are traced, not rendered");
         const fnd_render_desc& D = *desc;
         const bool train_only = (D.flags & FND_RENDER_TRAIN_ONLY) != 0;
         CHECK_CODE(rgb != nullptr || train_only, FND_ERR_INVALID_ARG, "rgb is NULL");
@@ -340,12 +363,12 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
         const int grid_shade = std::max(1, std::min<int>((int)((cap + 255) / 256), ctx->sm_count * 8));
         CUDA_CHECK(cudaMemsetAsync(ctx->d_render_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
         // tail megakernel threshold: by default two paths per resident tail thread
-        if (ctx->tail_blocks_per_sm == 0) ctx->tail_blocks_per_sm = PT::TailBlocksPerSm();
+        int& tail_occ = ctx->tail_blocks_per_sm[scene->two_level ? 1 : 0];
+        if (tail_occ == 0) tail_occ = PT::TailBlocksPerSm(scene->two_level);
         const uint32_t tail_paths =
             (D.flags & FND_RENDER_WAVEFRONT)
                 ? 0u
-                : (D.tail_paths ? D.tail_paths
-                                : 2u * (uint32_t)ctx->sm_count * (uint32_t)ctx->tail_blocks_per_sm * PT::kTailBlock);
+                : (D.tail_paths ? D.tail_paths : 2u * (uint32_t)ctx->sm_count * (uint32_t)tail_occ * PT::kTailBlock);
         PT::CacheIO C{};
         if (use_cache) {
             // 1) training, on the cache's own stream so it overlaps the render
@@ -360,6 +383,10 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
             CUDA_CHECK(cudaMemsetAsync(cs.counters + 1, 0, sizeof(uint32_t), ts));
             PT::TrainPathsArgs T{};
             T.scene = scene->view;
+            T.inst = scene->two_level && scene->num_instances
+                         ? static_cast<const RT::InstanceRec*>(scene->d_instances)
+                         : nullptr;
+            T.num_inst = scene->num_instances;
             T.R = R;
             T.S = S;
             T.n = train_paths;

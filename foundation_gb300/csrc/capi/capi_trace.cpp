@@ -102,6 +102,11 @@ using namespace Foundation::CApi;
 
 namespace {
 
+}  // namespace
+
+namespace Foundation {
+namespace CApi {
+
 // One grey Lambertian until fnd_rt_scene_set_materials.
 void DefaultMaterial(fnd_rt_scene* scene) {
     PT::DevMaterial m{};
@@ -112,6 +117,11 @@ void DefaultMaterial(fnd_rt_scene* scene) {
     CUDA_CHECK(cudaMemcpy(scene->d_materials, &m, sizeof(m), cudaMemcpyHostToDevice));
     scene->num_materials = 1;
 }
+
+}  // namespace CApi
+}  // namespace Foundation
+
+namespace {
 
 // FND_BVH_GPU_BUILD: the vertices and indices go to the device once and the
 // tree is built there (bvh/gpu_build.cu).
@@ -140,7 +150,7 @@ void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, ui
         scene->d_tris = go.d_tris;
         scene->d_tri_shade = go.d_tri_shade;
         go.d_nodes = go.d_tris = go.d_tri_shade = nullptr;
-        DefaultMaterial(scene);
+        CApi::DefaultMaterial(scene);
         fnd_rt_scene_info& I = scene->info;
         I.num_binary_nodes = go.num_binary_nodes;
         I.binary_depth = 0;  // not tracked by the GPU build
@@ -416,7 +426,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             CUDA_CHECK(cudaMalloc(&scene->d_tri_shade, 16ull * nt));
             CUDA_CHECK(cudaMemcpy(scene->d_tri_shade, scene->tri_shade.data(), 16ull * nt, cudaMemcpyHostToDevice));
             std::vector<float>().swap(scene->tri_shade);  // the device copy is the only one kept
-            DefaultMaterial(scene.get());
+            CApi::DefaultMaterial(scene.get());
         } catch (...) {
             if (scene->d_nodes) cudaFree(scene->d_nodes);
             if (scene->d_tris) cudaFree(scene->d_tris);

@@ -63,7 +63,7 @@ struct fnd_rt_ctx {
     float* d_rgb = nullptr;  // finalize target for host outputs
     size_t rgb_cap = 0;
     unsigned long long* d_render_stats = nullptr;  // [0] extension rays, [1] shadow rays
-    int tail_blocks_per_sm = 0;                    // occupancy of the tail megakernel (0: not yet queried)
+    int tail_blocks_per_sm[2] = {0, 0};            // occupancy of the tail megakernel, one- / two-level (0: not queried)
     void* d_sort = nullptr;                        // coherence-order scratch (rt/ray_sort.hpp)
     size_t d_sort_cap = 0;
     fnd_render_stats last_render{};
@@ -140,6 +140,9 @@ int TraceGrid(fnd_rt_ctx* ctx, const Foundation::RT::TraceConfig& cfg, int varia
 // scene box (context scratch), otherwise taken in input order.
 cudaError_t LaunchTraceOrdered(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, Foundation::RT::TraceLaunch L, bool any,
                                bool stats, const Foundation::RT::TraceConfig& cfg, int grid);
+
+// One grey Lambertian material table on a new scene (capi_trace.cpp).
+void DefaultMaterial(fnd_rt_scene* scene);
 
 // Radiance-cache session storage (capi_cache.cpp).
 void FreeCache(fnd_rt_ctx* ctx);

@@ -90,6 +90,8 @@ struct CacheIO {
 // sample with its target.
 struct TrainPathsArgs {
     RT::DeviceScene scene;
+    const RT::InstanceRec* inst;  // two-level scene: its instances (scene is the top level), else null
+    uint32_t num_inst;
     RenderParams R;
     ShadeScene S;
     uint32_t n;
@@ -120,6 +122,8 @@ constexpr int kCountTailDone = 8, kCountTailFetch = 9;
 // same hits; only the order of the frame-buffer additions differs.
 struct TailArgs {
     RT::DeviceScene scene;
+    const RT::InstanceRec* inst;  // two-level scene: its instances (scene is the top level), else null
+    uint32_t num_inst;
     PathBuffers B;
     RenderParams R;
     ShadeScene S;
@@ -131,7 +135,7 @@ struct TailArgs {
     unsigned long long* ray_stats;  // [0] extension rays, [1] shadow rays
 };
 cudaError_t LaunchTail(const TailArgs& A, int grid, cudaStream_t s);
-int TailBlocksPerSm();  // resident tail blocks per SM (occupancy)
+int TailBlocksPerSm(bool two_level);  // resident tail blocks per SM (occupancy of that variant)
 constexpr int kTailBlock = 128;
 
 cudaError_t LaunchGenerate(const PathBuffers& B, const RenderParams& R, uint64_t wave_base, uint32_t wave_n,

@@ -30,15 +30,15 @@ __device__ __forceinline__ void tl_add(float4* fb, uint32_t pixel, float3 L) {
     atomicAdd(p + 2, L.z);
 }
 
-__device__ __forceinline__ bool tl_occluded(const RT::DeviceScene& sc, float3 o, float3 d, float tmax,
-                                            uint32_t* status) {
+template <bool kTwoLevel>
+__device__ __forceinline__ bool tl_occluded(const TailArgs& A, float3 o, float3 d, float tmax) {
     float t = tmax;
     uint32_t p;
-    return RT::trace_single<true>(sc, RT::setup_ray(make_float4(o.x, o.y, o.z, 0.0f), make_float4(d.x, d.y, d.z, tmax)),
-                                  t, p, status);
+    return RT::trace_scene<true, kTwoLevel>(A.scene, A.inst, A.num_inst, make_float4(o.x, o.y, o.z, 0.0f),
+                                            make_float4(d.x, d.y, d.z, tmax), t, p, A.status);
 }
 
-template <uint32_t kMode>
+template <uint32_t kMode, bool kTwoLevel>
 __global__ void __launch_bounds__(kTailBlock) tail_kernel(const TailArgs A) {
     uint32_t* counts = A.B.counts;
     const uint32_t n = counts[A.q];
@@ -90,9 +90,8 @@ __global__ void __launch_bounds__(kTailBlock) tail_kernel(const TailArgs A) {
             VertexIn in;
             float t = __int_as_float(0x7F800000);
             uint32_t prim;
-            in.hit = RT::trace_single<false>(
-                A.scene, RT::setup_ray(make_float4(o.x, o.y, o.z, 0.0f), make_float4(d.x, d.y, d.z, t)), t, prim,
-                A.status);
+            in.hit = RT::trace_scene<false, kTwoLevel>(A.scene, A.inst, A.num_inst, make_float4(o.x, o.y, o.z, 0.0f),
+                                                       make_float4(d.x, d.y, d.z, t), t, prim, A.status);
             n_ext++;
             in.o = o;
             in.d = d;
@@ -113,12 +112,12 @@ __global__ void __launch_bounds__(kTailBlock) tail_kernel(const TailArgs A) {
             }
             if (v.shadow) {
                 n_sh++;
-                if (!tl_occluded(A.scene, v.surf_o, v.sh_d, v.sh_tmax, A.status)) tl_add(B.fb, pixel, v.sh_c);
+                if (!tl_occluded<kTwoLevel>(A, v.surf_o, v.sh_d, v.sh_tmax)) tl_add(B.fb, pixel, v.sh_c);
             }
             if (v.sun) {
                 n_sh++;
-                if (!tl_occluded(A.scene, v.surf_o, f3(A.R.sun_dir[0], A.R.sun_dir[1], A.R.sun_dir[2]),
-                                 __int_as_float(0x7F800000), A.status))
+                if (!tl_occluded<kTwoLevel>(A, v.surf_o, f3(A.R.sun_dir[0], A.R.sun_dir[1], A.R.sun_dir[2]),
+                                            __int_as_float(0x7F800000)))
                     tl_add(B.fb, pixel, v.sun_c);
             }
             if (v.next) {
@@ -153,19 +152,31 @@ __global__ void __launch_bounds__(kTailBlock) tail_kernel(const TailArgs A) {
 
 }  // namespace
 
-int TailBlocksPerSm() {
-    int b0 = 0, b1 = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, tail_kernel<0u>, kTailBlock, 0) != cudaSuccess) b0 = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, tail_kernel<1u>, kTailBlock, 0) != cudaSuccess) b1 = 1;
-    const int b = b0 < b1 ? b0 : b1;
+int TailBlocksPerSm(bool two_level) {
+    const void* fns[2] = {two_level ? (const void*)&tail_kernel<0u, true> : (const void*)&tail_kernel<0u, false>,
+                          two_level ? (const void*)&tail_kernel<1u, true> : (const void*)&tail_kernel<1u, false>};
+    int b = 1 << 30;
+    for (const void* f : fns) {
+        int k = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kTailBlock, 0) != cudaSuccess) k = 1;
+        b = k < b ? k : b;
+    }
     return b > 0 ? b : 1;
 }
 
 cudaError_t LaunchTail(const TailArgs& A, int grid, cudaStream_t s) {
-    if (A.C.mode == 1u)
-        tail_kernel<1u><<<grid, kTailBlock, 0, s>>>(A);
-    else
-        tail_kernel<0u><<<grid, kTailBlock, 0, s>>>(A);
+    const bool two = A.inst != nullptr;
+    if (A.C.mode == 1u) {
+        if (two)
+            tail_kernel<1u, true><<<grid, kTailBlock, 0, s>>>(A);
+        else
+            tail_kernel<1u, false><<<grid, kTailBlock, 0, s>>>(A);
+    } else {
+        if (two)
+            tail_kernel<0u, true><<<grid, kTailBlock, 0, s>>>(A);
+        else
+            tail_kernel<0u, false><<<grid, kTailBlock, 0, s>>>(A);
+    }
     return cudaGetLastError();
 }
 

@@ -34,10 +34,13 @@ __device__ __forceinline__ uint32_t hash32(uint32_t v) {
     return (w >> 22u) ^ w;
 }
 
-__device__ __forceinline__ RT::RayState make_ray(float3 o, float3 d, float tmax) {
-    return RT::setup_ray(make_float4(o.x, o.y, o.z, 0.0f), make_float4(d.x, d.y, d.z, tmax));
+template <bool kAny, bool kTwoLevel>
+__device__ __forceinline__ bool trace(const TrainPathsArgs& A, float3 o, float3 d, float& t, uint32_t& p) {
+    return RT::trace_scene<kAny, kTwoLevel>(A.scene, A.inst, A.num_inst, make_float4(o.x, o.y, o.z, 0.0f),
+                                            make_float4(d.x, d.y, d.z, t), t, p, A.status);
 }
 
+template <bool kTwoLevel>
 __global__ void __launch_bounds__(kBlock) training_paths_kernel(const TrainPathsArgs A) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < A.n;
@@ -66,7 +69,7 @@ __global__ void __launch_bounds__(kBlock) training_paths_kernel(const TrainPaths
             VertexIn in;
             float t = __int_as_float(0x7F800000);
             uint32_t prim;
-            in.hit = RT::trace_single<false>(A.scene, make_ray(o, d, t), t, prim, A.status);
+            in.hit = trace<false, kTwoLevel>(A, o, d, t, prim);
             in.o = o;
             in.d = d;
             in.prim = prim;
@@ -85,14 +88,12 @@ __global__ void __launch_bounds__(kBlock) training_paths_kernel(const TrainPaths
             if (v.shadow) {
                 float ts = v.sh_tmax;
                 uint32_t sp;
-                if (!RT::trace_single<true>(A.scene, make_ray(v.surf_o, v.sh_d, ts), ts, sp, A.status))
-                    total = total + v.sh_c;
+                if (!trace<true, kTwoLevel>(A, v.surf_o, v.sh_d, ts, sp)) total = total + v.sh_c;
             }
             if (v.sun) {
                 float ts = __int_as_float(0x7F800000);
                 uint32_t sp;
-                if (!RT::trace_single<true>(A.scene, make_ray(v.surf_o, ld3(R.sun_dir), ts), ts, sp, A.status))
-                    total = total + v.sun_c;
+                if (!trace<true, kTwoLevel>(A, v.surf_o, ld3(R.sun_dir), ts, sp)) total = total + v.sun_c;
             }
             if (!v.next) break;
             last_pdf = v.pdf;
@@ -135,7 +136,10 @@ __global__ void __launch_bounds__(kBlock) training_paths_kernel(const TrainPaths
 
 cudaError_t LaunchTrainingPaths(const TrainPathsArgs& A, cudaStream_t s) {
     if (A.n == 0) return cudaSuccess;
-    training_paths_kernel<<<(A.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
+    if (A.inst)
+        training_paths_kernel<true><<<(A.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
+    else
+        training_paths_kernel<false><<<(A.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
     return cudaGetLastError();
 }
 

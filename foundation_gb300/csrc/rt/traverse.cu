@@ -406,7 +406,8 @@ __global__ void __launch_bounds__(128, 6) instanced_trace_kernel(const Instanced
     src.rays = L.rays;
     src.hits = L.hits;
     src.occluded = L.occluded;
-    src.n = L.n;
+    src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
+    if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
     const Common C{L.counter, L.status, nullptr, 8u, 0u};
     persistent_trace<InstancedSource, kAny ? 1 : 0, false, 8, 128, true>(src, C, s_stack);
 }

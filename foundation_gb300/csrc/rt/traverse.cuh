@@ -373,5 +373,15 @@ __device__ __forceinline__ bool trace_two_level(const DeviceScene& tlas, const I
     return best_p != FND_INVALID_ID;
 }
 
+// One ray through a one- or two-level scene (per-thread traversal, for the
+// path-tracing megakernels). r0 / r1: the ray in the fnd_ray layout; best_t
+// starts at the ray's tmax.
+template <bool kAny, bool kTwoLevel>
+__device__ __forceinline__ bool trace_scene(const DeviceScene& sc, const InstanceRec* inst, uint32_t num_inst,
+                                            float4 r0, float4 r1, float& best_t, uint32_t& best_p, uint32_t* status) {
+    if constexpr (kTwoLevel) return trace_two_level<kAny>(sc, inst, num_inst, r0, r1, best_t, best_p, status);
+    return trace_single<kAny>(sc, setup_ray(r0, r1), best_t, best_p, status);
+}
+
 }  // namespace RT
 }  // namespace Foundation

@@ -66,7 +66,9 @@ struct InstancedLaunch {
     const InstanceRec* inst;
     uint32_t num_inst;
     const float4* rays;
-    uint32_t n;
+    uint32_t n;                  // ray count, or the capacity when n_dev is set
+    const uint32_t* n_dev;       // device-side ray count (a queue length), or null
+    unsigned long long* ray_total;  // if set, the launch adds its ray count here
     void* hits;                  // fnd_hit[n] (closest)
     uint8_t* occluded;           // uint8[n]   (any)
     uint32_t* counter;

@@ -363,9 +363,11 @@ int fnd_rt_render_stats_get(fnd_rt_ctx* ctx, fnd_render_stats* out);
  * cover the object-space ray origins its instances produce: an instance
  * scaled far below the world needs the bottom level uploaded with a larger
  * margin_scale (the call fails with FND_ERR_INVALID_SCENE naming the value).
- * Two-level scenes are traced only: not rendered, batched, tuned or traced
- * through the no-allocation entry point. Reference counterpart: none (the
- * reference draws one hard-coded quad). */
+ * Two-level scenes are traced and rendered (shading normals by global id are
+ * made at upload; fnd_rt_scene_set_materials takes one material id per global
+ * id, so instances' prim ranges should not overlap), not batched, tuned or
+ * traced through the no-allocation entry point. Reference counterpart: none
+ * (the reference draws one hard-coded quad). */
 typedef struct fnd_rt_instance {
     const fnd_rt_scene* scene;  /* bottom level: a triangle scene of the same context */
     float transform[12];        /* object -> world, row-major 3x4: x' = M (x, y, z, 1) */

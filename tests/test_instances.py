@@ -97,3 +97,68 @@ def test_instances_match_oracle_on_gpu(built):
         assert (empty.closest(rays[:100])["prim"] == fg.INVALID_ID).all()
         sc.close()
         blas[0].close()  # released with its two-level scene
+
+
+@pytest.mark.gpu
+def test_instanced_scene_renders_like_flattened(built):
+    """A Cornell box whose spheres are instances of one unit icosphere renders
+    like the same geometry flattened: same ray counts to within the few paths
+    that ulp-level hit differences send elsewhere, images within noise."""
+    import foundation_gb300 as fg
+    cs = S.cornell_scene(num_spheres=0)
+    sv, sf = S.icosphere(2)
+    rng = np.random.default_rng(2)
+    n = 24
+    centres = np.stack([rng.uniform(-0.8, 0.8, n), rng.uniform(0.2, 1.8, n), rng.uniform(-0.8, 0.8, n)], 1)
+    radii = rng.uniform(0.08, 0.2, n)
+    mats = list(cs.materials)
+    inst_mat = []
+    for k in range(n):
+        mats.append([k % 2, *rng.uniform(0.2, 0.9, 3), 0.3 if k % 2 else 1.0, 0, 0, 0])
+        inst_mat.append(len(mats) - 1)
+    mats = np.array(mats, np.float32)
+    walls_n = cs.num_tris
+    # flattened geometry and per-triangle materials in global-id order
+    flat_v = [cs.verts]
+    flat_f = [cs.idx]
+    tri_mat = [cs.tri_material]
+    base = len(cs.verts)
+    transforms = []
+    for k in range(n):
+        m = np.zeros((3, 4), np.float32)
+        m[:, :3] = np.eye(3) * radii[k]
+        m[:, 3] = centres[k]
+        transforms.append(m)
+        w = (sv.astype(np.float64) @ m[:, :3].T.astype(np.float64) + m[:, 3]).astype(np.float32)
+        flat_v.append(w)
+        flat_f.append(sf + base)
+        base += len(w)
+        tri_mat.append(np.full(len(sf), inst_mat[k], np.uint32))
+    flat_v = np.concatenate(flat_v).astype(np.float32)
+    flat_f = np.concatenate(flat_f).astype(np.uint32)
+    tri_mat = np.concatenate(tri_mat).astype(np.uint32)
+    sc_mats = S.Scene(flat_v, flat_f, tri_material=tri_mat, materials=mats, lights=cs.lights)
+    recs, lights = S.material_records(sc_mats), S.light_records(sc_mats)
+    kw = dict(seed=3)
+    with fg.Context(0) as ctx:
+        flat = ctx.upload(flat_v, flat_f)
+        flat.set_materials(tri_mat, recs)
+        flat.set_lights(lights)
+        a = ctx.render(flat, 64, 36, 256, S.CORNELL_CAMERA, **kw)
+        sa = ctx.render_stats()
+        walls = ctx.upload(cs.verts, cs.idx)
+        sphere = ctx.upload(sv.astype(np.float32), sf)
+        inst = [(walls, np.eye(3, 4, dtype=np.float32), 0)]
+        inst += [(sphere, transforms[k], walls_n + k * len(sf)) for k in range(n)]
+        two = ctx.instances(inst)
+        two.set_materials(tri_mat, recs)
+        two.set_lights(lights)
+        b = ctx.render(two, 64, 36, 256, S.CORNELL_CAMERA, **kw)
+        sb = ctx.render_stats()
+        assert abs(sb["extension_rays"] / sa["extension_rays"] - 1) < 1e-3
+        rel = float(np.mean((a - b) ** 2 / (a ** 2 + 1e-2)))
+        assert rel < 2e-3 and abs(b.mean() / a.mean() - 1) < 0.01, (rel, a.mean(), b.mean())
+        ctx.cache_create(two, train_paths=4096, train_steps=2, batch=1024, seed=1)
+        c = ctx.render(two, 64, 36, 4, S.CORNELL_CAMERA, cache=True)
+        assert np.isfinite(c).all() and c.mean() > 0
+        two.close()
