@@ -479,6 +479,7 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
     g.close()
     del rd, hd
     ref = CV.render_reference(ctx, s, W, H, cam, ref_spp, chunk=16, seed=9001, **kw)
+    inst = instanced_terrain(fg, ctx, tr, W, H, cam, kw, ref, spp, timed)
     out = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
     ctx.render(s, W, H, 1, cam, seed=5, out=out, **kw)  # warm-up (buffers)
     plain_ms = timed(lambda: ctx.render(s, W, H, spp, cam, seed=1, out=out, **kw))
@@ -513,7 +514,45 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
                       "grays_s_incl_shading": (st["extension_rays"] + st["shadow_rays"]) / (plain_ms * 1e-3) / 1e9},
             "cache_same_time": {"ms": t_cache, "warmup_frames": warmup_frames, "frames": frames, "relmse": r_cache},
             "cache_relmse_after_more_frames": {"frames": frames + 128, "relmse": r_bias,
-                                               "note": "bias + reference noise floor"}}
+                                               "note": "bias + reference noise floor"},
+            "instanced": inst}
+
+
+def instanced_terrain(fg, ctx, tr, W, H, cam, kw, ref, spp, timed):
+    """The config-5 scene as a two-level scene: the terrain (built on the GPU)
+    as one instance and the 4,096 spheres as instances of one level-4
+    icosphere; set-up time, device memory, and the plain 16-spp frame against
+    the same reference as the flattened scene."""
+    from foundation_gb300 import convergence as CV
+    from foundation_gb300 import scenes
+    import torch
+    n_inst = 4096
+    grid = 2237
+    n_terrain = (grid - 1) * (grid - 1) * 2
+    sv, sf = scenes.icosphere(4)
+    g = scenes.Pcg32Streams(3, np.arange(1 << 32, (1 << 32) + n_inst, dtype=np.uint64))
+    cx, cz = g.next_f64(), g.next_f64()
+    rad = 0.001 + g.next_f64() * 0.009
+    cy = scenes.value_noise(cx, cz, 3) + 0.5 * rad
+    t0 = time.perf_counter()
+    terrain = ctx.upload(tr.verts[:grid * grid], tr.idx[:n_terrain], gpu_build=True)
+    sphere = ctx.upload(sv.astype(np.float32), sf, margin_scale=64)
+    inst = [(terrain, np.eye(3, 4, dtype=np.float32), 0)]
+    for k in range(n_inst):
+        m = np.zeros((3, 4), np.float32)
+        m[:, :3] = np.eye(3) * rad[k]
+        m[:, 3] = (cx[k], cy[k], cz[k])
+        inst.append((sphere, m, n_terrain + k * len(sf)))
+    two = ctx.instances(inst)
+    two.set_materials(tr.tri_material, scenes.material_records(tr))
+    setup_s = time.perf_counter() - t0
+    out = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
+    ctx.render(two, W, H, 1, cam, seed=5, out=out, **kw)
+    ms = timed(lambda: ctx.render(two, W, H, spp, cam, seed=1, out=out, **kw))
+    r = CV.relmse(out, ref)
+    mem = sum(x.info()["node_bytes"] + x.info()["tri_bytes"] for x in (terrain, sphere, two))
+    two.close()
+    return {"setup_s": setup_s, "device_bvh_bytes": mem, "plain": {"spp": spp, "ms": ms, "relmse": r}}
 
 
 def cpu_baseline(sc, rays):
