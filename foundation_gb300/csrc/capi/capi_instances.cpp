@@ -12,47 +12,11 @@
 #include "../bvh/bvh_build.hpp"
 #include "../bvh/collapse.hpp"
 #include "../bvh/gpu_build.hpp"
+#include "../bvh/instances.hpp"
 #include "context.hpp"
 
 using namespace Foundation;
 using Foundation::CApi::Guard;
-
-namespace {
-
-// Row-major 3x4 inverse: adjugate over the determinant, translation
-// -inv(A) b, all in FP64 with the operation order of the oracle.
-bool Inverse(const float* m, double inv[12]) {
-    const double a00 = m[0], a01 = m[1], a02 = m[2], a10 = m[4], a11 = m[5], a12 = m[6];
-    const double a20 = m[8], a21 = m[9], a22 = m[10];
-    const double c00 = a11 * a22 - a12 * a21, c01 = a10 * a22 - a12 * a20, c02 = a10 * a21 - a11 * a20;
-    const double det = a00 * c00 - a01 * c01 + a02 * c02;
-    if (!(std::fabs(det) > 1e-30) || !std::isfinite(det)) return false;
-    inv[0] = c00 / det;
-    inv[1] = (a02 * a21 - a01 * a22) / det;
-    inv[2] = (a01 * a12 - a02 * a11) / det;
-    inv[4] = (a12 * a20 - a10 * a22) / det;
-    inv[5] = (a00 * a22 - a02 * a20) / det;
-    inv[6] = (a02 * a10 - a00 * a12) / det;
-    inv[8] = c02 / det;
-    inv[9] = (a01 * a20 - a00 * a21) / det;
-    inv[10] = (a00 * a11 - a01 * a10) / det;
-    for (int i = 0; i < 3; ++i)
-        inv[4 * i + 3] = -((inv[4 * i] * (double)m[3] + inv[4 * i + 1] * (double)m[7]) + inv[4 * i + 2] * (double)m[11]);
-    return true;
-}
-
-float Down(double x) {
-    float f = (float)x;
-    if ((double)f > x) f = std::nextafter(f, -INFINITY);
-    return f;
-}
-float Up(double x) {
-    float f = (float)x;
-    if ((double)f < x) f = std::nextafter(f, INFINITY);
-    return f;
-}
-
-}  // namespace
 
 extern "C" {
 
@@ -62,44 +26,26 @@ int fnd_rt_instances_upload(fnd_rt_ctx* ctx, const fnd_rt_instance* instances, u
         CHECK(out_scene != nullptr && (n == 0 || instances != nullptr));
         *out_scene = nullptr;
         CHECK_CODE(n <= (1u << 24), FND_ERR_INVALID_ARG, "%u instances", n);
-        std::vector<RT::InstanceRec> recs(n);
-        std::vector<float> boxes(9 * (size_t)n);
-        double wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        std::vector<std::array<double, 12>> invs(n);
+        std::vector<RT::InstanceInput> in(n);
         for (uint32_t i = 0; i < n; ++i) {
             const fnd_rt_instance& I = instances[i];
             CHECK_CODE(I.scene && I.scene->ctx == ctx, FND_ERR_INVALID_ARG, "instance %u: scene of another context", i);
             CHECK_CODE(!I.scene->two_level, FND_ERR_INVALID_ARG, "instance %u: a two-level scene cannot be instanced",
                        i);
-            for (int k = 0; k < 12; ++k)
-                CHECK_CODE(std::isfinite(I.transform[k]), FND_ERR_INVALID_ARG, "instance %u: non-finite transform", i);
-            CHECK_CODE(Inverse(I.transform, invs[i].data()), FND_ERR_INVALID_ARG, "instance %u: singular transform", i);
             CHECK_CODE((uint64_t)I.prim_offset + I.scene->info.num_tris <= 0xFFFFFFFFull, FND_ERR_INVALID_ARG,
                        "instance %u: prim_offset overflows the 32-bit id", i);
+            std::copy(I.transform, I.transform + 12, in[i].transform);
+            std::copy(I.scene->info.bounds_lo, I.scene->info.bounds_lo + 3, in[i].lo);
+            std::copy(I.scene->info.bounds_hi, I.scene->info.bounds_hi + 3, in[i].hi);
+        }
+        RT::InstanceTop top;
+        RT::BuildInstanceTop(in.data(), n, top);
+        std::vector<RT::InstanceRec> recs(n);
+        for (uint32_t i = 0; i < n; ++i) {
             RT::InstanceRec& r = recs[i];
-            r.blas = I.scene->view;
-            for (int k = 0; k < 12; ++k) r.inv[k] = (float)invs[i][k];
-            r.prim_offset = I.prim_offset;
-            // world box of the bottom level's bounds (an empty scene gets a point box)
-            const fnd_rt_scene_info& b = I.scene->info;
-            double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-            for (int c = 0; c < 8; ++c) {
-                const double p[3] = {(c & 1) ? b.bounds_hi[0] : b.bounds_lo[0], (c & 2) ? b.bounds_hi[1] : b.bounds_lo[1],
-                                     (c & 4) ? b.bounds_hi[2] : b.bounds_lo[2]};
-                for (int a = 0; a < 3; ++a) {
-                    const float* m = I.transform + 4 * a;
-                    const double w = ((double)m[0] * p[0] + (double)m[1] * p[1]) + (double)m[2] * p[2] + (double)m[3];
-                    lo[a] = std::min(lo[a], w);
-                    hi[a] = std::max(hi[a], w);
-                }
-            }
-            float* t = &boxes[9 * (size_t)i];
-            for (int a = 0; a < 3; ++a) {
-                t[a] = t[6 + a] = Down(lo[a]);
-                t[3 + a] = Up(hi[a]);
-                wlo[a] = std::min(wlo[a], lo[a]);
-                whi[a] = std::max(whi[a], hi[a]);
-            }
+            r.blas = instances[i].scene->view;
+            std::copy(&top.inv[12 * (size_t)i], &top.inv[12 * (size_t)i] + 12, r.inv);
+            r.prim_offset = instances[i].prim_offset;
         }
         // each bottom level's margin must cover object-space origins of rays
         // that start inside the world box (its margin covers origins within
@@ -107,14 +53,7 @@ int fnd_rt_instances_upload(fnd_rt_ctx* ctx, const fnd_rt_instance* instances, u
         for (uint32_t i = 0; i < n; ++i) {
             const fnd_rt_scene* sc = instances[i].scene;
             if (sc->info.num_tris == 0) continue;
-            double reach = 0.0;
-            for (int c = 0; c < 8; ++c) {
-                const double p[3] = {(c & 1) ? whi[0] : wlo[0], (c & 2) ? whi[1] : wlo[1], (c & 4) ? whi[2] : wlo[2]};
-                for (int a = 0; a < 3; ++a) {
-                    const double* m = invs[i].data() + 4 * a;
-                    reach = std::max(reach, std::fabs(((m[0] * p[0] + m[1] * p[1]) + m[2] * p[2]) + m[3]));
-                }
-            }
+            const double reach = RT::InstanceReach(&top.inv[12 * (size_t)i], top.lo, top.hi);
             const double covered = 32.0 * 65536.0 * (double)sc->info.box_margin;
             const double base = 32.0 * 65536.0 * (double)RT::SceneMargin(sc->info.bounds_lo, sc->info.bounds_hi);
             CHECK_CODE(reach <= covered, FND_ERR_INVALID_SCENE,
@@ -131,11 +70,8 @@ int fnd_rt_instances_upload(fnd_rt_ctx* ctx, const fnd_rt_instance* instances, u
                                                                               instances[i].scene->info.num_tris);
         scene->info.num_tris = (uint32_t)prims;
         if (n) {
-            RT::BuildParams bp;
-            RT::BinaryBvh bin;
-            RT::BuildBinaryBvh(boxes.data(), n, bp, bin);
-            RT::WideBvh wide;
-            RT::CollapseToWide(bin, boxes.data(), n, wide);
+            const RT::BinaryBvh& bin = top.bin;
+            const RT::WideBvh& wide = top.wide;
             CHECK_CODE(wide.depth <= (uint32_t)RT::kMaxStack / 2, FND_ERR_INVALID_SCENE, "top level too deep");
             fnd_rt_scene_info& I = scene->info;
             I.num_binary_nodes = (uint32_t)bin.nodes.size();

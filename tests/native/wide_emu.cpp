@@ -63,6 +63,7 @@ using std::signbit;
 #include "../../include/fnd_rt.h"
 #include "../../foundation_gb300/csrc/bvh/bvh_build.hpp"
 #include "../../foundation_gb300/csrc/bvh/collapse.hpp"
+#include "../../foundation_gb300/csrc/bvh/instances.hpp"
 #include "../../foundation_gb300/csrc/rt/traverse.cuh"
 
 using namespace Foundation::RT;
@@ -90,8 +91,16 @@ emu_bvh* emu_build2(const float* verts, uint32_t nv, const uint32_t* idx, uint32
     return emu_build3(verts, nv, idx, nt, threads, spatial, 1.0f);
 }
 
+emu_bvh* emu_build4(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads,
+                    int spatial, float trav_cost, float margin_scale);
+
 emu_bvh* emu_build3(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads,
                     int spatial, float trav_cost) {
+    return emu_build4(verts, nv, idx, nt, threads, spatial, trav_cost, 1.0f);
+}
+
+emu_bvh* emu_build4(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t threads,
+                    int spatial, float trav_cost, float margin_scale) {
     auto* e = new emu_bvh();
     std::vector<float> tri(9 * (size_t)nt);
     for (uint32_t t = 0; t < nt; ++t)
@@ -104,7 +113,7 @@ emu_bvh* emu_build3(const float* verts, uint32_t nv, const uint32_t* idx, uint32
         BuildBinarySbvh(tri.data(), nt, p, e->bin);
     else
         BuildBinaryBvh(tri.data(), nt, p, e->bin);
-    CollapseToWide(e->bin, tri.data(), nt, e->wide);
+    CollapseToWide(e->bin, tri.data(), nt, e->wide, margin_scale);
     e->view.nodes = reinterpret_cast<const uint4*>(e->wide.nodes.data());
     e->view.v0 = reinterpret_cast<const float4*>(e->wide.v0.data());
     e->view.v1 = reinterpret_cast<const float4*>(e->wide.v1.data());
@@ -192,6 +201,59 @@ void emu_trace(const emu_bvh* e, const float* rays, uint64_t n, uint32_t* hits, 
     stats[2] = max_sp;
     stats[3] = occupied;  // occupied child slots over the visited nodes
 }
+
+// Two-level scenes: the product's host-side top level (bvh/instances.cpp)
+// over emulated bottom levels, traced with RT::trace_two_level (the
+// per-thread two-level traversal of the path-tracing megakernels).
+struct emu_two {
+    InstanceTop top;
+    std::vector<InstanceRec> recs;
+    DeviceScene tlas{};
+};
+
+emu_two* emu_instances(const emu_bvh* const* blas, const float* transforms, const uint32_t* offsets, uint32_t n) {
+    auto* t = new emu_two();
+    std::vector<InstanceInput> in(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        std::memcpy(in[i].transform, transforms + 12 * (size_t)i, 48);
+        std::memcpy(in[i].lo, blas[i]->wide.lo, 12);
+        std::memcpy(in[i].hi, blas[i]->wide.hi, 12);
+    }
+    BuildInstanceTop(in.data(), n, t->top);
+    t->recs.resize(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        t->recs[i].blas = blas[i]->view;
+        std::memcpy(t->recs[i].inv, &t->top.inv[12 * (size_t)i], 48);
+        t->recs[i].prim_offset = offsets[i];
+    }
+    t->tlas.nodes = reinterpret_cast<const uint4*>(t->top.wide.nodes.data());
+    t->tlas.v0 = reinterpret_cast<const float4*>(t->top.wide.v0.data());
+    t->tlas.v1 = reinterpret_cast<const float4*>(t->top.wide.v1.data());
+    t->tlas.v2 = reinterpret_cast<const float4*>(t->top.wide.v2.data());
+    t->tlas.num_nodes = (uint32_t)t->top.wide.nodes.size();
+    t->tlas.num_tris = n;
+    return t;
+}
+
+void emu_instances_trace(const emu_two* t, const float* rays, uint64_t n, uint32_t* hits, int any) {
+    uint32_t status = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* rp = rays + 8 * i;
+        const float4 r0{rp[0], rp[1], rp[2], rp[3]}, r1{rp[4], rp[5], rp[6], rp[7]};
+        float best_t = r1.w;
+        uint32_t p = FND_INVALID_ID;
+        const bool h = any ? trace_two_level<true>(t->tlas, t->recs.data(), (uint32_t)t->recs.size(), r0, r1, best_t, p,
+                                                   &status)
+                           : trace_two_level<false>(t->tlas, t->recs.data(), (uint32_t)t->recs.size(), r0, r1, best_t,
+                                                    p, &status);
+        hits[2 * i] = h ? p : FND_INVALID_ID;
+        hits[2 * i + 1] = h ? __float_as_uint(best_t) : 0x7F800000u;
+    }
+}
+
+double emu_instance_reach(const emu_two* t, uint32_t i) { return InstanceReach(&t->top.inv[12 * (size_t)i], t->top.lo, t->top.hi); }
+
+void emu_instances_free(emu_two* t) { delete t; }
 
 // The same rays through RT::trace_single (the per-thread traversal of the
 // cache's training paths).

@@ -162,3 +162,46 @@ def test_instanced_scene_renders_like_flattened(built):
         c = ctx.render(two, 64, 36, 4, S.CORNELL_CAMERA, cache=True)
         assert np.isfinite(c).all() and c.mean() > 0
         two.close()
+
+
+def test_emulated_two_level_traversal_matches_oracle(built):
+    """The per-thread two-level traversal of the path-tracing megakernels
+    (traverse.cuh trace_two_level, compiled for the host) over the product's
+    host-side top level (bvh/instances.cpp): ids and t equal the oracle's."""
+    import ctypes as C
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    L = C.CDLL(os.path.join(here, "_build", "libwide_emu.so"))
+    P = C.c_void_p
+    L.emu_build4.restype = P
+    L.emu_build4.argtypes = [P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_int, C.c_float, C.c_float]
+    L.emu_instances.restype = P
+    L.emu_instances.argtypes = [P, P, P, C.c_uint32]
+    L.emu_instances_trace.argtypes = [P, P, C.c_uint64, P, C.c_int]
+    L.emu_instance_reach.restype = C.c_double
+    L.emu_instance_reach.argtypes = [P, C.c_uint32]
+    L.emu_instances_free.argtypes = [P]
+    L.emu_free.argtypes = [P]
+    ptr = lambda a: a.ctypes.data_as(P)  # noqa: E731
+    lv = levels()
+    inst = random_instances(30, 2, seed=11)
+    keep = [(np.ascontiguousarray(v, np.float32), np.ascontiguousarray(f, np.uint32)) for v, f in lv]
+    blas = [L.emu_build4(ptr(v), len(v), ptr(f), len(f), 0, 0, 1.0, 64.0) for v, f in keep]
+    arr = (P * len(inst))(*[blas[l] for l, _, _ in inst])
+    tr = np.ascontiguousarray(np.stack([m.reshape(12) for _, m, _ in inst]), np.float32)
+    off = np.asarray([o for _, _, o in inst], np.uint32)
+    two = L.emu_instances(arr, ptr(tr), ptr(off), len(inst))
+    assert max(L.emu_instance_reach(two, i) for i in range(len(inst))) < 32 * 64  # margin_scale 64 covers it
+    rays = np.ascontiguousarray(np.concatenate([S.incoherent_rays(6000, (-2, -2, -2), (2, 2, 2), seed=8),
+                                                S.camera_rays(48, 48, eye=(0, 0, 6), target=(0, 0, 0))]), np.float32)
+    out = np.zeros(2 * len(rays), np.uint32)
+    L.emu_instances_trace(two, ptr(rays), len(rays), ptr(out), 0)
+    want = O.instances_trace(lv, inst, rays)
+    assert np.array_equal(out[0::2], want["prim"])
+    assert np.array_equal(out[1::2], want["t"].view(np.uint32))
+    assert (want["prim"] != 0xFFFFFFFF).mean() > 0.05
+    L.emu_instances_trace(two, ptr(rays), len(rays), ptr(out), 1)
+    assert np.array_equal((out[0::2] != 0xFFFFFFFF).astype(np.uint8), O.instances_trace(lv, inst, rays, any_hit=True))
+    L.emu_instances_free(two)
+    for b in blas:
+        L.emu_free(b)
