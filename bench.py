@@ -220,6 +220,17 @@ def algorithmic_bytes_per_ray(sc, rays, sample=1 << 20):
     return 32.0 + 8.0 + 32.0 * nodes + 36.0 * tris, nodes, tris
 
 
+def trace_counters(scene, rd, hd):
+    """Per-ray node fetches and triangle tests of the device traversal (the
+    counting variant of the kernel, untimed) and the active-lane fraction of
+    its node and triangle phases."""
+    st = scene.closest(rd, hd, stats=True)
+    n = max(1, st["rays"])
+    return {"nodes_per_ray": st["node_fetches"] / n, "tris_per_ray": st["tri_tests"] / n,
+            "node_lane_util": st["node_fetches"] / max(1, 32 * st["warp_node_steps"]),
+            "tri_lane_util": st["tri_tests"] / max(1, 32 * st["warp_tri_steps"])}
+
+
 def path_tracer_block(fg, torch, stream, local):
     """One 1920x1080, 64-spp frame of the Cornell scene (max depth 8, RR from
     bounce 3, NEE to the area light), timed with CUDA events on the pass's
@@ -278,6 +289,7 @@ def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
     s = ctx.upload(so.verts, so.idx)
     info = s.info()
     ms_ref = time_it(s)
+    counters_ref = trace_counters(s, rd, hd)
     s.close()
     best = None
     for budget in (0.5, 1.0, 2.0):
@@ -289,7 +301,8 @@ def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
         if best is None or ms < best["kernel_ms"]:
             best = {"kernel_ms": ms, "split_budget": budget, "launch_shape": cfg, "refs": sinfo["num_refs"],
                     "wide_nodes": sinfo["num_wide_nodes"], "node_bytes": sinfo["node_bytes"],
-                    "tri_bytes": sinfo["tri_bytes"], "build_ms": sinfo["build_ms"]}
+                    "tri_bytes": sinfo["tri_bytes"], "build_ms": sinfo["build_ms"],
+                    "device_counters": trace_counters(s, rd, hd)}
         ctx.set_trace_config()
         s.close()
     ctx.close()
@@ -297,7 +310,7 @@ def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
     return {"workload": "soup 1,048,576 tris, 8,388,608 incoherent rays",
             "reference_tree": {"kernel_ms": ms_ref, "mrays_s": n_rays / (ms_ref * 1e-3) / 1e6,
                                "wide_nodes": info["num_wide_nodes"], "wide_depth": info["wide_depth"],
-                               "build_ms": info["build_ms"]},
+                               "build_ms": info["build_ms"], "device_counters": counters_ref},
             "best": best, "target_mrays_s": 1500.0}
 
 
@@ -698,6 +711,7 @@ def main():
     dev_hits = hd.cpu().numpy().view(np.uint32)
     e2e_ok = bool(np.array_equal(dev_hits[0::2], ho["prim"]))
     clocks.stop()
+    counters = trace_counters(scene, rd, hd)
 
     if rank == 0:
         peaks, peak_kind = measured_peaks()
@@ -719,7 +733,7 @@ def main():
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                          "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
                          "algorithmic_bytes_per_ray": bpr, "oracle_nodes_per_ray": nodes,
-                         "oracle_tris_per_ray": tris, "kernel_ms_avg": kern_ms,
+                         "oracle_tris_per_ray": tris, "kernel_ms_avg": kern_ms, "device_counters": counters,
                          "l2_measured": l2, "frac_of_l2": achieved / l2_peak},
             "clocks": clk,
             "scene_info": {k: info[k] for k in ("num_wide_nodes", "wide_depth", "node_bytes", "tri_bytes",

@@ -538,18 +538,20 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
                 CUDA_CHECK(RT::LaunchInstanced(I, any, ctx->sm_count, ctx->stream));
             }
         } else {
-            if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+            if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
             const int variant = (any ? 1 : 0) + (stats ? 2 : 0);
             const int grid = TraceGrid(ctx, ctx->trace_cfg, variant);
             CUDA_CHECK(LaunchTraceOrdered(ctx, scene, L, any, stats != nullptr, ctx->trace_cfg, grid));
         }
         if (stats) {
-            unsigned long long h[2] = {0, 0};
+            unsigned long long h[4] = {0, 0, 0, 0};
             CUDA_CHECK(cudaMemcpyAsync(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
             CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
             stats->rays = n;
             stats->node_fetches = h[0];
             stats->tri_tests = h[1];
+            stats->warp_node_steps = h[2];
+            stats->warp_tri_steps = h[3];
         }
         if (mem == FND_MEM_HOST) {
             if (n) CUDA_CHECK(cudaMemcpyAsync(out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));

@@ -144,12 +144,118 @@ struct InstancedSource {
 
 constexpr uint32_t kInstanceMarker = 0xFFFFFFFFu;  // stack entry: return to the top level
 
+// ---- warp-cooperative triangle tests ----------------------------------------
+// After a node step each lane holds a triangle group (base + bit mask); lane
+// by lane the groups are uneven (most lanes have none, a few have a whole
+// leaf set), so a loop over its own group leaves most of the warp idle. Here
+// the warp lays its (ray, triangle) pairs out in lane order (owner lanes in
+// ascending order, each owner's triangles in ascending order) and tests up to
+// 32 of them per round, one per lane, with the owner's ray constants taken by
+// shuffle. Each owner then merges the hits of its pairs with the sequential
+// rule (smaller t, on equal t the lower id), so the result is the one of the
+// per-lane loop. The round tests against the owner's best t at its start;
+// a later round sees the improved bound.
+// s_coop: 3 * 32 words per warp (pair entries, hit t, hit id). All 32 lanes
+// of the warp call this; lanes without a ray pass mine = false.
+template <int kKind, bool kStats>
+__device__ __forceinline__ void coop_triangles(const DeviceScene& sc, const RayState& r, bool mine_ok, bool any_hit,
+                                               uint32_t tg_base, uint32_t& tg_mask, float& best_t,
+                                               uint32_t& best_p, uint32_t& ng_group, int& sp, uint32_t* s_coop,
+                                               unsigned long long& st_tris, uint32_t& st_wtri) {
+    if (__ballot_sync(kFull, mine_ok && tg_mask != 0u) == 0u) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t* s_pair = s_coop + (threadIdx.x & ~31u) * 3u;
+    float* s_t = reinterpret_cast<float*>(s_pair + 32);
+    uint32_t* s_pid = s_pair + 64;
+    for (int round = 0; round < 33; ++round) {  // at most 32 x 32 pairs: 32 rounds
+        const uint32_t mine = mine_ok ? tg_mask : 0u;
+        const uint32_t cnt = (uint32_t)__popc(mine);
+        uint32_t inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(kFull, inc, o);
+            if (lane >= (uint32_t)o) inc += v;
+        }
+        const uint32_t total = __shfl_sync(kFull, inc, 31);
+        if (total == 0u) break;
+        const uint32_t off = inc - cnt;
+        // owners write the pairs of this round: positions off .. 31
+        uint32_t m = mine;
+        for (uint32_t p = off; p < 32u && m; ++p) {
+            const uint32_t k = (uint32_t)__ffs(m) - 1u;
+            m &= m - 1u;
+            s_pair[p] = lane << 5 | k;
+        }
+        if (mine_ok) tg_mask = m;
+        __syncwarp();
+        const uint32_t np = total < 32u ? total : 32u;
+        const uint32_t e = lane < np ? s_pair[lane] : 0u;
+        const uint32_t owner = e >> 5;
+        RayState q;
+        q.ox = __shfl_sync(kFull, r.ox, owner);
+        q.oy = __shfl_sync(kFull, r.oy, owner);
+        q.oz = __shfl_sync(kFull, r.oz, owner);
+        q.nSx = __shfl_sync(kFull, r.nSx, owner);
+        q.nSy = __shfl_sync(kFull, r.nSy, owner);
+        q.Sz = __shfl_sync(kFull, r.Sz, owner);
+        q.tmin = __shfl_sync(kFull, r.tmin, owner);
+        q.kz = __shfl_sync(kFull, r.kz, owner);
+        const float qt = __shfl_sync(kFull, best_t, owner);
+        const uint32_t ti = __shfl_sync(kFull, tg_base, owner) + (e & 31u);
+        bool hit = false;
+        float t = 0.0f;
+        uint32_t pid = 0;
+        if (lane < np) {
+            const float4 v0 = __ldg(sc.v0 + ti);
+            hit = intersect_tri(q, v0, __ldg(sc.v1 + ti), __ldg(sc.v2 + ti), qt, t);
+            pid = __float_as_uint(v0.w);
+            if (kStats) {
+                st_tris++;
+                if (lane == 0u) st_wtri++;
+            }
+        }
+        const uint32_t hm = __ballot_sync(kFull, hit);
+        if (hm) {
+            if (hit) {
+                s_t[lane] = t;
+                s_pid[lane] = pid;
+            }
+            __syncwarp();
+            if (cnt && off < 32u) {
+                const uint32_t len = (off + cnt < 32u ? off + cnt : 32u) - off;
+                uint32_t c = hm & (len == 32u ? kFull : ((1u << len) - 1u) << off);
+                while (c) {
+                    const uint32_t j = (uint32_t)__ffs(c) - 1u;
+                    c &= c - 1u;
+                    const float tj = s_t[j];
+                    const uint32_t pj = s_pid[j];
+                    if (kKind == 1 || (kKind == 2 && any_hit)) {
+                        best_t = tj;
+                        best_p = pj;
+                        tg_mask = 0;
+                        ng_group = 0;
+                        sp = 0;
+                        break;
+                    }
+                    if (best_p == FND_INVALID_ID || tj < best_t || (tj == best_t && pj < best_p)) {
+                        best_t = tj;
+                        best_p = pj;
+                    }
+                }
+            }
+        }
+        __syncwarp();  // the entries are rewritten by the next round
+    }
+}
+
 // ---- the persistent traversal loop ----------------------------------------
 // kKind: 0 closest, 1 any, 2 per-lane (from the source). kTwoLevel: the
 // source is an InstancedSource (triangle leaves of the top level are
 // instances; per-lane node / triangle arrays).
-template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLevel = false>
-__device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack) {
+template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLevel = false, bool kCoop = false>
+__device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack,
+                                                 uint32_t* s_coop = nullptr) {
+    static_assert(!(kCoop && kTwoLevel), "cooperative triangle tests need one scene per warp");
     static_assert((kShort & (kShort - 1)) == 0, "short stack size must be a power of two");
     uint2 l_stack[kMaxStack - kShort];
     const int tid = threadIdx.x;
@@ -165,6 +271,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
     uint32_t ng_base = 0, ng_group = 0, tg_base = 0, tg_mask = 0;
     int sp = 0;
     unsigned long long st_nodes = 0, st_tris = 0;
+    uint32_t st_wnode = 0, st_wtri = 0;  // warp steps, counted by the lowest active lane
     // two-level state: the arrays the lane traverses now, and its instance
     bool in_blas = false;
     DeviceScene cur{};
@@ -217,12 +324,14 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
             if (exhausted) break;
             continue;
         }
-        if (!active) continue;
+        // the cooperative triangle stage needs the whole warp: idle lanes
+        // run the iteration with empty node and triangle groups
+        if (!kCoop && !active) continue;
 
         const DeviceScene& sc = kTwoLevel ? cur : src.scene_of(ln);
         bool overflow = false;
         // ---- one node --------------------------------------------------------
-        if (ng_group & 0xFFu) {
+        if ((kCoop ? active : true) && (ng_group & 0xFFu)) {
             const uint32_t b = (uint32_t)__ffs(ng_group & 0xFFu) - 1u;
             ng_group &= ~(1u << b);
             const uint32_t slot = b ^ r.oct;
@@ -231,7 +340,10 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
             if (overflow) {
             } else if (child < sc.num_nodes) {
                 const NodeHits h = intersect_node(r, sc.nodes, child, best_t);
-                if (kStats) st_nodes++;
+                if (kStats) {
+                    st_nodes++;
+                    if (lane == (uint32_t)__ffs(__activemask()) - 1u) st_wnode++;
+                }
                 ng_base = h.child_base;
                 ng_group = h.group;
                 tg_base = h.tri_base;
@@ -246,7 +358,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                 // triangle postponement (Ylitie et al. 2017): when only a few
                 // lanes of the warp have triangles to test, keep traversing
                 // nodes with the rest and test the triangles later
-                if (!kTwoLevel && C.postpone_min) {
+                if (!kTwoLevel && !kCoop && C.postpone_min) {
                     const uint32_t tri_lanes = __ballot_sync(__activemask(), tg_mask != 0u);
                     if (tg_mask && (ng_group & 0xFFu) && (uint32_t)__popc(tri_lanes) < C.postpone_min &&
                         push(make_uint2(tg_base | kTriGroupFlag, tg_mask)))
@@ -259,8 +371,14 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                 sp = 0;
             }
         }
+        // ---- its triangles, tested by the whole warp ------------------------
+        if constexpr (kCoop) {
+            coop_triangles<kKind, kStats>(sc, r, active && !overflow, any_hit, tg_base, tg_mask, best_t, best_p,
+                                          ng_group, sp, s_coop, st_tris, st_wtri);
+            if (!active) continue;
+        }
         // ---- its triangles (or, on the top level, its instances) ------------
-        while (tg_mask && !overflow) {
+        while (!kCoop && tg_mask && !overflow) {
             const uint32_t k = (uint32_t)__ffs(tg_mask) - 1u;
             tg_mask &= tg_mask - 1u;
             const uint32_t ti = tg_base + k;
@@ -296,7 +414,10 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
             const float4 v0 = __ldg(sc.v0 + ti);
             const float4 v1 = __ldg(sc.v1 + ti);
             const float4 v2 = __ldg(sc.v2 + ti);
-            if (kStats) st_tris++;
+            if (kStats) {
+                st_tris++;
+                if (lane == (uint32_t)__ffs(__activemask()) - 1u) st_wtri++;
+            }
             float t;
             if (intersect_tri(r, v0, v1, v2, best_t, t)) {
                 const uint32_t pid = __float_as_uint(v0.w) + (kTwoLevel ? prim_off : 0u);
@@ -352,15 +473,21 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
         if (overflow) atomicOr(C.status, kStatusStackOverflow);
         src.store(ray_id, ln, any_hit, best_p, best_t);
         active = false;
+        ng_group = 0;
+        tg_mask = 0;
     }
     if (kStats) {
         for (int o = 16; o > 0; o >>= 1) {
             st_nodes += __shfl_down_sync(kFull, st_nodes, o);
             st_tris += __shfl_down_sync(kFull, st_tris, o);
+            st_wnode += __shfl_down_sync(kFull, st_wnode, o);
+            st_wtri += __shfl_down_sync(kFull, st_wtri, o);
         }
         if (lane == 0) {
             atomicAdd(C.stats + 0, st_nodes);
             atomicAdd(C.stats + 1, st_tris);
+            atomicAdd(C.stats + 2, (unsigned long long)st_wnode);
+            atomicAdd(C.stats + 3, (unsigned long long)st_wtri);
         }
     }
 }
@@ -372,6 +499,7 @@ constexpr int MinBlocks(int block) { return block == 256 ? 4 : 1152 / block; }
 template <bool kAny, bool kStats, int kShort, int kBlock>
 __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const TraceLaunch L) {
     __shared__ uint2 s_stack[kShort * kBlock];
+    __shared__ uint32_t s_coop[3 * kBlock];
     SingleSource src;
     src.scene = L.scene;
     src.rays = L.rays;
@@ -381,7 +509,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const 
     src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
     if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
     const Common C{L.counter, L.status, L.stats, L.refill_min, L.postpone_min};
-    persistent_trace<SingleSource, kAny ? 1 : 0, kStats, kShort, kBlock>(src, C, s_stack);
+    persistent_trace<SingleSource, kAny ? 1 : 0, kStats, kShort, kBlock, false, true>(src, C, s_stack, s_coop);
 }
 
 template <int kShort, int kBlock>

@@ -131,6 +131,19 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 #endif
 }
 
+// Bit 7 of each byte of w gathered into bits 0..3: the product places bits
+// 7, 15, 23 and 31 at 28..31 and its other partial products at distinct
+// lower positions, so no carry reaches the result.
+__device__ __forceinline__ uint32_t meta_leaf_bits(uint32_t w) { return ((w & 0x80808080u) * 0x00204081u) >> 28; }
+
+// Bit s of the 8-bit mask m moved to bit s ^ oct.
+__device__ __forceinline__ uint32_t xor_permute8(uint32_t m, uint32_t oct) {
+    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (oct & 4u) m = ((m & 0x0Fu) << 4) | (m >> 4);
+    return m;
+}
+
 // Tests the 8 child boxes of one compressed node against the ray.
 // Returns the hit mask of internal children in traversal order (bit i is
 // slot i ^ oct) in bits 0..7 with the node's imask in bits 8..15, and the
@@ -175,11 +188,12 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
     const float bnx = __fmaf_rd(-8388608.0f, sx, bx), bfx = __fmaf_ru(-8388608.0f, sx, bx);
     const float bny = __fmaf_rd(-8388608.0f, sy, by), bfy = __fmaf_ru(-8388608.0f, sy, by);
     const float bnz = __fmaf_rd(-8388608.0f, sz, bz), bfz = __fmaf_ru(-8388608.0f, sz, bz);
-    uint32_t hits = 0, tris = 0;
+    // the boxes alone: bit s of hitm for slot s (empty slots included; the
+    // slot kinds below mask them out)
+    uint32_t hitm = 0;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const uint32_t sel = (uint32_t)(s & 3);
-        const uint32_t meta = __byte_perm(s < 4 ? w1.z : w1.w, 0u, 0x4440u | sel);
         const float tnx = __fmaf_rd(byte_plus_2p23(s < 4 ? nx0 : nx1, sel), sx, bnx);
         const float tny = __fmaf_rd(byte_plus_2p23(s < 4 ? ny0 : ny1, sel), sy, bny);
         const float tnz = __fmaf_rd(byte_plus_2p23(s < 4 ? nz0 : nz1, sel), sz, bnz);
@@ -188,19 +202,21 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
         const float tfz = __fmaf_ru(byte_plus_2p23(s < 4 ? gz0 : gz1, sel), sz, bfz);
         const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
         const float tf = min3f(tfx, tfy, fminf(tfz, tfar));
-        if (meta != 0u && tn <= tf) {
-            if (imask & (1u << s)) {
-                hits |= 1u << ((uint32_t)s ^ r.oct);
-            } else {
-                const uint32_t cnt = ((meta >> 5) & 3u) + 1u;
-                tris |= ((1u << cnt) - 1u) << (meta & 31u);
-            }
-        }
+        hitm |= tn <= tf ? 1u << s : 0u;
+    }
+    // leaf slots: the 0x80 flag of their meta byte
+    const uint32_t leaves = meta_leaf_bits(w1.z) | meta_leaf_bits(w1.w) << 4;
+    uint32_t lh = hitm & leaves, tris = 0;
+    while (lh) {  // about one hit leaf per three nodes on incoherent rays
+        const uint32_t s = (uint32_t)__ffs(lh) - 1u;
+        lh &= lh - 1u;
+        const uint32_t meta = __byte_perm(s < 4u ? w1.z : w1.w, 0u, 0x4440u | (s & 3u));
+        tris |= ((2u << ((meta >> 5) & 3u)) - 1u) << (meta & 31u);
     }
     NodeHits out;
     out.child_base = w1.x;
     out.tri_base = w1.y;
-    out.group = (imask << 8) | hits;
+    out.group = (imask << 8) | xor_permute8(hitm & imask, r.oct);
     out.tris = tris;
     return out;
 }

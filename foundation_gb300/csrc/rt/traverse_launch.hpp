@@ -23,7 +23,8 @@ struct TraceLaunch {
     uint8_t* occluded;   // uint8[n]   (any)
     uint32_t* counter;   // work-queue counter (zeroed before each launch)
     uint32_t* status;    // latched kStatus* bits
-    unsigned long long* stats;  // [0] node fetches, [1] triangle tests (stats variants)
+    unsigned long long* stats;  // [0] node fetches, [1] triangle tests, [2] / [3] warp steps of the node /
+                                // triangle tests (stats variants)
     uint32_t refill_min;        // refill a warp once this many lanes are idle
     uint32_t postpone_min;      // triangle postponement threshold (0: off)
     const uint32_t* order;      // fetch position -> ray index (ray_sort.hpp), or null: input order

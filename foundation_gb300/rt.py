@@ -155,7 +155,8 @@ class CacheStats(C.Structure):
 
 
 class TraceStats(C.Structure):
-    _fields_ = [("rays", C.c_uint64), ("node_fetches", C.c_uint64), ("tri_tests", C.c_uint64)]
+    _fields_ = [("rays", C.c_uint64), ("node_fetches", C.c_uint64), ("tri_tests", C.c_uint64),
+                ("warp_node_steps", C.c_uint64), ("warp_tri_steps", C.c_uint64)]
 
 
 # every symbol include/fnd_rt.h declares, with (restype, argtypes)
@@ -490,7 +491,8 @@ class Scene:
             st = TraceStats()
             _check(L.fnd_rt_trace_closest_stats(self.ctx.handle, self._h, _ptr(rays), n, _ptr(out), mem,
                                                 C.byref(st)), self.ctx.handle)
-            return dict(rays=st.rays, node_fetches=st.node_fetches, tri_tests=st.tri_tests)
+            return dict(rays=st.rays, node_fetches=st.node_fetches, tri_tests=st.tri_tests,
+                        warp_node_steps=st.warp_node_steps, warp_tri_steps=st.warp_tri_steps)
         fn = L.fnd_rt_trace_any if any_hit else L.fnd_rt_trace_closest
         _check(fn(self.ctx.handle, self._h, _ptr(rays), n, _ptr(out), mem), self.ctx.handle)
         return None

@@ -191,11 +191,17 @@ int fnd_rt_trace_any(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* 
                      uint8_t* out, int mem);
 
 /* Traversal counters of the last trace call (device-side totals), for the
- * memory-roofline accounting: wide nodes fetched and triangles tested. */
+ * memory-roofline accounting: wide nodes fetched and triangles tested; and
+ * for the SIMT accounting: warp steps of the node test and of the triangle
+ * test (steps a warp executed, whatever its active lanes), so that
+ * node_fetches / (32 * warp_node_steps) is the node phase's lane
+ * utilisation and tri_tests / (32 * warp_tri_steps) the triangle phase's. */
 typedef struct fnd_rt_trace_stats {
     uint64_t rays;
     uint64_t node_fetches;
     uint64_t tri_tests;
+    uint64_t warp_node_steps;
+    uint64_t warp_tri_steps;
 } fnd_rt_trace_stats;
 
 /* Re-runs a closest-hit trace with per-ray counters enabled (slower variant of

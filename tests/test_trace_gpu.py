@@ -104,6 +104,9 @@ def test_device_pointers_and_stats(ctx):
     hh, st = sc.closest(rays, stats=True)
     assert_same(hh, ref)
     assert st["rays"] == len(rays) and st["node_fetches"] >= len(rays)
+    # a warp step covers at most 32 lanes' node fetches / triangle tests
+    assert st["node_fetches"] <= 32 * st["warp_node_steps"] and st["warp_node_steps"] <= st["node_fetches"]
+    assert st["tri_tests"] <= 32 * st["warp_tri_steps"] and st["warp_tri_steps"] <= st["tri_tests"]
     occ = torch.empty(len(rays), dtype=torch.uint8, device="cuda")
     sc.any(rd, occ)
     ctx.sync()
