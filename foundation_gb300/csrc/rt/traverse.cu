@@ -148,26 +148,57 @@ constexpr uint32_t kInstanceMarker = 0xFFFFFFFFu;  // stack entry: return to the
 // After a node step each lane holds a triangle group (base + bit mask); lane
 // by lane the groups are uneven (most lanes have none, a few have a whole
 // leaf set), so a loop over its own group leaves most of the warp idle. Here
-// the warp lays its (ray, triangle) pairs out in lane order (owner lanes in
-// ascending order, each owner's triangles in ascending order) and tests up to
-// 32 of them per round, one per lane, with the owner's ray constants taken by
-// shuffle. Each owner then merges the hits of its pairs with the sequential
-// rule (smaller t, on equal t the lower id), so the result is the one of the
-// per-lane loop. The round tests against the owner's best t at its start;
-// a later round sees the improved bound.
-// s_coop: 3 * 32 words per warp (pair entries, hit t, hit id). All 32 lanes
-// of the warp call this; lanes without a ray pass mine = false.
-template <int kKind, bool kStats>
-__device__ __forceinline__ void coop_triangles(const DeviceScene& sc, const RayState& r, bool mine_ok, bool any_hit,
-                                               uint32_t tg_base, uint32_t& tg_mask, float& best_t,
-                                               uint32_t& best_p, uint32_t& ng_group, int& sp, uint32_t* s_coop,
+// the warp lays its (ray, triangle) pairs out in lane order and tests up to
+// 32 of them per round, one per lane: a round takes the owners (lanes with a
+// group) in ascending lane order while their groups fit, each owner's
+// triangles in ascending order. A pair lane finds its owner from the mask of
+// group start positions (an OR over the warp) and its triangle as the k-th
+// set bit of the owner's mask; the owner's ray constants come from its slot
+// in shared memory, written when the ray was fetched. Each owner merges the
+// hits of its pairs with the sequential rule (smaller t, on equal t the lower
+// id), so the result is the one of a loop over its own group. A round tests
+// against the owner's best t at its start; a later round sees the improved
+// bound.
+
+// Position of the k-th set bit (k from 0) of m; k < popc(m).
+__device__ __forceinline__ uint32_t select_bit(uint32_t m, uint32_t k) {
+    uint32_t pos = 0, c;
+    c = (uint32_t)__popc(m & 0xFFFFu);
+    if (k >= c) { k -= c; m >>= 16; pos += 16; }
+    c = (uint32_t)__popc(m & 0xFFu);
+    if (k >= c) { k -= c; m >>= 8; pos += 8; }
+    c = (uint32_t)__popc(m & 0xFu);
+    if (k >= c) { k -= c; m >>= 4; pos += 4; }
+    c = (uint32_t)__popc(m & 0x3u);
+    if (k >= c) { k -= c; m >>= 2; pos += 2; }
+    return pos + (k >= (m & 1u) ? 1u : 0u);
+}
+
+// Per-thread shared slots of the cooperative stage (kBlock threads).
+template <int kBlock>
+struct CoopShared {
+    float4 ray[2 * kBlock];  // [tid]: ox, oy, oz, tmin; [kBlock + tid]: -Sx, -Sy, Sz, kz bits
+    uint32_t owner[kBlock];  // per warp: lane of the group starting at a position
+    float t[kBlock];         // per warp: hit t of the pair at a position
+    uint32_t pid[kBlock];    // per warp: hit id of the pair at a position
+};
+
+template <int kBlock>
+__device__ __forceinline__ void coop_store_ray(CoopShared<kBlock>* cs, const RayState& r) {
+    cs->ray[threadIdx.x] = make_float4(r.ox, r.oy, r.oz, r.tmin);
+    cs->ray[kBlock + threadIdx.x] = make_float4(r.nSx, r.nSy, r.Sz, __int_as_float(r.kz));
+}
+
+// All 32 lanes of the warp call this; lanes without a ray pass mine_ok = false.
+template <int kKind, bool kStats, int kBlock>
+__device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_ok, bool any_hit, uint32_t tg_base,
+                                               uint32_t& tg_mask, float& best_t, uint32_t& best_p,
+                                               uint32_t& ng_group, int& sp, CoopShared<kBlock>* cs,
                                                unsigned long long& st_tris, uint32_t& st_wtri) {
     if (__ballot_sync(kFull, mine_ok && tg_mask != 0u) == 0u) return;
     const uint32_t lane = threadIdx.x & 31u;
-    uint32_t* s_pair = s_coop + (threadIdx.x & ~31u) * 3u;
-    float* s_t = reinterpret_cast<float*>(s_pair + 32);
-    uint32_t* s_pid = s_pair + 64;
-    for (int round = 0; round < 33; ++round) {  // at most 32 x 32 pairs: 32 rounds
+    const uint32_t wbase = threadIdx.x & ~31u;
+    for (int round = 0; round < 33; ++round) {  // every round empties at least one group
         const uint32_t mine = mine_ok ? tg_mask : 0u;
         const uint32_t cnt = (uint32_t)__popc(mine);
         uint32_t inc = cnt;
@@ -176,75 +207,73 @@ __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, const RayS
             const uint32_t v = __shfl_up_sync(kFull, inc, o);
             if (lane >= (uint32_t)o) inc += v;
         }
-        const uint32_t total = __shfl_sync(kFull, inc, 31);
-        if (total == 0u) break;
+        if (__shfl_sync(kFull, inc, 31) == 0u) break;
         const uint32_t off = inc - cnt;
-        // owners write the pairs of this round: positions off .. 31
-        uint32_t m = mine;
-        for (uint32_t p = off; p < 32u && m; ++p) {
-            const uint32_t k = (uint32_t)__ffs(m) - 1u;
-            m &= m - 1u;
-            s_pair[p] = lane << 5 | k;
-        }
-        if (mine_ok) tg_mask = m;
+        // this round: the owners whose whole group fits in positions 0..31
+        // (the first owner always does, at position 0)
+        const bool part = cnt != 0u && inc <= 32u;
+        const uint32_t starts = __reduce_or_sync(kFull, part ? 1u << off : 0u);
+        const uint32_t np = __reduce_max_sync(kFull, part ? inc : 0u);
+        if (part) cs->owner[wbase + off] = lane;
         __syncwarp();
-        const uint32_t np = total < 32u ? total : 32u;
-        const uint32_t e = lane < np ? s_pair[lane] : 0u;
-        const uint32_t owner = e >> 5;
-        RayState q;
-        q.ox = __shfl_sync(kFull, r.ox, owner);
-        q.oy = __shfl_sync(kFull, r.oy, owner);
-        q.oz = __shfl_sync(kFull, r.oz, owner);
-        q.nSx = __shfl_sync(kFull, r.nSx, owner);
-        q.nSy = __shfl_sync(kFull, r.nSy, owner);
-        q.Sz = __shfl_sync(kFull, r.Sz, owner);
-        q.tmin = __shfl_sync(kFull, r.tmin, owner);
-        q.kz = __shfl_sync(kFull, r.kz, owner);
+        const uint32_t q = 31u - (uint32_t)__clz(starts & ((2u << lane) - 1u));  // start of this lane's group
+        const uint32_t owner = lane < np ? cs->owner[wbase + q] : 0u;
+        const uint32_t omask = __shfl_sync(kFull, mine, owner);
+        const uint32_t obase = __shfl_sync(kFull, tg_base, owner);
         const float qt = __shfl_sync(kFull, best_t, owner);
-        const uint32_t ti = __shfl_sync(kFull, tg_base, owner) + (e & 31u);
         bool hit = false;
         float t = 0.0f;
         uint32_t pid = 0;
         if (lane < np) {
+            const uint32_t ti = obase + select_bit(omask, lane - q);
+            const float4 a = cs->ray[wbase + owner];
+            const float4 b = cs->ray[kBlock + wbase + owner];
+            RayState rq;
+            rq.ox = a.x;
+            rq.oy = a.y;
+            rq.oz = a.z;
+            rq.tmin = a.w;
+            rq.nSx = b.x;
+            rq.nSy = b.y;
+            rq.Sz = b.z;
+            rq.kz = __float_as_int(b.w);
             const float4 v0 = __ldg(sc.v0 + ti);
-            hit = intersect_tri(q, v0, __ldg(sc.v1 + ti), __ldg(sc.v2 + ti), qt, t);
+            hit = intersect_tri(rq, v0, __ldg(sc.v1 + ti), __ldg(sc.v2 + ti), qt, t);
             pid = __float_as_uint(v0.w);
             if (kStats) {
                 st_tris++;
                 if (lane == 0u) st_wtri++;
             }
         }
+        if (part && mine_ok) tg_mask = 0u;
         const uint32_t hm = __ballot_sync(kFull, hit);
         if (hm) {
             if (hit) {
-                s_t[lane] = t;
-                s_pid[lane] = pid;
+                cs->t[wbase + lane] = t;
+                cs->pid[wbase + lane] = pid;
             }
             __syncwarp();
-            if (cnt && off < 32u) {
-                const uint32_t len = (off + cnt < 32u ? off + cnt : 32u) - off;
-                uint32_t c = hm & (len == 32u ? kFull : ((1u << len) - 1u) << off);
-                while (c) {
-                    const uint32_t j = (uint32_t)__ffs(c) - 1u;
-                    c &= c - 1u;
-                    const float tj = s_t[j];
-                    const uint32_t pj = s_pid[j];
-                    if (kKind == 1 || (kKind == 2 && any_hit)) {
-                        best_t = tj;
-                        best_p = pj;
-                        tg_mask = 0;
-                        ng_group = 0;
-                        sp = 0;
-                        break;
-                    }
-                    if (best_p == FND_INVALID_ID || tj < best_t || (tj == best_t && pj < best_p)) {
-                        best_t = tj;
-                        best_p = pj;
-                    }
+            uint32_t c = part ? hm & (cnt == 32u ? kFull : ((1u << cnt) - 1u) << off) : 0u;
+            while (c) {
+                const uint32_t j = (uint32_t)__ffs(c) - 1u;
+                c &= c - 1u;
+                const float tj = cs->t[wbase + j];
+                const uint32_t pj = cs->pid[wbase + j];
+                if (kKind == 1 || (kKind == 2 && any_hit)) {
+                    best_t = tj;
+                    best_p = pj;
+                    tg_mask = 0;
+                    ng_group = 0;
+                    sp = 0;
+                    break;
+                }
+                if (best_p == FND_INVALID_ID || tj < best_t || (tj == best_t && pj < best_p)) {
+                    best_t = tj;
+                    best_p = pj;
                 }
             }
         }
-        __syncwarp();  // the entries are rewritten by the next round
+        __syncwarp();  // the slots are rewritten by the next round
     }
 }
 
@@ -254,7 +283,7 @@ __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, const RayS
 // instances; per-lane node / triangle arrays).
 template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLevel = false, bool kCoop = false>
 __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack,
-                                                 uint32_t* s_coop = nullptr) {
+                                                 CoopShared<kBlock>* s_coop = nullptr) {
     static_assert(!(kCoop && kTwoLevel), "cooperative triangle tests need one scene per warp");
     static_assert((kShort & (kShort - 1)) == 0, "short stack size must be a power of two");
     uint2 l_stack[kMaxStack - kShort];
@@ -303,6 +332,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                     src.load(id, r0, r1, ln);
                     if (kKind == 2) any_hit = src.any_of(ln, false);
                     r = setup_ray(r0, r1);
+                    if constexpr (kCoop) coop_store_ray<kBlock>(s_coop, r);
                     ray_id = id;
                     best_t = r.tmax;
                     best_p = FND_INVALID_ID;
@@ -373,8 +403,8 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
         }
         // ---- its triangles, tested by the whole warp ------------------------
         if constexpr (kCoop) {
-            coop_triangles<kKind, kStats>(sc, r, active && !overflow, any_hit, tg_base, tg_mask, best_t, best_p,
-                                          ng_group, sp, s_coop, st_tris, st_wtri);
+            coop_triangles<kKind, kStats, kBlock>(sc, active && !overflow, any_hit, tg_base, tg_mask, best_t, best_p,
+                                                  ng_group, sp, s_coop, st_tris, st_wtri);
             if (!active) continue;
         }
         // ---- its triangles (or, on the top level, its instances) ------------
@@ -499,7 +529,7 @@ constexpr int MinBlocks(int block) { return block == 256 ? 4 : 1152 / block; }
 template <bool kAny, bool kStats, int kShort, int kBlock>
 __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const TraceLaunch L) {
     __shared__ uint2 s_stack[kShort * kBlock];
-    __shared__ uint32_t s_coop[3 * kBlock];
+    __shared__ CoopShared<kBlock> s_coop;
     SingleSource src;
     src.scene = L.scene;
     src.rays = L.rays;
@@ -509,7 +539,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const 
     src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
     if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
     const Common C{L.counter, L.status, L.stats, L.refill_min, L.postpone_min};
-    persistent_trace<SingleSource, kAny ? 1 : 0, kStats, kShort, kBlock, false, true>(src, C, s_stack, s_coop);
+    persistent_trace<SingleSource, kAny ? 1 : 0, kStats, kShort, kBlock, false, true>(src, C, s_stack, &s_coop);
 }
 
 template <int kShort, int kBlock>
