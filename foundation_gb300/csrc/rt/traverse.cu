@@ -174,26 +174,35 @@ __device__ __forceinline__ uint32_t select_bit(uint32_t m, uint32_t k) {
     return pos + (k >= (m & 1u) ? 1u : 0u);
 }
 
-// Per-thread shared slots of the cooperative stage (kBlock threads).
-template <int kBlock>
+// Per-thread shared slots of the cooperative stage (kBlock threads); with
+// kMulti (lanes of one warp in different scenes) also the triangle planes of
+// each lane's scene.
+template <int kBlock, bool kMulti>
 struct CoopShared {
     float4 ray[2 * kBlock];  // [tid]: ox, oy, oz, tmin; [kBlock + tid]: -Sx, -Sy, Sz, kz bits
     uint32_t owner[kBlock];  // per warp: lane of the group starting at a position
     float t[kBlock];         // per warp: hit t of the pair at a position
     uint32_t pid[kBlock];    // per warp: hit id of the pair at a position
+    const float4* planes[kMulti ? 3 * kBlock : 1];  // [a * kBlock + tid]: vertex plane a of the lane's scene
 };
 
-template <int kBlock>
-__device__ __forceinline__ void coop_store_ray(CoopShared<kBlock>* cs, const RayState& r) {
+template <int kBlock, bool kMulti>
+__device__ __forceinline__ void coop_store_ray(CoopShared<kBlock, kMulti>* cs, const RayState& r,
+                                               const DeviceScene& sc) {
     cs->ray[threadIdx.x] = make_float4(r.ox, r.oy, r.oz, r.tmin);
     cs->ray[kBlock + threadIdx.x] = make_float4(r.nSx, r.nSy, r.Sz, __int_as_float(r.kz));
+    if constexpr (kMulti) {
+        cs->planes[threadIdx.x] = sc.v0;
+        cs->planes[kBlock + threadIdx.x] = sc.v1;
+        cs->planes[2 * kBlock + threadIdx.x] = sc.v2;
+    }
 }
 
 // All 32 lanes of the warp call this; lanes without a ray pass mine_ok = false.
-template <int kKind, bool kStats, int kBlock>
+template <int kKind, bool kStats, int kBlock, bool kMulti>
 __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_ok, bool any_hit, uint32_t tg_base,
                                                uint32_t& tg_mask, float& best_t, uint32_t& best_p,
-                                               uint32_t& ng_group, int& sp, CoopShared<kBlock>* cs,
+                                               uint32_t& ng_group, int& sp, CoopShared<kBlock, kMulti>* cs,
                                                unsigned long long& st_tris, uint32_t& st_wtri) {
     if (__ballot_sync(kFull, mine_ok && tg_mask != 0u) == 0u) return;
     const uint32_t lane = threadIdx.x & 31u;
@@ -237,8 +246,14 @@ __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_
             rq.nSy = b.y;
             rq.Sz = b.z;
             rq.kz = __float_as_int(b.w);
-            const float4 v0 = __ldg(sc.v0 + ti);
-            hit = intersect_tri(rq, v0, __ldg(sc.v1 + ti), __ldg(sc.v2 + ti), qt, t);
+            const float4 *p0 = sc.v0, *p1 = sc.v1, *p2 = sc.v2;
+            if constexpr (kMulti) {
+                p0 = cs->planes[wbase + owner];
+                p1 = cs->planes[kBlock + wbase + owner];
+                p2 = cs->planes[2 * kBlock + wbase + owner];
+            }
+            const float4 v0 = __ldg(p0 + ti);
+            hit = intersect_tri(rq, v0, __ldg(p1 + ti), __ldg(p2 + ti), qt, t);
             pid = __float_as_uint(v0.w);
             if (kStats) {
                 st_tris++;
@@ -281,10 +296,11 @@ __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_
 // kKind: 0 closest, 1 any, 2 per-lane (from the source). kTwoLevel: the
 // source is an InstancedSource (triangle leaves of the top level are
 // instances; per-lane node / triangle arrays).
-template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLevel = false, bool kCoop = false>
+template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLevel = false, bool kCoop = false,
+          bool kMulti = false>
 __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack,
-                                                 CoopShared<kBlock>* s_coop = nullptr) {
-    static_assert(!(kCoop && kTwoLevel), "cooperative triangle tests need one scene per warp");
+                                                 CoopShared<kBlock, kMulti>* s_coop = nullptr) {
+    static_assert(!(kCoop && kTwoLevel), "the top level of a two-level scene holds instances, not triangles");
     static_assert((kShort & (kShort - 1)) == 0, "short stack size must be a power of two");
     uint2 l_stack[kMaxStack - kShort];
     const int tid = threadIdx.x;
@@ -332,7 +348,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                     src.load(id, r0, r1, ln);
                     if (kKind == 2) any_hit = src.any_of(ln, false);
                     r = setup_ray(r0, r1);
-                    if constexpr (kCoop) coop_store_ray<kBlock>(s_coop, r);
+                    if constexpr (kCoop) coop_store_ray<kBlock, kMulti>(s_coop, r, src.scene_of(ln));
                     ray_id = id;
                     best_t = r.tmax;
                     best_p = FND_INVALID_ID;
@@ -403,8 +419,8 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
         }
         // ---- its triangles, tested by the whole warp ------------------------
         if constexpr (kCoop) {
-            coop_triangles<kKind, kStats, kBlock>(sc, active && !overflow, any_hit, tg_base, tg_mask, best_t, best_p,
-                                                  ng_group, sp, s_coop, st_tris, st_wtri);
+            coop_triangles<kKind, kStats, kBlock, kMulti>(sc, active && !overflow, any_hit, tg_base, tg_mask, best_t,
+                                                          best_p, ng_group, sp, s_coop, st_tris, st_wtri);
             if (!active) continue;
         }
         // ---- its triangles (or, on the top level, its instances) ------------
@@ -529,7 +545,7 @@ constexpr int MinBlocks(int block) { return block == 256 ? 4 : 1152 / block; }
 template <bool kAny, bool kStats, int kShort, int kBlock>
 __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const TraceLaunch L) {
     __shared__ uint2 s_stack[kShort * kBlock];
-    __shared__ CoopShared<kBlock> s_coop;
+    __shared__ CoopShared<kBlock, false> s_coop;
     SingleSource src;
     src.scene = L.scene;
     src.rays = L.rays;
@@ -545,13 +561,14 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const 
 template <int kShort, int kBlock>
 __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) batch_kernel(const BatchLaunch B) {
     __shared__ uint2 s_stack[kShort * kBlock];
+    __shared__ CoopShared<kBlock, true> s_coop;
     BatchSource src;
     src.jobs = B.jobs;
     src.prefix = B.prefix;
     src.njobs = B.njobs;
     src.n = B.total;
     const Common C{B.counter, B.status, nullptr, B.refill_min, B.postpone_min};
-    persistent_trace<BatchSource, 2, false, kShort, kBlock>(src, C, s_stack);
+    persistent_trace<BatchSource, 2, false, kShort, kBlock, false, true, true>(src, C, s_stack, &s_coop);
 }
 
 template <bool kAny>
