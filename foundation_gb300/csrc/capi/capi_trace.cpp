@@ -301,8 +301,13 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             if (bvh->traversal_cost != 0.0f) bp.trav_cost = bvh->traversal_cost;
             if (bvh->split_budget != 0.0f) bp.max_refs_factor = bvh->split_budget;
         }
-        CHECK_CODE(bp.max_refs_factor >= 0.0 && bp.max_refs_factor <= 4.0, FND_ERR_INVALID_ARG,
-                   "split_budget %g not in [0, 4]", bp.max_refs_factor);
+        CHECK_CODE(bp.max_refs_factor >= 0.0 && bp.max_refs_factor <= 16.0, FND_ERR_INVALID_ARG,
+                   "split_budget %g not in [0, 16]", bp.max_refs_factor);
+        // references are indexed with 32 bits
+        CHECK_CODE(!(bvh && (bvh->flags & FND_BVH_SPATIAL_SPLITS)) ||
+                       (double)nt * (1.0 + bp.max_refs_factor) < 4294967295.0,
+                   FND_ERR_INVALID_ARG, "split_budget %g allows more than 2^32 references for %u triangles",
+                   bp.max_refs_factor, nt);
         const float margin_scale = bvh && bvh->margin_scale != 0.0f ? bvh->margin_scale : 1.0f;
         CHECK_CODE(margin_scale >= 1.0f && margin_scale <= 65536.0f, FND_ERR_INVALID_ARG,
                    "margin_scale %g not in [1, 65536]", (double)margin_scale);

@@ -90,7 +90,10 @@ typedef struct fnd_rt_bvh_desc {
     float traversal_cost;   /* SAH cost of a traversal step relative to a triangle
                                test, (0, 64]; 0: default 1 (the reference tree) */
     float split_budget;     /* FND_BVH_SPATIAL_SPLITS: references the splits may add,
-                               per triangle, [0, 4]; 0: default 2 */
+                               per triangle, [0, 16]; 0: default 2. The builder stops
+                               splitting where the SAH gains nothing, so a large budget
+                               is a cap rather than a target (a dense soup of 1M
+                               triangles settles near 6 references per triangle) */
     float margin_scale;     /* box inflation relative to the default (2^-16 of the scene
                                size), [1, 2^16]; 0: 1. A scene instanced at a scale far below
                                the world's needs more (fnd_rt_instances_upload checks it) */
@@ -102,7 +105,7 @@ typedef struct fnd_rt_bvh_desc {
  * which tightens the tree of scenes with long, overlapping triangles. Hits
  * are identical either way. */
 enum { FND_BVH_SPATIAL_SPLITS = 1u };
-/* Build on the GPU: linear BVH over 30-bit Morton codes (Karras 2012) with
+/* Build on the GPU: linear BVH over 63-bit Morton codes (Karras 2012) with
  * SAH leaf merging, collapsed to the same 8-wide format on the device. Much
  * faster to build, somewhat slower to trace than the binned-SAH tree; hits
  * are identical. Up to 2^27 triangles; not combined with spatial splits;

@@ -85,6 +85,13 @@ def test_soup_1m_tris(ctx):
     assert ss.info()["num_refs"] > len(so.idx)
     assert_same(ss.closest(rays), ref)
     ss.close()
+    # an uncapped split budget (about 6.4 references per triangle here): the
+    # tree the 1M-triangle throughput figure is measured on
+    ss = ctx.upload(so.verts, so.idx, spatial_splits=True, split_budget=8.0)
+    assert ss.info()["num_refs"] > 5 * len(so.idx)
+    assert_same(ss.closest(rays), ref)
+    assert np.array_equal(ss.any(rays), b.any(rays))
+    ss.close()
 
 
 def test_device_pointers_and_stats(ctx):
