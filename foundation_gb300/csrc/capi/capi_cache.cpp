@@ -41,6 +41,7 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
         4 * P, 4 * P, 4 * P, 4 * P,            // master, m, v, grad
         sizeof(double) * 4,                    // loss
         sizeof(NRC::TrainSample) * scap, sizeof(float4) * scap, sizeof(NRC::CachePoint) * qcap, 256,
+        sizeof(uint16_t) * NRC::kFwdElems, 4 * P,  // weight average: query image, fp32 average
     };
     size_t total = 0;
     for (size_t sz : sizes) total += Align256(sz);
@@ -60,6 +61,10 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
     net.adam_v = reinterpret_cast<float*>(take(sizes[4]));
     net.grad = reinterpret_cast<float*>(take(sizes[5]));
     net.loss = reinterpret_cast<double*>(take(sizes[6]));
+    const bool averaging = c.desc.weight_average > 0.0f;
+    net.fwd_avg = averaging ? reinterpret_cast<uint16_t*>(take(sizes[11])) : nullptr;
+    net.avg = averaging ? reinterpret_cast<float*>(take(sizes[12])) : nullptr;
+    net.avg_decay = c.desc.weight_average;
     if (c.d_block) {
         if (c.train_stream) CUDA_CHECK(cudaStreamSynchronize(c.train_stream));
         // keep the trained state: copy the network, moments and images across
@@ -69,6 +74,10 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
         CUDA_CHECK(cudaMemcpyAsync(net.adam_m, c.net.adam_m, 4 * P, cudaMemcpyDeviceToDevice, ctx->stream));
         CUDA_CHECK(cudaMemcpyAsync(net.adam_v, c.net.adam_v, 4 * P, cudaMemcpyDeviceToDevice, ctx->stream));
         CUDA_CHECK(cudaMemsetAsync(net.grad, 0, 4 * P, ctx->stream));
+        if (averaging) {
+            CUDA_CHECK(cudaMemcpyAsync(net.fwd_avg, c.net.fwd_avg, sizes[11], cudaMemcpyDeviceToDevice, ctx->stream));
+            CUDA_CHECK(cudaMemcpyAsync(net.avg, c.net.avg, 4 * P, cudaMemcpyDeviceToDevice, ctx->stream));
+        }
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
         CUDA_CHECK(cudaFree(c.d_block));
     }
@@ -113,6 +122,8 @@ int fnd_rt_cache_create(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ca
                    "batch / train_steps out of range");
         CHECK_CODE(desc->learning_rate > 0.0f && desc->learning_rate < 1.0f, FND_ERR_INVALID_ARG,
                    "learning rate %g out of range", desc->learning_rate);
+        CHECK_CODE(desc->weight_average >= 0.0f && desc->weight_average < 1.0f, FND_ERR_INVALID_ARG,
+                   "weight_average %g not in [0, 1)", desc->weight_average);
         CUDA_CHECK(cudaSetDevice(ctx->device));
         FreeCache(ctx);
         ctx->cache = new FndCacheState();
@@ -185,6 +196,7 @@ int fnd_rt_cache_set_weights(fnd_rt_ctx* ctx, const float* w, uint32_t n) {
         for (uint32_t i = 0; i < n; ++i) CHECK_CODE(std::isfinite(w[i]), FND_ERR_INVALID_ARG, "weight %u not finite", i);
         CUDA_CHECK(cudaSetDevice(ctx->device));
         CUDA_CHECK(cudaMemcpyAsync(c.net.master, w, 4ull * n, cudaMemcpyHostToDevice, ctx->stream));
+        c.net.avg_steps = 0;
         CUDA_CHECK(NRC::RewriteImages(c.net, ctx->stream));
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });
@@ -239,6 +251,7 @@ int fnd_rt_cache_load(fnd_rt_ctx* ctx, const char* path) {
             c.net.lo[a] = lo[a];
             c.net.hi[a] = hi[a];
         }
+        c.net.avg_steps = 0;
         CUDA_CHECK(NRC::RewriteImages(c.net, ctx->stream));
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });

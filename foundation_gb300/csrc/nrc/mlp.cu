@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(32 * kInferWarps) infer_kernel(const Net net, 
     const int g = lane >> 2, t = lane & 3;
     uint16_t* xbuf = s_fwd + kFwdElems + warp * (16 * kStrideX);
     {
-        const int4* src = reinterpret_cast<const int4*>(net.fwd);
+        const int4* src = reinterpret_cast<const int4*>(net.fwd_avg ? net.fwd_avg : net.fwd);
         int4* dst = reinterpret_cast<int4*>(s_fwd);
         for (int i = tid; i < kFwdElems / 8; i += 32 * kInferWarps) dst[i] = src[i];
     }
@@ -490,7 +490,25 @@ __device__ __forceinline__ void write_images(const Net& net, int i, float w) {
     net.bwd[BwdOffset(l) + k * (LayerNb(l) + kPad) + nn] = b;
 }
 
-__global__ void adam_kernel(const Net net, float lr, float c1, float c2) {
+// The forward image only (the averaged weights are never trained).
+__device__ __forceinline__ void write_fwd_image(uint16_t* fwd, int i, float w) {
+    int l = 0;
+    while (l + 1 < kLayers && i >= ParamOffset(l + 1)) ++l;
+    const int N = LayerN(l), K = LayerK(l);
+    const int k = (i - ParamOffset(l)) / N, nn = (i - ParamOffset(l)) % N;
+    fwd[FwdOffset(l) + nn * (K + kPad) + k] = bf16_bits(w);
+}
+
+// Weight averaging restarts from the current weights: the average is empty
+// and the query image holds the weights themselves.
+__device__ __forceinline__ void restart_average(const Net& net, int i, float w) {
+    if (!net.avg) return;
+    net.avg[i] = 0.0f;
+    write_fwd_image(net.fwd_avg, i, w);
+}
+
+// c3 = 1 - avg_decay^avg_steps (the bias correction of the average)
+__global__ void adam_kernel(const Net net, float lr, float c1, float c2, float c3) {
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kNumParams; i += gridDim.x * blockDim.x) {
         const float gr = net.grad[i];
@@ -502,6 +520,11 @@ __global__ void adam_kernel(const Net net, float lr, float c1, float c2) {
         net.master[i] = w;
         net.grad[i] = 0.0f;
         write_images(net, i, w);
+        if (net.avg) {
+            const float a = net.avg_decay * net.avg[i] + (1.0f - net.avg_decay) * w;
+            net.avg[i] = a;
+            write_fwd_image(net.fwd_avg, i, a / c3);
+        }
     }
 }
 
@@ -518,12 +541,15 @@ __global__ void init_kernel(const Net net, uint64_t seed) {
         net.adam_v[i] = 0.0f;
         net.grad[i] = 0.0f;
         write_images(net, i, w);
+        restart_average(net, i, w);
     }
 }
 
 __global__ void images_kernel(const Net net) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kNumParams; i += gridDim.x * blockDim.x)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kNumParams; i += gridDim.x * blockDim.x) {
         write_images(net, i, net.master[i]);
+        restart_average(net, i, net.master[i]);
+    }
 }
 
 size_t train_smem() {
@@ -546,6 +572,7 @@ size_t InferSmemBytes() { return infer_smem(); }
 cudaError_t InitNet(const Net& net, uint64_t seed, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(net.fwd, 0, sizeof(uint16_t) * kFwdElems, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(net.bwd, 0, sizeof(uint16_t) * kBwdElems, s);
+    if (e == cudaSuccess && net.fwd_avg) e = cudaMemsetAsync(net.fwd_avg, 0, sizeof(uint16_t) * kFwdElems, s);
     if (e != cudaSuccess) return e;
     init_kernel<<<(kNumParams + 255) / 256, 256, 0, s>>>(net, seed);
     return cudaGetLastError();
@@ -578,7 +605,12 @@ cudaError_t InferRaw(const Net& net, const float* feats, uint32_t n, float* out,
 static cudaError_t launch_adam(Net& net, float lr, cudaStream_t s) {
     net.step += 1;
     const double c1 = 1.0 - std::pow(0.9, (double)net.step), c2 = 1.0 - std::pow(0.99, (double)net.step);
-    adam_kernel<<<(kNumParams + 255) / 256, 256, 0, s>>>(net, lr, (float)c1, (float)c2);
+    double c3 = 1.0;
+    if (net.avg) {
+        net.avg_steps += 1;
+        c3 = 1.0 - std::pow((double)net.avg_decay, (double)net.avg_steps);
+    }
+    adam_kernel<<<(kNumParams + 255) / 256, 256, 0, s>>>(net, lr, (float)c1, (float)c2, (float)c3);
     return cudaGetLastError();
 }
 

@@ -72,11 +72,18 @@ struct Net {
     float* grad;      // fp32 gradient accumulator (kNumParams)
     double* loss;     // [0] running sum of the loss of the current step
     uint32_t step;    // Adam steps taken
+    // weight averaging (queries only): fp32 moving average of the iterates
+    // and the bf16 forward image of avg / (1 - decay^avg_steps); null: off
+    float* avg;
+    uint16_t* fwd_avg;
+    float avg_decay;
+    uint32_t avg_steps;
     float lo[3], hi[3];  // scene box for the position encoding
 };
 
 // Host API (launches on `s`).
 cudaError_t InitNet(const Net& net, uint64_t seed, cudaStream_t s);        // He-uniform init + images
+// Queries evaluate the averaged weights when averaging is on, else the latest.
 cudaError_t Infer(const Net& net, const CachePoint* pts, const uint32_t* count, uint32_t capacity,
                   float4* fb, int grid, cudaStream_t s);                     // fb[pixel] += beta * max(0, f(x))
 cudaError_t InferRaw(const Net& net, const float* feats, uint32_t n, float* out, cudaStream_t s);  // test hook
@@ -87,7 +94,9 @@ cudaError_t TrainStep(Net& net, const TrainSample* smp, const float4* targets, c
 // Test hook: gradient of the loss on explicit features / targets (no Adam).
 cudaError_t GradRaw(const Net& net, const float* feats, const float* targets, uint32_t n, cudaStream_t s);
 cudaError_t AdamRaw(Net& net, float lr, cudaStream_t s);
-cudaError_t RewriteImages(const Net& net, cudaStream_t s);  // bf16 images from the fp32 master weights
+// bf16 images from the fp32 master weights; restarts the weight average
+// (the caller zeroes net.avg_steps)
+cudaError_t RewriteImages(const Net& net, cudaStream_t s);
 // Test hook: the bf16 input features (widened to float) of n cache points.
 cudaError_t EncodeRaw(const Net& net, const CachePoint* pts, uint32_t n, float* out, cudaStream_t s);
 size_t TrainSmemBytes();

@@ -5,6 +5,8 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../../include/fnd_rt.h"
@@ -104,9 +106,22 @@ __device__ __forceinline__ bool intersect_tri(const RayState& r, float4 v0, floa
     return true;
 }
 
-// 2^23 + byte, exactly: the byte placed in the low mantissa bits of 2^23.
-__device__ __forceinline__ float byte_plus_2p23(uint32_t word, uint32_t sel) {
-    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | sel));
+// Two quantised planes as floats 1024 + q, exactly: one PRMT builds the
+// half2 (0x64 | q) pair (a half with exponent 2^10 and q in its low mantissa
+// bits), and the two halves widen to float off the integer pipe. sel picks
+// the byte pair: 0x4140 for bytes 0 and 1, 0x4342 for bytes 2 and 3.
+__device__ __forceinline__ void plane_pair(uint32_t word, uint32_t sel, float& a, float& b) {
+#if defined(__CUDA_ARCH__)
+    const uint32_t h2 = __byte_perm(word, 0x64u, sel);
+    __half2 h;
+    memcpy(&h, &h2, sizeof(h));
+    a = __low2float(h);
+    b = __high2float(h);
+#else
+    const uint32_t k = (sel & 0xFu) * 8u;
+    a = 1024.0f + (float)((word >> k) & 0xFFu);
+    b = 1024.0f + (float)((word >> (k + 8u)) & 0xFFu);
+#endif
 }
 
 // max / min of three (one instruction on the sm_100 family; NaN operands
@@ -179,30 +194,41 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
     const uint32_t nz0 = fz ? w4.z : w3.x, nz1 = fz ? w4.w : w3.y;
     const uint32_t gz0 = fz ? w3.x : w4.z, gz1 = fz ? w3.y : w4.w;
     // A plane's t is q * s + b with q the quantised byte. The byte is read
-    // as the float 2^23 + q (one PRMT) and the 2^23 * s is folded into the
+    // as the float 1024 + q (plane_pair) and the 1024 * s is folded into the
     // offset, near planes rounded down and far planes up:
-    //   near: rd((2^23+q) s + rd(b - 2^23 s)) <= rd(q s + b) <= rn(q s + b)
-    //   far:  ru((2^23+q) s + ru(b - 2^23 s)) >= ru(q s + b) >= rn(q s + b)
+    //   near: rd((1024+q) s + rd(b - 1024 s)) <= rd(q s + b) <= rn(q s + b)
+    //   far:  ru((1024+q) s + ru(b - 1024 s)) >= ru(q s + b) >= rn(q s + b)
     // so every child box is at least as wide as under round-to-nearest
     // fma(q, s, b), the culling stays conservative and the hits exact.
-    const float bnx = __fmaf_rd(-8388608.0f, sx, bx), bfx = __fmaf_ru(-8388608.0f, sx, bx);
-    const float bny = __fmaf_rd(-8388608.0f, sy, by), bfy = __fmaf_ru(-8388608.0f, sy, by);
-    const float bnz = __fmaf_rd(-8388608.0f, sz, bz), bfz = __fmaf_ru(-8388608.0f, sz, bz);
+    const float bnx = __fmaf_rd(-1024.0f, sx, bx), bfx = __fmaf_ru(-1024.0f, sx, bx);
+    const float bny = __fmaf_rd(-1024.0f, sy, by), bfy = __fmaf_ru(-1024.0f, sy, by);
+    const float bnz = __fmaf_rd(-1024.0f, sz, bz), bfz = __fmaf_ru(-1024.0f, sz, bz);
     // the boxes alone: bit s of hitm for slot s (empty slots included; the
-    // slot kinds below mask them out)
+    // slot kinds below mask them out); two slots per byte pair
     uint32_t hitm = 0;
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        const uint32_t sel = (uint32_t)(s & 3);
-        const float tnx = __fmaf_rd(byte_plus_2p23(s < 4 ? nx0 : nx1, sel), sx, bnx);
-        const float tny = __fmaf_rd(byte_plus_2p23(s < 4 ? ny0 : ny1, sel), sy, bny);
-        const float tnz = __fmaf_rd(byte_plus_2p23(s < 4 ? nz0 : nz1, sel), sz, bnz);
-        const float tfx = __fmaf_ru(byte_plus_2p23(s < 4 ? gx0 : gx1, sel), sx, bfx);
-        const float tfy = __fmaf_ru(byte_plus_2p23(s < 4 ? gy0 : gy1, sel), sy, bfy);
-        const float tfz = __fmaf_ru(byte_plus_2p23(s < 4 ? gz0 : gz1, sel), sz, bfz);
-        const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
-        const float tf = min3f(tfx, tfy, fminf(tfz, tfar));
-        hitm |= tn <= tf ? 1u << s : 0u;
+    for (int pr = 0; pr < 4; ++pr) {
+        const uint32_t sel = (pr & 1) ? 0x4342u : 0x4140u;
+        float q0[6], q1[6];
+        plane_pair(pr < 2 ? nx0 : nx1, sel, q0[0], q1[0]);
+        plane_pair(pr < 2 ? ny0 : ny1, sel, q0[1], q1[1]);
+        plane_pair(pr < 2 ? nz0 : nz1, sel, q0[2], q1[2]);
+        plane_pair(pr < 2 ? gx0 : gx1, sel, q0[3], q1[3]);
+        plane_pair(pr < 2 ? gy0 : gy1, sel, q0[4], q1[4]);
+        plane_pair(pr < 2 ? gz0 : gz1, sel, q0[5], q1[5]);
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float* q = e ? q1 : q0;
+            const float tnx = __fmaf_rd(q[0], sx, bnx);
+            const float tny = __fmaf_rd(q[1], sy, bny);
+            const float tnz = __fmaf_rd(q[2], sz, bnz);
+            const float tfx = __fmaf_ru(q[3], sx, bfx);
+            const float tfy = __fmaf_ru(q[4], sy, bfy);
+            const float tfz = __fmaf_ru(q[5], sz, bfz);
+            const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
+            const float tf = min3f(tfx, tfy, fminf(tfz, tfar));
+            hitm |= tn <= tf ? 1u << (2 * pr + e) : 0u;
+        }
     }
     // leaf slots: the 0x80 flag of their meta byte
     const uint32_t leaves = meta_leaf_bits(w1.z) | meta_leaf_bits(w1.w) << 4;

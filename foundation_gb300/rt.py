@@ -146,7 +146,7 @@ BATCH_NO_GRAPH = 1
 class CacheDesc(C.Structure):
     _fields_ = [("train_paths", C.c_uint32), ("train_steps", C.c_uint32), ("batch", C.c_uint32),
                 ("learning_rate", C.c_float), ("specular_alpha", C.c_float), ("flags", C.c_uint32),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("weight_average", C.c_float)]
 
 
 class CacheStats(C.Structure):
@@ -377,8 +377,9 @@ class Context:
 
     # ---- radiance cache -------------------------------------------------
     def cache_create(self, scene: "Scene", train_paths: int = 65536, train_steps: int = 4, batch: int = 16384,
-                     learning_rate: float = 1e-2, specular_alpha: float = 0.1, seed: int = 1):
-        d = CacheDesc(train_paths, train_steps, batch, learning_rate, specular_alpha, 0, seed)
+                     learning_rate: float = 1e-2, specular_alpha: float = 0.1, seed: int = 1,
+                     weight_average: float = 0.0):
+        d = CacheDesc(train_paths, train_steps, batch, learning_rate, specular_alpha, 0, seed, weight_average)
         _check(load().fnd_rt_cache_create(self._h, scene.handle, C.byref(d)), self._h)
 
     def cache_destroy(self):

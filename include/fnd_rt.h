@@ -462,6 +462,12 @@ typedef struct fnd_cache_desc {
     float specular_alpha;   /* GGX alpha below which a vertex counts as specular (0.1) */
     uint32_t flags;         /* reserved, 0 */
     uint64_t seed;          /* weight initialisation and sampling seed */
+    float weight_average;   /* [0, 1): 0 queries the latest weights; d > 0 queries an
+                               exponential moving average of the optimiser's iterates,
+                               a <- d a + (1 - d) w after every Adam step, divided by
+                               1 - d^steps (Polyak averaging; it damps the weight noise
+                               of a high learning rate). Training always uses the latest
+                               weights; set_weights / load restart the average. */
 } fnd_cache_desc;
 
 typedef struct fnd_cache_stats {

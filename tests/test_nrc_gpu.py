@@ -128,6 +128,44 @@ def test_overfit_and_checkpoint(cache_ctx, tmp_path):
     assert np.array_equal(ctx.cache_eval(x), y0)
 
 
+def test_weight_average_matches_host_restatement(built):
+    """With weight averaging, queries (and cache_eval) use the bias-corrected
+    moving average of the Adam iterates: a_k = d a_(k-1) + (1 - d) w_k,
+    evaluated at a_k / (1 - d^k); training keeps the latest weights, and
+    set_weights restarts the average."""
+    import foundation_gb300 as fg
+    d = 0.9
+    cs = S.cornell_scene(num_spheres=4, level=1)
+    with fg.Context(0) as ctx:
+        s = ctx.upload(cs.verts, cs.idx)
+        ctx.cache_create(s, seed=11, weight_average=d)
+        x = features(300, 9)
+        w0 = ctx.cache_weights()
+        ref0, _, _ = O.mlp_forward_backward(bf16_round(w0), x, None, emulate_bf16=True)
+        y0 = ctx.cache_eval(x)
+        assert np.abs(y0 - ref0).max() / (np.abs(ref0).max() + 1e-6) < 2e-2
+        rng = np.random.default_rng(12)
+        a = np.zeros(len(w0), np.float64)
+        for k in range(1, 6):
+            ctx.cache_adam_step((rng.normal(size=len(w0)) * 1e-2).astype(np.float32), 5e-2)
+            a = d * a + (1 - d) * ctx.cache_weights().astype(np.float64)
+        avg = (a / (1 - d ** 5)).astype(np.float32)
+        w5 = ctx.cache_weights()
+        y = ctx.cache_eval(x)
+        ref, _, _ = O.mlp_forward_backward(bf16_round(avg), x, None, emulate_bf16=True)
+        latest, _, _ = O.mlp_forward_backward(bf16_round(w5), x, None, emulate_bf16=True)
+        err = np.abs(y - ref).max() / (np.abs(ref).max() + 1e-6)
+        assert err < 2e-2, err
+        # the average differs measurably from the latest iterate
+        assert np.abs(latest - ref).max() / (np.abs(ref).max() + 1e-6) > 5 * err
+        ctx.cache_set_weights(w5)
+        y5 = ctx.cache_eval(x)
+        assert np.abs(y5 - latest).max() / (np.abs(latest).max() + 1e-6) < 2e-2
+        with pytest.raises(fg.FndError):
+            ctx.cache_create(s, seed=11, weight_average=1.0)
+        s.close()
+
+
 def test_cache_render_beats_plain_at_equal_samples(built):
     """Cornell box at 96x54: after 32 training calls the cache-terminated
     render at 16 spp has lower relMSE against the 4096-spp FP64 fixture than
