@@ -42,6 +42,10 @@ N_RAYS = 8_388_608
 METRIC = "Mrays/s closest-hit"
 UNIT = "Mrays/s"
 PROFILES = os.path.join(ROOT, "profiles")
+# Tree of the Cornell blocks (path tracer, cache frames, time to relMSE):
+# binned SAH with spatial splits, split budget 8 (the SAH stops splitting
+# before the budget); hits are those of any other tree.
+CORNELL_BVH = dict(spatial_splits=True, split_budget=8.0)
 # Radiance cache of the cache blocks: 65,536 training paths per frame (the
 # workload's figure), 8 Adam steps of 16,384 samples at lr 1e-2, queries on
 # the exponential moving average (0.98) of the iterates, GGX alpha below 0.05
@@ -62,9 +66,10 @@ def parse_args():
     p.add_argument("--no-extra", action="store_true", help="skip the path-tracer and 1M-triangle blocks")
     p.add_argument("--workload", default="cornell", choices=["cornell", "soup1m"],
                    help="traversal workload of the timed steps (cornell: the headline)")
-    p.add_argument("--spatial-splits", action="store_true", help="build the scene with spatial splits")
-    p.add_argument("--split-budget", type=float, default=0.0,
-                   help="with --spatial-splits: extra references per triangle the splits may add (0: default 2)")
+    p.add_argument("--bvh", default="spatial", choices=["spatial", "binned"],
+                   help="tree of the timed scene: binned SAH with spatial splits (default) or binned SAH alone")
+    p.add_argument("--split-budget", type=float, default=8.0,
+                   help="with --bvh spatial: extra references per triangle the splits may add")
     p.add_argument("--extra", default="path_tracer,incoherent_1m_tris,time_to_relmse_1080p,batched_256_scenes,"
                                       "large_scene_4k",
                    help="comma-separated extra blocks to run (also: cache_frames)")
@@ -99,7 +104,6 @@ def config_block(sc, n_rays, world, kind: str = "cornell"):
         "scene_tris": sc.num_tris,
         "rays_per_step_per_gpu": n_rays,
         "rays": "origins uniform in the box, directions uniform on S^2",
-        "bvh": "binned SAH 32 bins, <=4 tris/leaf, collapsed to 8-wide compressed nodes",
         "l2": "inputs larger than L2: 268 MB of rays streamed per step per GPU",
         "parallelism": f"replicas x{world}",
     }
@@ -247,7 +251,7 @@ def path_tracer_block(fg, torch, stream, local):
     from foundation_gb300 import scenes
     cs = scenes.cornell_scene()
     ctx = fg.Context(local, stream=stream.cuda_stream)
-    s = ctx.upload(cs.verts, cs.idx)
+    s = ctx.upload(cs.verts, cs.idx, **CORNELL_BVH)
     s.set_materials(cs.tri_material, scenes.material_records(cs))
     s.set_lights(scenes.light_records(cs))
     out = torch.empty(1920 * 1080 * 3, dtype=torch.float32, device="cuda")
@@ -333,7 +337,7 @@ def cache_frames_block(fg, torch, stream, local, frames: int = 8):
     from foundation_gb300 import scenes
     cs = scenes.cornell_scene()
     ctx = fg.Context(local, stream=stream.cuda_stream)
-    s = ctx.upload(cs.verts, cs.idx)
+    s = ctx.upload(cs.verts, cs.idx, **CORNELL_BVH)
     s.set_materials(cs.tri_material, scenes.material_records(cs))
     s.set_lights(scenes.light_records(cs))
     out = torch.empty(1920 * 1080 * 3, dtype=torch.float32, device="cuda")
@@ -371,7 +375,7 @@ def time_to_relmse_block(fg, torch, stream, local, ref_spp: int = 8192):
     from foundation_gb300 import scenes
     cs = scenes.cornell_scene()
     ctx = fg.Context(local, stream=stream.cuda_stream)
-    s = ctx.upload(cs.verts, cs.idx)
+    s = ctx.upload(cs.verts, cs.idx, **CORNELL_BVH)
     s.set_materials(cs.tri_material, scenes.material_records(cs))
     s.set_lights(scenes.light_records(cs))
     W, H, cam = 1920, 1080, scenes.CORNELL_CAMERA
@@ -667,7 +671,8 @@ def main():
     n = len(rays)
     stream = torch.cuda.Stream()
     ctx = fg.Context(local, stream=stream.cuda_stream)
-    scene = ctx.upload(sc.verts, sc.idx, spatial_splits=args.spatial_splits, split_budget=args.split_budget)
+    bvh = dict(spatial_splits=True, split_budget=args.split_budget) if args.bvh == "spatial" else {}
+    scene = ctx.upload(sc.verts, sc.idx, **bvh)
     info = scene.info()
     rd = torch.from_numpy(rays).to("cuda")
     hd = torch.empty(2 * n, dtype=torch.int32, device="cuda")
@@ -745,9 +750,11 @@ def main():
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(config_block(sc, n, world, args.workload),
-                           **({"bvh": f"binned SAH 32 bins with spatial splits, split budget "
-                                      f"{args.split_budget or 2.0:g}, collapsed to 8-wide compressed nodes"}
-                              if args.spatial_splits else {})),
+                           bvh=(f"binned SAH 32 bins, <=4 tris/leaf, spatial splits (split budget "
+                                f"{args.split_budget:g}), collapsed to 8-wide compressed nodes"
+                                if args.bvh == "spatial" else
+                                "binned SAH 32 bins, <=4 tris/leaf, collapsed to 8-wide compressed nodes"),
+                           roofline_bytes="algorithmic bytes counted by the oracle on the binary binned-SAH tree"),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8,
                     "steps": e2e_steps, "matches_device_result": e2e_ok},
             "gpu_launches": args.steps,
@@ -758,7 +765,7 @@ def main():
                          "oracle_tris_per_ray": tris, "kernel_ms_avg": kern_ms, "device_counters": counters,
                          "l2_measured": l2, "frac_of_l2": achieved / l2_peak},
             "clocks": clk,
-            "scene_info": {k: info[k] for k in ("num_wide_nodes", "wide_depth", "node_bytes", "tri_bytes",
+            "scene_info": {k: info[k] for k in ("num_wide_nodes", "num_refs", "wide_depth", "node_bytes", "tri_bytes",
                                                 "build_ms", "collapse_ms")},
         }
         if not args.no_extra:
