@@ -77,14 +77,8 @@ def parse_args():
 
 
 def workload(rank: int, n_rays: int, kind: str = "cornell"):
-    from foundation_gb300 import scenes
-    if kind == "soup1m":
-        sc = scenes.soup_scene(1 << 20, seed=2)
-        rays = scenes.incoherent_rays(n_rays, (0, 0, 0), (1, 1, 1), seed=2, stream_base=(1 << 40) + rank * n_rays)
-        return sc, rays
-    sc = scenes.cornell_scene()
-    rays = scenes.incoherent_rays(n_rays, *sc.bounds, seed=1, stream_base=(1 << 40) + rank * n_rays)
-    return sc, rays
+    from foundation_gb300 import replicas
+    return replicas.shard_workload(kind, rank, n_rays)
 
 
 def config_block(sc, n_rays, world, kind: str = "cornell"):
@@ -666,6 +660,7 @@ def main():
     if world > 1:
         dist.init_process_group("nccl")
     import foundation_gb300 as fg
+    from foundation_gb300 import replicas
     fg.load()  # fails loudly when the native library is missing
     sc, rays = workload(rank, args.rays, args.workload)
     n = len(rays)
@@ -706,11 +701,8 @@ def main():
     per_step = [s.elapsed_time(e) for s, e in ev]
     total_ms = ev[0][0].elapsed_time(ev[-1][1])
     clk = clocks.summary(t_wall0, t_wall1)
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
-    value = n * args.steps * world / (total_ms * 1e-3) / 1e6
+    total_ms = replicas.max_over_ranks(total_ms, dist, "cuda")
+    value = replicas.job_rate(n, args.steps, world, total_ms * 1e-3)
 
     # end to end through the C ABI with pinned host buffers
     pin_in = fg.PinnedBuffer(n * 32)
@@ -727,10 +719,7 @@ def main():
     for _ in range(e2e_steps):
         scene.closest(hr, ho)
     e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = n * e2e_steps * world / float(te.item()) / 1e6
+    e2e_value = replicas.job_rate(n, e2e_steps, world, replicas.max_over_ranks(e2e_s, dist, "cuda"))
     # spot-check the end-to-end result against the device result
     dev_hits = hd.cpu().numpy().view(np.uint32)
     e2e_ok = bool(np.array_equal(dev_hits[0::2], ho["prim"]))
