@@ -5,6 +5,7 @@
 // a message in fnd_rt_last_error; nothing throws across the ABI and nothing
 // terminates the process (the reference's CHECK -> BugCheck -> terminate,
 // src/Core/Core.cpp:7-10, is not acceptable behind a C ABI).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -58,7 +59,8 @@ void EnsureDevice(void*& ptr, size_t& cap, size_t bytes) {
 }
 
 cudaError_t LaunchTraceOrdered(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, RT::TraceLaunch L, bool any, bool stats,
-                               const RT::TraceConfig& cfg, int grid) {
+                               const RT::TraceConfig& cfg, int grid, cudaStream_t stream) {
+    if (!stream) stream = ctx->stream;
     L.order = nullptr;
     if (cfg.sort_bits && L.n > 1 && scene->view.num_nodes) {
         const size_t m = size_t(1) << cfg.sort_bits;
@@ -75,11 +77,11 @@ cudaError_t LaunchTraceOrdered(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, RT::T
         p += align(sizeof(uint32_t) * m);
         B.sums = reinterpret_cast<uint32_t*>(p);
         const cudaError_t e = RT::LaunchRaySort(L.rays, L.n, L.n_dev, scene->info.bounds_lo, scene->info.bounds_hi,
-                                                cfg.sort_bits, B, ctx->stream);
+                                                cfg.sort_bits, B, stream);
         if (e != cudaSuccess) return e;
         L.order = B.order;
     }
-    return RT::LaunchTraceConfigured(L, any, stats, cfg, grid, ctx->stream);
+    return RT::LaunchTraceConfigured(L, any, stats, cfg, grid, stream);
 }
 
 int ReadStatus(fnd_rt_ctx* ctx) {
@@ -261,6 +263,11 @@ int fnd_rt_destroy(fnd_rt_ctx* ctx) {
     if (ctx->d_rgb) cudaFree(ctx->d_rgb);
     if (ctx->d_sort) cudaFree(ctx->d_sort);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    for (cudaEvent_t e : ctx->pipe_ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
+    if (ctx->compute2) cudaStreamDestroy(ctx->compute2);
+    if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return rc;
@@ -487,6 +494,31 @@ int fnd_rt_scene_destroy(fnd_rt_scene* scene) {
 
 namespace {
 
+// Host-buffer traces of at least two chunks run as a pipeline: chunk k's rays
+// go in on one copy stream while chunk k - 1 is traced and chunk k - 2's hits
+// come back on another, so the copies hide under the traversal. In input
+// order the chunks alternate between the context stream and a second compute
+// stream, each with its own work counter, so a chunk's blocks start on the
+// SMs the previous chunk's last blocks leave; in coherence order (which
+// shares the sort scratch) they all run on the context stream. Chunks of at
+// least 2^19 rays, at most 16 per call.
+constexpr uint32_t kPipeMinChunk = 1u << 19;
+constexpr uint32_t kPipeMaxChunks = 16;
+
+uint32_t PipelineChunk(uint32_t n) {
+    uint32_t chunk = std::max(kPipeMinChunk, (n + 7u) / 8u);
+    chunk = std::max(chunk, (uint32_t)(((uint64_t)n + kPipeMaxChunks - 1) / kPipeMaxChunks));
+    return chunk;
+}
+
+void EnsurePipeline(fnd_rt_ctx* ctx) {
+    if (!ctx->copy_in) CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+    if (!ctx->copy_out) CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+    if (!ctx->compute2) CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->compute2, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : ctx->pipe_ev)
+        if (!e) CUDA_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+}
+
 int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n, void* out, int mem,
               bool any, fnd_rt_trace_stats* stats) {
     if (!ctx) return FND_ERR_INVALID_ARG;
@@ -495,58 +527,101 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
         CHECK(mem == FND_MEM_HOST || mem == FND_MEM_DEVICE);
         CHECK(n == 0 || (rays != nullptr && out != nullptr));
         CHECK_CODE(n <= (1u << 31), FND_ERR_INVALID_ARG, "%u rays exceed the 2^31 limit per call", n);
+        CHECK_CODE(!(scene->two_level && stats), FND_ERR_INVALID_ARG,
+                   "trace statistics are not kept for two-level scenes");
         UseDevice(ctx);
-        const size_t out_bytes = any ? (size_t)n : sizeof(fnd_hit) * (size_t)n;
-        const size_t in_bytes = sizeof(fnd_ray) * (size_t)n;
-        RT::TraceLaunch L{};
-        L.scene = scene->view;
-        L.n = n;
-        L.counter = ctx->d_counter;
-        L.status = ctx->d_status;
-        L.stats = ctx->d_stats;
-        L.refill_min = ctx->refill_min;
+        const size_t hit_bytes = any ? 1 : sizeof(fnd_hit);
+        // one traversal launch over `cnt` device-resident rays on `st` with
+        // work counter `counter`
+        auto launch = [&](const float4* d_rays, uint32_t cnt, void* d_out, cudaStream_t st, uint32_t* counter) {
+            RT::TraceLaunch L{};
+            L.scene = scene->view;
+            L.n = cnt;
+            L.counter = counter;
+            L.status = ctx->d_status;
+            L.stats = ctx->d_stats;
+            L.refill_min = ctx->refill_min;
+            L.rays = d_rays;
+            if (any)
+                L.occluded = static_cast<uint8_t*>(d_out);
+            else
+                L.hits = d_out;
+            if (scene->two_level) {
+                RT::InstancedLaunch I{};
+                I.tlas = scene->view;
+                I.inst = static_cast<const RT::InstanceRec*>(scene->d_instances);
+                I.num_inst = scene->num_instances;
+                I.rays = L.rays;
+                I.n = cnt;
+                I.hits = L.hits;
+                I.occluded = L.occluded;
+                I.counter = counter;
+                I.status = ctx->d_status;
+                if (scene->num_instances == 0) {
+                    RT::TraceLaunch E = L;  // no instances: every ray misses
+                    E.scene = RT::DeviceScene{};
+                    CUDA_CHECK(RT::LaunchTraceConfigured(E, any, false, ctx->trace_cfg, 1, st));
+                } else {
+                    CUDA_CHECK(RT::LaunchInstanced(I, any, ctx->sm_count, st));
+                }
+            } else {
+                const int variant = (any ? 1 : 0) + (stats ? 2 : 0);
+                const int grid = TraceGrid(ctx, ctx->trace_cfg, variant);
+                CUDA_CHECK(LaunchTraceOrdered(ctx, scene, L, any, stats != nullptr, ctx->trace_cfg, grid, st));
+            }
+        };
+        if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
+        bool copied_back = false;
         if (mem == FND_MEM_DEVICE) {
             CHECK_CODE(((uintptr_t)rays & 15u) == 0 && ((uintptr_t)out & (any ? 0u : 7u)) == 0, FND_ERR_INVALID_ARG,
                        "device rays must be 16-byte aligned and hits 8-byte aligned");
-            L.rays = reinterpret_cast<const float4*>(rays);
-            if (any)
-                L.occluded = static_cast<uint8_t*>(out);
-            else
-                L.hits = out;
-        } else {
-            EnsureDevice(ctx->d_in, ctx->d_in_cap, in_bytes);
-            EnsureDevice(ctx->d_out, ctx->d_out_cap, out_bytes);
-            if (n) CUDA_CHECK(cudaMemcpyAsync(ctx->d_in, rays, in_bytes, cudaMemcpyHostToDevice, ctx->stream));
-            L.rays = static_cast<const float4*>(ctx->d_in);
-            if (any)
-                L.occluded = static_cast<uint8_t*>(ctx->d_out);
-            else
-                L.hits = ctx->d_out;
-        }
-        if (scene->two_level) {
-            CHECK_CODE(stats == nullptr, FND_ERR_INVALID_ARG, "trace statistics are not kept for two-level scenes");
-            RT::InstancedLaunch I{};
-            I.tlas = scene->view;
-            I.inst = static_cast<const RT::InstanceRec*>(scene->d_instances);
-            I.num_inst = scene->num_instances;
-            I.rays = L.rays;
-            I.n = n;
-            I.hits = L.hits;
-            I.occluded = L.occluded;
-            I.counter = ctx->d_counter;
-            I.status = ctx->d_status;
-            if (scene->num_instances == 0) {
-                RT::TraceLaunch E = L;  // no instances: every ray misses
-                E.scene = RT::DeviceScene{};
-                CUDA_CHECK(RT::LaunchTraceConfigured(E, any, false, ctx->trace_cfg, 1, ctx->stream));
+            launch(reinterpret_cast<const float4*>(rays), n, out, ctx->stream, ctx->d_counter);
+        } else if (n > 0) {
+            EnsureDevice(ctx->d_in, ctx->d_in_cap, sizeof(fnd_ray) * (size_t)n);
+            EnsureDevice(ctx->d_out, ctx->d_out_cap, hit_bytes * (size_t)n);
+            auto* d_in = static_cast<char*>(ctx->d_in);
+            auto* d_out = static_cast<char*>(ctx->d_out);
+            const uint32_t chunk = PipelineChunk(n);
+            if (stats || n <= chunk) {
+                CUDA_CHECK(cudaMemcpyAsync(d_in, rays, sizeof(fnd_ray) * (size_t)n, cudaMemcpyHostToDevice,
+                                           ctx->stream));
+                launch(reinterpret_cast<const float4*>(d_in), n, d_out, ctx->stream, ctx->d_counter);
             } else {
-                CUDA_CHECK(RT::LaunchInstanced(I, any, ctx->sm_count, ctx->stream));
+                EnsurePipeline(ctx);
+                cudaEvent_t* ev = ctx->pipe_ev;
+                const bool two = ctx->trace_cfg.sort_bits == 0;
+                // the copy and compute streams start after the context
+                // stream's earlier work
+                CUDA_CHECK(cudaEventRecord(ev[0], ctx->stream));
+                CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_in, ev[0], 0));
+                CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_out, ev[0], 0));
+                if (two) CUDA_CHECK(cudaStreamWaitEvent(ctx->compute2, ev[0], 0));
+                const uint32_t chunks = (n + chunk - 1) / chunk;
+                for (uint32_t k = 0; k < chunks; ++k) {
+                    const size_t first = (size_t)k * chunk;
+                    const uint32_t cnt = (uint32_t)std::min<size_t>(chunk, n - first);
+                    cudaEvent_t in_done = ev[2 + 2 * k], traced = ev[3 + 2 * k];
+                    CUDA_CHECK(cudaMemcpyAsync(d_in + sizeof(fnd_ray) * first, rays + first, sizeof(fnd_ray) * cnt,
+                                               cudaMemcpyHostToDevice, ctx->copy_in));
+                    CUDA_CHECK(cudaEventRecord(in_done, ctx->copy_in));
+                    // odd chunks on the second compute stream, with the
+                    // counter 32 bytes further in the counter slot
+                    const bool odd = two && (k & 1u);
+                    cudaStream_t cs = odd ? ctx->compute2 : ctx->stream;
+                    CUDA_CHECK(cudaStreamWaitEvent(cs, in_done, 0));
+                    launch(reinterpret_cast<const float4*>(d_in + sizeof(fnd_ray) * first), cnt,
+                           d_out + hit_bytes * first, cs, ctx->d_counter + (odd ? 8 : 0));
+                    CUDA_CHECK(cudaEventRecord(traced, cs));
+                    CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_out, traced, 0));
+                    CUDA_CHECK(cudaMemcpyAsync(static_cast<char*>(out) + hit_bytes * first, d_out + hit_bytes * first,
+                                               hit_bytes * cnt, cudaMemcpyDeviceToHost, ctx->copy_out));
+                }
+                // the context stream (which the status read below waits on)
+                // covers the last copy back
+                CUDA_CHECK(cudaEventRecord(ev[1], ctx->copy_out));
+                CUDA_CHECK(cudaStreamWaitEvent(ctx->stream, ev[1], 0));
+                copied_back = true;
             }
-        } else {
-            if (stats) CUDA_CHECK(cudaMemsetAsync(ctx->d_stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
-            const int variant = (any ? 1 : 0) + (stats ? 2 : 0);
-            const int grid = TraceGrid(ctx, ctx->trace_cfg, variant);
-            CUDA_CHECK(LaunchTraceOrdered(ctx, scene, L, any, stats != nullptr, ctx->trace_cfg, grid));
         }
         if (stats) {
             unsigned long long h[4] = {0, 0, 0, 0};
@@ -559,7 +634,9 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
             stats->warp_tri_steps = h[3];
         }
         if (mem == FND_MEM_HOST) {
-            if (n) CUDA_CHECK(cudaMemcpyAsync(out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+            if (n && !copied_back)
+                CUDA_CHECK(cudaMemcpyAsync(out, ctx->d_out, hit_bytes * (size_t)n, cudaMemcpyDeviceToHost,
+                                           ctx->stream));
             const int s = ReadStatus(ctx);
             if (s != FND_OK)
                 Fail(s, "device status: %s",

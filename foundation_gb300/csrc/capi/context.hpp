@@ -51,6 +51,10 @@ struct fnd_rt_ctx {
     size_t d_in_cap = 0;
     void* d_out = nullptr;
     size_t d_out_cap = 0;
+    // pipelined FND_MEM_HOST traces: copy streams (created on first use) and
+    // events: [0] start, [1] end, then per chunk "rays in" and "traced"
+    cudaStream_t copy_in = nullptr, copy_out = nullptr, compute2 = nullptr;
+    cudaEvent_t pipe_ev[2 + 2 * 16] = {};
     int live_scenes = 0;
     Foundation::RT::TraceConfig trace_cfg{};  // launch shape of the traversal kernels
     // path-tracing state: path buffers (capacity paths) and the frame buffer
@@ -138,8 +142,10 @@ int TraceGrid(fnd_rt_ctx* ctx, const Foundation::RT::TraceConfig& cfg, int varia
 // Launches a traversal under a launch shape; with cfg.sort_bits the rays
 // (L.n, or *L.n_dev when set) are first put in coherence order over the
 // scene box (context scratch), otherwise taken in input order.
+// `stream` null: the context stream.
 cudaError_t LaunchTraceOrdered(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, Foundation::RT::TraceLaunch L, bool any,
-                               bool stats, const Foundation::RT::TraceConfig& cfg, int grid);
+                               bool stats, const Foundation::RT::TraceConfig& cfg, int grid,
+                               cudaStream_t stream = nullptr);
 
 // One grey Lambertian material table on a new scene (capi_trace.cpp).
 void DefaultMaterial(fnd_rt_scene* scene);

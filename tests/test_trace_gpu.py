@@ -94,6 +94,42 @@ def test_soup_1m_tris(ctx):
     ss.close()
 
 
+def test_pipelined_host_traces_match_device_traces(ctx):
+    """Host-buffer calls of more than 2^19 rays run as a chunked copy / trace /
+    copy pipeline over two copy streams; the results must equal a
+    device-buffer call's, with pinned and pageable host memory, for closest
+    and any hits, in input and in coherence order, including a short last
+    chunk (2,500,000 rays: five chunks of 524,288 and one of 402,848)."""
+    import torch
+    import foundation_gb300 as fg
+    cs = S.cornell_scene(num_spheres=50)
+    sc = ctx.upload(cs.verts, cs.idx)
+    n = 2_500_000
+    rays = S.incoherent_rays(n, *cs.bounds, seed=13)
+    rd = torch.from_numpy(rays).cuda()
+    hd = torch.empty(2 * n, dtype=torch.int32, device="cuda")
+    od = torch.empty(n, dtype=torch.uint8, device="cuda")
+    pin_in = fg.PinnedBuffer(n * 32)
+    pin_out = fg.PinnedBuffer(n * 8)
+    pr = pin_in.view(np.float32, (n, 8))
+    pr[:] = rays
+    ph = pin_out.view(fg.HIT_DTYPE, (n,))
+    for bits in (0, 12):
+        ctx.set_trace_config(sort_bits=bits)
+        torch.cuda.synchronize()
+        sc.closest(rd, hd)
+        sc.any(rd, od)
+        ctx.sync()
+        dev = hd.cpu().numpy().view(np.uint32)
+        occ = od.cpu().numpy()
+        for h in (sc.closest(rays), sc.closest(pr, ph)):
+            assert np.array_equal(h["prim"], dev[0::2])
+            assert np.array_equal(h["t"].view(np.uint32), dev[1::2])
+        assert np.array_equal(sc.any(rays), occ)
+    ctx.set_trace_config()
+    sc.close()
+
+
 def test_device_pointers_and_stats(ctx):
     import torch
     cs = S.cornell_scene(num_spheres=50)
