@@ -96,10 +96,11 @@ def test_soup_1m_tris(ctx):
 
 def test_pipelined_host_traces_match_device_traces(ctx):
     """Host-buffer calls of more than 2^19 rays run as a chunked copy / trace /
-    copy pipeline over two copy streams; the results must equal a
-    device-buffer call's, with pinned and pageable host memory, for closest
-    and any hits, in input and in coherence order, including a short last
-    chunk (2,500,000 rays: five chunks of 524,288 and one of 402,848)."""
+    copy pipeline over two copy streams and two compute streams; the results
+    must equal a device-buffer call's, with pinned and pageable host memory,
+    for closest and any hits, in input and in coherence order, including a
+    short last chunk (2,500,000 rays: four chunks of 524,288 and one of
+    402,848)."""
     import torch
     import foundation_gb300 as fg
     cs = S.cornell_scene(num_spheres=50)
