@@ -106,6 +106,43 @@ __device__ __forceinline__ bool intersect_tri(const RayState& r, float4 v0, floa
     return true;
 }
 
+// Packed FP32 pairs for the child-box test: two slots' plane FMAs in one
+// fma.rm / fma.rp .f32x2 (sm_100 family). Each lane rounds exactly like the
+// scalar __fmaf_rd / __fmaf_ru (tests/test_minmax_gpu.py checks it on the
+// GPU); the host build evaluates the scalar forms.
+struct F2 {
+#if defined(__CUDA_ARCH__)
+    unsigned long long v;
+#else
+    float x, y;
+#endif
+};
+__device__ __forceinline__ F2 pack_f2(float a, float b) {
+    F2 r;
+#if defined(__CUDA_ARCH__)
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+#else
+    r.x = a;
+    r.y = b;
+#endif
+    return r;
+}
+// out = a * b + c per lane, rounded down (kUp false) or up (kUp true)
+template <bool kUp>
+__device__ __forceinline__ void fma_dir_f2(F2 a, F2 b, F2 c, float out[2]) {
+#if defined(__CUDA_ARCH__)
+    unsigned long long d;
+    if (kUp)
+        asm("fma.rp.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a.v), "l"(b.v), "l"(c.v));
+    else
+        asm("fma.rm.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a.v), "l"(b.v), "l"(c.v));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(out[0]), "=f"(out[1]) : "l"(d));
+#else
+    out[0] = kUp ? __fmaf_ru(a.x, b.x, c.x) : __fmaf_rd(a.x, b.x, c.x);
+    out[1] = kUp ? __fmaf_ru(a.y, b.y, c.y) : __fmaf_rd(a.y, b.y, c.y);
+#endif
+}
+
 // Two quantised planes as floats 1024 + q, exactly: one PRMT builds the
 // half2 (0x64 | q) pair (a half with exponent 2^10 and q in its low mantissa
 // bits), and the two halves widen to float off the integer pipe. sel picks
@@ -204,7 +241,11 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
     const float bny = __fmaf_rd(-1024.0f, sy, by), bfy = __fmaf_ru(-1024.0f, sy, by);
     const float bnz = __fmaf_rd(-1024.0f, sz, bz), bfz = __fmaf_ru(-1024.0f, sz, bz);
     // the boxes alone: bit s of hitm for slot s (empty slots included; the
-    // slot kinds below mask them out); two slots per byte pair
+    // slot kinds below mask them out); two slots per byte pair, their plane
+    // FMAs as packed pairs
+    const F2 sx2 = pack_f2(sx, sx), sy2 = pack_f2(sy, sy), sz2 = pack_f2(sz, sz);
+    const F2 bnx2 = pack_f2(bnx, bnx), bny2 = pack_f2(bny, bny), bnz2 = pack_f2(bnz, bnz);
+    const F2 bfx2 = pack_f2(bfx, bfx), bfy2 = pack_f2(bfy, bfy), bfz2 = pack_f2(bfz, bfz);
     uint32_t hitm = 0;
 #pragma unroll
     for (int pr = 0; pr < 4; ++pr) {
@@ -216,17 +257,17 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
         plane_pair(pr < 2 ? gx0 : gx1, sel, q0[3], q1[3]);
         plane_pair(pr < 2 ? gy0 : gy1, sel, q0[4], q1[4]);
         plane_pair(pr < 2 ? gz0 : gz1, sel, q0[5], q1[5]);
+        float tnx[2], tny[2], tnz[2], tfx[2], tfy[2], tfz[2];
+        fma_dir_f2<false>(pack_f2(q0[0], q1[0]), sx2, bnx2, tnx);
+        fma_dir_f2<false>(pack_f2(q0[1], q1[1]), sy2, bny2, tny);
+        fma_dir_f2<false>(pack_f2(q0[2], q1[2]), sz2, bnz2, tnz);
+        fma_dir_f2<true>(pack_f2(q0[3], q1[3]), sx2, bfx2, tfx);
+        fma_dir_f2<true>(pack_f2(q0[4], q1[4]), sy2, bfy2, tfy);
+        fma_dir_f2<true>(pack_f2(q0[5], q1[5]), sz2, bfz2, tfz);
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
-            const float* q = e ? q1 : q0;
-            const float tnx = __fmaf_rd(q[0], sx, bnx);
-            const float tny = __fmaf_rd(q[1], sy, bny);
-            const float tnz = __fmaf_rd(q[2], sz, bnz);
-            const float tfx = __fmaf_ru(q[3], sx, bfx);
-            const float tfy = __fmaf_ru(q[4], sy, bfy);
-            const float tfz = __fmaf_ru(q[5], sz, bfz);
-            const float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
-            const float tf = min3f(tfx, tfy, fminf(tfz, tfar));
+            const float tn = max3f(tnx[e], tny[e], fmaxf(tnz[e], r.tmin));
+            const float tf = min3f(tfx[e], tfy[e], fminf(tfz[e], tfar));
             hitm |= tn <= tf ? 1u << (2 * pr + e) : 0u;
         }
     }
