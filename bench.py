@@ -44,8 +44,9 @@ UNIT = "Mrays/s"
 PROFILES = os.path.join(ROOT, "profiles")
 # Tree of the Cornell blocks (path tracer, cache frames, time to relMSE):
 # binned SAH with spatial splits, split budget 8 (the SAH stops splitting
-# before the budget); hits are those of any other tree.
-CORNELL_BVH = dict(spatial_splits=True, split_budget=8.0)
+# before the budget), collapsed to 8-wide nodes by the SAH-optimal rule; hits
+# are those of any other tree.
+CORNELL_BVH = dict(spatial_splits=True, split_budget=8.0, sah_collapse=True)
 # Radiance cache of the cache blocks: 65,536 training paths per frame (the
 # workload's figure), 8 Adam steps of 16,384 samples at lr 1e-2, queries on
 # the exponential moving average (0.98) of the iterates, GGX alpha below 0.05
@@ -70,6 +71,8 @@ def parse_args():
                    help="tree of the timed scene: binned SAH with spatial splits (default) or binned SAH alone")
     p.add_argument("--split-budget", type=float, default=8.0,
                    help="with --bvh spatial: extra references per triangle the splits may add")
+    p.add_argument("--collapse", default="sah", choices=["sah", "greedy"],
+                   help="binary tree -> 8-wide nodes: SAH-optimal (default) or greedy")
     p.add_argument("--extra", default="path_tracer,incoherent_1m_tris,time_to_relmse_1080p,batched_256_scenes,"
                                       "large_scene_4k",
                    help="comma-separated extra blocks to run (also: cache_frames)")
@@ -272,9 +275,9 @@ def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
     on the reference tree (binned SAH, default launch shape) and on the
     best configuration: spatial splits with a split budget of 4 or 8 extra
     references per triangle (at 8 the builder stops on the SAH before the
-    budget: about 6.4 references per triangle), launch shape and coherence
-    order picked by the autotuner in set-up (the timed launches include the
-    ray-sorting kernels when the tuner chose them)."""
+    budget: about 6.4 references per triangle) and the SAH-optimal collapse,
+    launch shape and coherence order picked by the autotuner in set-up (the
+    timed launches include the ray-sorting kernels when the tuner chose them)."""
     from foundation_gb300 import scenes
     so = scenes.soup_scene(1 << 20, seed=2)
     rays = scenes.incoherent_rays(n_rays, (0, 0, 0), (1, 1, 1), seed=2)
@@ -302,7 +305,7 @@ def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
     s.close()
     best = None
     for budget in (4.0, 8.0):
-        s = ctx.upload(so.verts, so.idx, spatial_splits=True, split_budget=budget)
+        s = ctx.upload(so.verts, so.idx, spatial_splits=True, split_budget=budget, sah_collapse=True)
         cfg, _ = ctx.tune(s, rd, reps=2)
         ctx.set_trace_config(**cfg)
         ms = time_it(s)
@@ -667,6 +670,7 @@ def main():
     stream = torch.cuda.Stream()
     ctx = fg.Context(local, stream=stream.cuda_stream)
     bvh = dict(spatial_splits=True, split_budget=args.split_budget) if args.bvh == "spatial" else {}
+    bvh["sah_collapse"] = args.collapse == "sah"
     scene = ctx.upload(sc.verts, sc.idx, **bvh)
     info = scene.info()
     rd = torch.from_numpy(rays).to("cuda")
@@ -739,10 +743,11 @@ def main():
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(config_block(sc, n, world, args.workload),
-                           bvh=(f"binned SAH 32 bins, <=4 tris/leaf, spatial splits (split budget "
-                                f"{args.split_budget:g}), collapsed to 8-wide compressed nodes"
-                                if args.bvh == "spatial" else
-                                "binned SAH 32 bins, <=4 tris/leaf, collapsed to 8-wide compressed nodes"),
+                           bvh=("binned SAH 32 bins, <=4 tris/leaf" +
+                                (f", spatial splits (split budget {args.split_budget:g})" if args.bvh == "spatial"
+                                 else "") +
+                                (", SAH-optimal collapse" if args.collapse == "sah" else ", greedy collapse") +
+                                " to 8-wide compressed nodes"),
                            roofline_bytes="algorithmic bytes counted by the oracle on the binary binned-SAH tree"),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8,
                     "steps": e2e_steps, "matches_device_result": e2e_ok},

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <memory>
 
 #include "../core/core.hpp"
 
@@ -42,10 +43,137 @@ float HalfArea(const BinaryNode& n) {
     return dx * dy + dy * dz + dz * dx;
 }
 
+// A child of a wide node: a binary subtree that becomes either an internal
+// wide node or one leaf slot holding all of the subtree's triangles.
+struct Kid {
+    uint32_t bnode;
+    bool leaf;
+};
+
+// SAH-optimal collapse (after Ylitie, Karras & Laine 2017): bottom-up over the
+// binary tree, C(n, i) is the least cost of representing n's subtree by at most
+// i roots (wide nodes or leaf slots of at most kMaxLeafTris triangles), with a
+// wide node costing c_node x its half area and a leaf c_tri x half area x its
+// triangles; a wide node's children are the best split of 8 roots between
+// the two binary children.
+class SahCollapse {
+public:
+    SahCollapse(const BinaryBvh& bin, double c_node, double c_tri) : m_bin(bin) {
+        const size_t n = bin.nodes.size();
+        m_cost.assign(8 * n, 0.0f);
+        m_choice.assign(8 * n, 0);
+        m_node_j.assign(n, 0);
+        m_as_leaf.assign(n, 0);
+        std::vector<uint32_t> tris(n, 0);
+        for (size_t k = n; k-- > 0;) {
+            const BinaryNode& b = bin.nodes[k];
+            const double area = (double)HalfArea(b);
+            float* c = &m_cost[8 * k];
+            if (b.count) {
+                tris[k] = b.count;
+                for (int i = 0; i < 8; ++i) c[i] = (float)(area * c_tri * b.count);
+                m_as_leaf[k] = 1;
+                continue;
+            }
+            const uint32_t l = b.a, r = b.a + 1;
+            CHECK_CODE(l > k && r < n, FND_ERR_INVALID_SCENE, "binary tree not in parent-before-child order");
+            tris[k] = tris[l] + tris[r];
+            const float* cl = &m_cost[8 * (size_t)l];
+            const float* cr = &m_cost[8 * (size_t)r];
+            float split[9];
+            uint8_t split_j[9];
+            for (int i = 2; i <= 8; ++i) {
+                split[i] = FLT_MAX;
+                split_j[i] = 1;
+                for (int j = 1; j < i; ++j) {
+                    const float v = cl[j - 1] + cr[i - j - 1];
+                    if (v < split[i]) {
+                        split[i] = v;
+                        split_j[i] = (uint8_t)j;
+                    }
+                }
+            }
+            const float node_cost = (float)(area * c_node) + split[8];
+            m_node_j[k] = split_j[8];
+            c[0] = node_cost;
+            if (tris[k] <= (uint32_t)kMaxLeafTris) {
+                const float leaf_cost = (float)(area * c_tri * tris[k]);
+                if (leaf_cost <= node_cost) {
+                    c[0] = leaf_cost;
+                    m_as_leaf[k] = 1;
+                }
+            }
+            for (int i = 2; i <= 8; ++i) {
+                if (split[i] < c[i - 2]) {
+                    c[i - 1] = split[i];
+                    m_choice[8 * k + i - 1] = split_j[i];
+                } else {
+                    c[i - 1] = c[i - 2];
+                }
+            }
+        }
+    }
+
+    // The children of a wide node made of binary node n.
+    void NodeKids(uint32_t n, Kid* kids, int& nk) const {
+        nk = 0;
+        const BinaryNode& b = m_bin.nodes[n];
+        if (b.count) {
+            kids[nk++] = {n, true};
+            return;
+        }
+        Gather(b.a, m_node_j[n], kids, nk);
+        Gather(b.a + 1, 8 - m_node_j[n], kids, nk);
+    }
+
+private:
+    void Gather(uint32_t n, int k, Kid* kids, int& nk) const {
+        const BinaryNode& b = m_bin.nodes[n];
+        while (k >= 2 && !b.count && m_choice[8 * (size_t)n + k - 1] == 0) --k;
+        if (k >= 2 && !b.count) {
+            const int j = m_choice[8 * (size_t)n + k - 1];
+            Gather(b.a, j, kids, nk);
+            Gather(b.a + 1, k - j, kids, nk);
+            return;
+        }
+        CHECK(nk < kWidth);
+        kids[nk++] = {n, m_as_leaf[n] != 0};
+    }
+
+    const BinaryBvh& m_bin;
+    std::vector<float> m_cost;       // [8 n + i - 1]: C(n, i)
+    std::vector<uint8_t> m_choice;   // [8 n + i - 1], i >= 2: 0 = C(n, i - 1), else roots given to the left child
+    std::vector<uint8_t> m_node_j;   // roots given to the left child when n is a wide node
+    std::vector<uint8_t> m_as_leaf;  // C(n, 1) is a leaf slot
+};
+
+// The triangles (leaf slots) of binary subtree n, in leaf order.
+void SubtreePrims(const BinaryBvh& bin, uint32_t n, uint32_t* out, uint32_t& cnt) {
+    uint32_t stack[64];
+    int sp = 0;
+    stack[sp++] = n;
+    while (sp) {
+        const BinaryNode& b = bin.nodes[stack[--sp]];
+        if (b.count) {
+            for (uint32_t i = 0; i < b.count; ++i) {
+                CHECK_CODE(cnt < (uint32_t)kMaxLeafTris, FND_ERR_INVALID_SCENE, "leaf larger than 4 triangles");
+                out[cnt++] = bin.prims[b.a + i];
+            }
+        } else {
+            CHECK(sp + 2 <= 64);
+            stack[sp++] = b.a + 1;
+            stack[sp++] = b.a;
+        }
+    }
+}
+
 }  // namespace
 
-void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out, float margin_scale) {
+void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out, float margin_scale,
+                    const CollapseOptions& opt) {
     CHECK(!bin.nodes.empty());
+    std::unique_ptr<SahCollapse> sah;
+    if (opt.sah) sah = std::make_unique<SahCollapse>(bin, opt.c_node, opt.c_tri);
     const BinaryNode& root = bin.nodes[0];
     for (int i = 0; i < 3; ++i) {
         out.lo[i] = root.lo[i];
@@ -69,31 +197,36 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
         const Item it = queue.front();
         queue.pop_front();
         out.depth = std::max(out.depth, it.depth);
-        // gather up to 8 children by expanding the largest internal child
-        uint32_t kids[kWidth];
-        int nk = 1;
-        kids[0] = it.bnode;
-        for (;;) {
-            int pick = -1;
-            float best = -1.0f;
-            for (int k = 0; k < nk; ++k) {
-                const BinaryNode& c = bin.nodes[kids[k]];
-                if (c.count) continue;
-                const float a = HalfArea(c);
-                if (a > best) {
-                    best = a;
-                    pick = k;
+        Kid kids[kWidth];
+        int nk = 0;
+        if (sah) {
+            sah->NodeKids(it.bnode, kids, nk);
+        } else {
+            // gather up to 8 children by expanding the largest internal child
+            nk = 1;
+            kids[0] = {it.bnode, bin.nodes[it.bnode].count > 0};
+            for (;;) {
+                int pick = -1;
+                float best = -1.0f;
+                for (int k = 0; k < nk; ++k) {
+                    const BinaryNode& c = bin.nodes[kids[k].bnode];
+                    if (c.count) continue;
+                    const float a = HalfArea(c);
+                    if (a > best) {
+                        best = a;
+                        pick = k;
+                    }
                 }
+                if (pick < 0 || nk == kWidth) break;
+                const uint32_t l = bin.nodes[kids[pick].bnode].a;
+                kids[pick] = {l, bin.nodes[l].count > 0};
+                kids[nk++] = {l + 1, bin.nodes[l + 1].count > 0};
             }
-            if (pick < 0 || nk == kWidth) break;
-            const uint32_t l = bin.nodes[kids[pick]].a;
-            kids[pick] = l;
-            kids[nk++] = l + 1;
         }
         // inflated child boxes and the node box
         float clo[kWidth][3], chi[kWidth][3], nlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, nhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
         for (int k = 0; k < nk; ++k) {
-            const BinaryNode& c = bin.nodes[kids[k]];
+            const BinaryNode& c = bin.nodes[kids[k].bnode];
             for (int a = 0; a < 3; ++a) {
                 clo[k][a] = c.lo[a] - margin;
                 chi[k][a] = c.hi[a] + margin;
@@ -161,7 +294,7 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
         for (int s = 0; s < kWidth; ++s) {
             const int k = child_in_slot[s];
             if (k < 0) continue;
-            const BinaryNode& c = bin.nodes[kids[k]];
+            const BinaryNode& c = bin.nodes[kids[k].bnode];
             for (int a = 0; a < 3; ++a) {
                 const double p = nd.p[a];
                 double ql = std::floor(((double)clo[k][a] - p) / step[a]);
@@ -175,11 +308,13 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
                 nd.qlo[a][s] = (uint8_t)ql;
                 nd.qhi[a][s] = (uint8_t)qh;
             }
-            if (c.count) {
-                CHECK_CODE(c.count <= (uint32_t)kMaxLeafTris, FND_ERR_INVALID_SCENE, "leaf larger than 4 triangles");
-                nd.meta[s] = (uint8_t)(kMetaLeafFlag | ((c.count - 1) << 5) | tri_off);
-                for (uint32_t i = 0; i < c.count; ++i) {
-                    const uint32_t p = bin.prims[c.a + i];
+            if (kids[k].leaf) {
+                uint32_t lp[kMaxLeafTris], lc = 0;
+                SubtreePrims(bin, kids[k].bnode, lp, lc);
+                CHECK_CODE(lc >= 1, FND_ERR_INVALID_SCENE, "empty leaf");
+                nd.meta[s] = (uint8_t)(kMetaLeafFlag | ((lc - 1) << 5) | tri_off);
+                for (uint32_t i = 0; i < lc; ++i) {
+                    const uint32_t p = lp[i];
                     const size_t d = 4 * (size_t)(next_tri + tri_off + i);
                     const float* v = tri + 9 * (size_t)p;
                     uint32_t pid = p;
@@ -194,14 +329,14 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
                     out.v2[d + 1] = v[7];
                     out.v2[d + 2] = v[8];
                 }
-                tri_off += c.count;
+                tri_off += lc;
                 out.leaves++;
             } else {
                 nd.imask |= (uint8_t)(1u << s);
                 nd.meta[s] = kMetaInternal;
                 const uint32_t w = (uint32_t)out.nodes.size();
                 out.nodes.push_back(WideNode{});
-                queue.push_back({kids[k], w, it.depth + 1});
+                queue.push_back({kids[k].bnode, w, it.depth + 1});
             }
         }
         CHECK_CODE(tri_off <= 32, FND_ERR_INVALID_SCENE, "more than 32 triangles under one wide node");

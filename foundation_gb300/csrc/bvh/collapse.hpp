@@ -24,12 +24,20 @@ struct WideBvh {
 // rounding of (p - o) * inv_dir for ray origins within about 50x that size.
 float SceneMargin(const float lo[3], const float hi[3]);
 
+struct CollapseOptions {
+    bool sah = false;     // SAH-optimal collapse instead of the greedy one
+    double c_node = 1.0;  // its cost of a wide-node visit per unit of half area
+    double c_tri = 0.3;   // and of a triangle test (the kernel's best of 0.05 - 1)
+};
+
 // Greedy collapse (largest-surface-area internal child expanded first until 8
-// children), octant-ordered slot assignment, 8-bit outward quantisation.
-// margin_scale multiplies SceneMargin (a bottom-level scene whose instances
-// shrink it far below the world's size needs a wider margin: its object-space
-// ray origins lie further away, see fnd_rt_instances_upload).
-void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out, float margin_scale = 1.0f);
+// children) or SAH-optimal collapse (opt.sah), octant-ordered slot assignment,
+// 8-bit outward quantisation. margin_scale multiplies SceneMargin (a
+// bottom-level scene whose instances shrink it far below the world's size
+// needs a wider margin: its object-space ray origins lie further away, see
+// fnd_rt_instances_upload).
+void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out, float margin_scale = 1.0f,
+                    const CollapseOptions& opt = CollapseOptions{});
 
 }  // namespace RT
 }  // namespace Foundation

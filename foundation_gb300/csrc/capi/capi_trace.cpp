@@ -323,8 +323,14 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         CHECK_CODE(bp.bins >= 2 && bp.bins <= 64, FND_ERR_INVALID_ARG, "sah_bins %u not in [2, 64]", bp.bins);
         CHECK_CODE(bp.max_leaf >= 1 && bp.max_leaf <= 4, FND_ERR_INVALID_ARG, "max_leaf_tris %u not in [1, 4]",
                    bp.max_leaf);
-        CHECK_CODE(!bvh || (bvh->flags & ~(uint32_t)(FND_BVH_SPATIAL_SPLITS | FND_BVH_GPU_BUILD)) == 0,
+        CHECK_CODE(!bvh || (bvh->flags & ~(uint32_t)(FND_BVH_SPATIAL_SPLITS | FND_BVH_GPU_BUILD |
+                                                     FND_BVH_SAH_COLLAPSE)) == 0,
                    FND_ERR_INVALID_ARG, "unknown BVH flags 0x%x", bvh ? bvh->flags : 0u);
+        RT::CollapseOptions copt;
+        copt.sah = bvh && (bvh->flags & FND_BVH_SAH_COLLAPSE);
+        copt.c_tri = bvh && bvh->collapse_tri_cost != 0.0f ? bvh->collapse_tri_cost : 0.3;
+        CHECK_CODE(copt.c_tri > 0.0 && copt.c_tri <= 16.0, FND_ERR_INVALID_ARG, "collapse_tri_cost %g not in (0, 16]",
+                   copt.c_tri);
         const bool gpu_build = bvh && (bvh->flags & FND_BVH_GPU_BUILD);
         CHECK_CODE(!(gpu_build && (bvh->flags & FND_BVH_SPATIAL_SPLITS)), FND_ERR_INVALID_ARG,
                    "FND_BVH_GPU_BUILD does not combine with FND_BVH_SPATIAL_SPLITS");
@@ -406,7 +412,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         scene->info.build_ms = MsSince(t0);
         t0 = std::chrono::steady_clock::now();
         RT::WideBvh wide;
-        RT::CollapseToWide(bin, tri.data(), nt, wide, margin_scale);
+        RT::CollapseToWide(bin, tri.data(), nt, wide, margin_scale, copt);
         scene->info.collapse_ms = MsSince(t0);
         CHECK_CODE(wide.depth <= (uint32_t)RT::kMaxStack / 2, FND_ERR_INVALID_SCENE,
                    "wide BVH depth %u exceeds the traversal stack bound %d", wide.depth, RT::kMaxStack / 2);

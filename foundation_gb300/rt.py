@@ -43,6 +43,7 @@ MAT_LAMBERT, MAT_GGX, MAT_EMISSIVE = 0, 1, 2
 RENDER_ACCUMULATE = 1
 BVH_SPATIAL_SPLITS = 1
 BVH_GPU_BUILD = 2
+BVH_SAH_COLLAPSE = 4
 RENDER_CACHE = 2
 RENDER_WAVEFRONT = 4
 RENDER_TRAIN_ONLY = 8
@@ -64,7 +65,7 @@ class _Desc(C.Structure):
 class _BvhDesc(C.Structure):
     _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("build_threads", C.c_uint32),
                 ("flags", C.c_uint32), ("traversal_cost", C.c_float), ("split_budget", C.c_float),
-                ("margin_scale", C.c_float)]
+                ("margin_scale", C.c_float), ("collapse_tri_cost", C.c_float)]
 
 
 class SceneInfo(C.Structure):
@@ -289,9 +290,10 @@ class Context:
 
     def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0,
                spatial_splits: bool = False, traversal_cost: float = 0.0, gpu_build: bool = False,
-               split_budget: float = 0.0, margin_scale: float = 0.0) -> "Scene":
+               split_budget: float = 0.0, margin_scale: float = 0.0, sah_collapse: bool = False,
+               collapse_tri_cost: float = 0.0) -> "Scene":
         return Scene(self, verts, idx, bins, max_leaf, threads, spatial_splits, traversal_cost, gpu_build,
-                     split_budget, margin_scale)
+                     split_budget, margin_scale, sah_collapse, collapse_tri_cost)
 
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
@@ -439,13 +441,15 @@ class Context:
 
 class Scene:
     def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0, spatial_splits=False,
-                 traversal_cost=0.0, gpu_build=False, split_budget=0.0, margin_scale=0.0):
+                 traversal_cost=0.0, gpu_build=False, split_budget=0.0, margin_scale=0.0, sah_collapse=False,
+                 collapse_tri_cost=0.0):
         self._h = None
         self.ctx = ctx
         v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
-        flags = (BVH_SPATIAL_SPLITS if spatial_splits else 0) | (BVH_GPU_BUILD if gpu_build else 0)
-        bd = _BvhDesc(bins, max_leaf, threads, flags, traversal_cost, split_budget, margin_scale)
+        flags = ((BVH_SPATIAL_SPLITS if spatial_splits else 0) | (BVH_GPU_BUILD if gpu_build else 0) |
+                 (BVH_SAH_COLLAPSE if sah_collapse else 0))
+        bd = _BvhDesc(bins, max_leaf, threads, flags, traversal_cost, split_budget, margin_scale, collapse_tri_cost)
         h = C.c_void_p()
         _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),
                ctx.handle)

@@ -86,7 +86,7 @@ typedef struct fnd_rt_bvh_desc {
     uint32_t sah_bins;      /* 2..64, default 32 */
     uint32_t max_leaf_tris; /* 1..4, default 4 */
     uint32_t build_threads; /* 0: all host cores */
-    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD or 0 */
+    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD, FND_BVH_SAH_COLLAPSE or 0 */
     float traversal_cost;   /* SAH cost of a traversal step relative to a triangle
                                test, (0, 64]; 0: default 1 (the reference tree) */
     float split_budget;     /* FND_BVH_SPATIAL_SPLITS: references the splits may add,
@@ -97,6 +97,9 @@ typedef struct fnd_rt_bvh_desc {
     float margin_scale;     /* box inflation relative to the default (2^-16 of the scene
                                size), [1, 2^16]; 0: 1. A scene instanced at a scale far below
                                the world's needs more (fnd_rt_instances_upload checks it) */
+    float collapse_tri_cost; /* FND_BVH_SAH_COLLAPSE: cost of a triangle test relative to a
+                               wide-node visit, (0, 16]; 0: default 0.3 (the fastest of
+                               0.05 - 1 on the traversal kernel) */
 } fnd_rt_bvh_desc;
 
 /* Spatial splits (Stich et al. 2009): references of triangles that straddle
@@ -111,6 +114,11 @@ enum { FND_BVH_SPATIAL_SPLITS = 1u };
  * are identical. Up to 2^27 triangles; not combined with spatial splits;
  * build_threads is ignored. */
 enum { FND_BVH_GPU_BUILD = 2u };
+/* Collapse the binary tree into 8-wide nodes by the SAH-optimal dynamic
+ * programme (Ylitie, Karras & Laine 2017) instead of the greedy rule: fuller
+ * nodes, small subtrees merged into leaf slots of up to 4 triangles. Host
+ * builds only; hits are identical either way. */
+enum { FND_BVH_SAH_COLLAPSE = 4u };
 
 typedef struct fnd_rt_scene_info {
     uint32_t num_tris;

@@ -145,6 +145,35 @@ emu_bvh* emu_build_sbvh(const float* verts, uint32_t nv, const uint32_t* idx, ui
     return e;
 }
 
+// Binned SAH (spatial: with spatial splits at split budget 8) collapsed by the
+// SAH-optimal rule with triangle cost c_tri.
+emu_bvh* emu_build_sah_collapse(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, int spatial,
+                                double c_tri) {
+    auto* e = new emu_bvh();
+    std::vector<float> tri(9 * (size_t)nt);
+    for (uint32_t t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) tri[9 * (size_t)t + 3 * k + c] = verts[3 * (size_t)idx[3 * (size_t)t + k] + c];
+    BuildParams p;
+    p.max_refs_factor = 8.0;
+    if (spatial)
+        BuildBinarySbvh(tri.data(), nt, p, e->bin);
+    else
+        BuildBinaryBvh(tri.data(), nt, p, e->bin);
+    CollapseOptions o;
+    o.sah = true;
+    o.c_tri = c_tri;
+    CollapseToWide(e->bin, tri.data(), nt, e->wide, 1.0f, o);
+    e->view.nodes = reinterpret_cast<const uint4*>(e->wide.nodes.data());
+    e->view.v0 = reinterpret_cast<const float4*>(e->wide.v0.data());
+    e->view.v1 = reinterpret_cast<const float4*>(e->wide.v1.data());
+    e->view.v2 = reinterpret_cast<const float4*>(e->wide.v2.data());
+    e->view.num_nodes = (uint32_t)e->wide.nodes.size();
+    e->view.num_tris = (uint32_t)e->bin.prims.size();
+    (void)nv;
+    return e;
+}
+
 // Leaf references (triangles, plus the duplicates spatial splits added).
 uint64_t emu_num_refs(const emu_bvh* e) { return e->bin.prims.size(); }
 

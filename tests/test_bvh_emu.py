@@ -27,6 +27,8 @@ def emu(built):
     L.emu_build_sbvh.argtypes = [P, C.c_uint32, P, C.c_uint32, C.c_float]
     L.emu_num_refs.restype = C.c_uint64
     L.emu_num_refs.argtypes = [P]
+    L.emu_build_sah_collapse.restype = P
+    L.emu_build_sah_collapse.argtypes = [P, C.c_uint32, P, C.c_uint32, C.c_int, C.c_double]
     return L
 
 
@@ -154,6 +156,32 @@ def test_emulated_spatial_split_bvh_matches_oracle(emu, case, budget):
     b = O.OracleBVH(sc.verts, sc.idx)
     st = e.stats()
     assert st["wide_depth"] <= 32
+    prim, tbits, _ = e.trace(rays)
+    ref = b.closest(rays)
+    assert np.array_equal(prim, ref["prim"])
+    assert np.array_equal(tbits, ref["t"].view(np.uint32))
+    prim_a, _, _ = e.trace(rays, any_hit=True)
+    assert np.array_equal((prim_a != 0xFFFFFFFF).astype(np.uint8), b.any(rays))
+
+
+@pytest.mark.parametrize("spatial", [0, 1])
+@pytest.mark.parametrize("case", ["soup", "cornell_incoherent"])
+def test_emulated_sah_collapse_matches_oracle(emu, case, spatial):
+    """The SAH-optimal collapse (fuller wide nodes, small subtrees merged into
+    leaf slots of up to 4 triangles) gives the oracle's hits, with fewer wide
+    nodes than the greedy collapse."""
+    sc, rays = CASES[case]()
+    v = np.ascontiguousarray(sc.verts, np.float32)
+    f = np.ascontiguousarray(sc.idx, np.uint32)
+    e = Emu.__new__(Emu)
+    e.L, e.v, e.f = emu, v, f
+    e.h = emu.emu_build_sah_collapse(_p(v), len(v), _p(f), len(f), spatial, 0.3)
+    st = e.stats()
+    assert st["wide_depth"] <= 32
+    greedy = Emu(emu, sc.verts, sc.idx).stats() if not spatial else None
+    if greedy:
+        assert st["wide_nodes"] < greedy["wide_nodes"]
+    b = O.OracleBVH(sc.verts, sc.idx)
     prim, tbits, _ = e.trace(rays)
     ref = b.closest(rays)
     assert np.array_equal(prim, ref["prim"])

@@ -60,6 +60,13 @@ def test_cornell_incoherent_and_camera(ctx):
     assert np.array_equal(sc.any(ir), b.any(ir))
     cr = S.camera_rays(480, 270, **S.CORNELL_CAMERA)
     assert_same(sc.closest(cr), b.closest(cr))
+    # spatial splits + the SAH-optimal collapse (the measured tree): same hits
+    ss = ctx.upload(cs.verts, cs.idx, spatial_splits=True, split_budget=8.0, sah_collapse=True,
+                    collapse_tri_cost=0.3)
+    assert ss.info()["num_wide_nodes"] < sc.info()["num_wide_nodes"]
+    assert_same(ss.closest(ir), b.closest(ir))
+    assert np.array_equal(ss.any(ir), b.any(ir))
+    ss.close()
     g = np.load(os.path.join(GOLDEN, "cornell_rows.npz"))
     h = sc.closest(g["rays"])
     assert np.array_equal(h["prim"], g["prim"])
@@ -87,7 +94,7 @@ def test_soup_1m_tris(ctx):
     ss.close()
     # an uncapped split budget (about 6.4 references per triangle here): the
     # tree the 1M-triangle throughput figure is measured on
-    ss = ctx.upload(so.verts, so.idx, spatial_splits=True, split_budget=8.0)
+    ss = ctx.upload(so.verts, so.idx, spatial_splits=True, split_budget=8.0, sah_collapse=True)
     assert ss.info()["num_refs"] > 5 * len(so.idx)
     assert_same(ss.closest(rays), ref)
     assert np.array_equal(ss.any(rays), b.any(rays))
