@@ -416,7 +416,8 @@ def batched_block(fg, torch, stream, local, num_scenes: int = 256, reps: int = 5
     closest-hit rays) and as many any-hit shadow segments, all served by ONE
     persistent launch over the job table, replayed from a CUDA graph, launch
     shape picked by the autotuner. The scenes are generated on the host cores
-    (spawned workers, one scene each; identical to the serial generator)."""
+    (spawned workers, one scene each; identical to the serial generator) and
+    built with binned SAH and the SAH-optimal collapse."""
     import concurrent.futures as cf
     import multiprocessing as mp
     from foundation_gb300 import scenes
@@ -430,7 +431,7 @@ def batched_block(fg, torch, stream, local, num_scenes: int = 256, reps: int = 5
     t0 = time.perf_counter()
     jobs, tris = [], 0
     for w in work:
-        s = ctx.upload(w["scene"].verts, w["scene"].idx)
+        s = ctx.upload(w["scene"].verts, w["scene"].idx, sah_collapse=True)
         tris += w["scene"].num_tris
         for kind, rays in ((0, w["closest"]), (1, w["any"])):
             rd = torch.from_numpy(rays).to("cuda")
@@ -467,8 +468,9 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
     """Config 5: heightfield terrain (2237^2 vertices, 8-octave value noise,
     seed 3) plus 4,096 level-4 icospheres, 30,970,912 triangles, lit by a
     directional sun and a constant sky; 3840x2160, max depth 6, RR from
-    bounce 3. Reported: the host build, incoherent closest-hit throughput on
-    the scene, the plain tracer's 16-spp frame, and the radiance cache
+    bounce 3. Reported: the host build (binned SAH, SAH-optimal collapse),
+    incoherent closest-hit throughput on the scene, the plain tracer's 16-spp
+    frame, and the radiance cache
     (training-only warm-up frames, then 1-spp frames) given the same wall
     time; both scored by relMSE against a plain render of `ref_spp` spp."""
     from foundation_gb300 import convergence as CV
@@ -478,7 +480,7 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
     gen_s = time.perf_counter() - t0
     ctx = fg.Context(local, stream=stream.cuda_stream)
     t0 = time.perf_counter()
-    s = ctx.upload(tr.verts, tr.idx)
+    s = ctx.upload(tr.verts, tr.idx, sah_collapse=True)
     upload_s = time.perf_counter() - t0
     info = s.info()
     s.set_materials(tr.tri_material, scenes.material_records(tr))
