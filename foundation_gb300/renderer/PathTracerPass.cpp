@@ -36,7 +36,11 @@ void PathTracerPass::SetScene(const SceneDesc& s) {
         Check(fnd_rt_scene_destroy(m_scene), "fnd_rt_scene_destroy");
         m_scene = nullptr;
     }
-    fnd_rt_bvh_desc b{s.sah_bins, s.max_leaf_tris, 0, 0};
+    fnd_rt_bvh_desc b{};
+    b.sah_bins = s.sah_bins;
+    b.max_leaf_tris = s.max_leaf_tris;
+    b.flags = s.bvh_flags;
+    b.split_budget = s.split_budget;
     Check(fnd_rt_scene_upload(m_ctx, s.verts.data(), (uint32_t)(s.verts.size() / 3), s.indices.data(), nt, &b, &m_scene),
           "fnd_rt_scene_upload");
     Check(fnd_rt_scene_info_get(m_scene, &m_info), "fnd_rt_scene_info_get");

@@ -38,6 +38,11 @@ struct SceneDesc {
     std::span<const fnd_quad_light> lights;
     uint32_t sah_bins = 32;
     uint32_t max_leaf_tris = 4;
+    // FND_BVH_* flags of the upload. The SAH-optimal collapse costs little at
+    // build time and traces faster; add FND_BVH_SPATIAL_SPLITS (with a split
+    // budget, 8 lets the SAH decide) for scenes of long, overlapping triangles.
+    uint32_t bvh_flags = FND_BVH_SAH_COLLAPSE;
+    float split_budget = 0.0f;
 };
 
 class PathTracerPass {
