@@ -355,7 +355,8 @@ def cache_frames_block(fg, torch, stream, local, frames: int = 8):
               for f in range(frames)]
     st = ctx.render_stats()
     ctx.close()
-    return {"workload": "cornell200 1920x1080, cache frames (65,536 training paths, 8 x 16,384-sample steps, weight average 0.98)",
+    return {"workload": "cornell200 1920x1080, cache frames (65,536 training paths, 8 x 16,384-sample steps, "
+                        "weight average 0.98)",
             "train_only_ms": float(np.median(train)), "cache_frame_ms": float(np.median(render)),
             "extension_rays_last": st["extension_rays"], "shadow_rays_last": st["shadow_rays"]}
 

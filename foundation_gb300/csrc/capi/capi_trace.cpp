@@ -597,38 +597,53 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
                 launch(reinterpret_cast<const float4*>(d_in), n, d_out, ctx->stream, ctx->d_counter);
             } else {
                 EnsurePipeline(ctx);
-                cudaEvent_t* ev = ctx->pipe_ev;
-                const bool two = ctx->trace_cfg.sort_bits == 0;
-                // the copy and compute streams start after the context
-                // stream's earlier work
-                CUDA_CHECK(cudaEventRecord(ev[0], ctx->stream));
-                CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_in, ev[0], 0));
-                CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_out, ev[0], 0));
-                if (two) CUDA_CHECK(cudaStreamWaitEvent(ctx->compute2, ev[0], 0));
-                const uint32_t chunks = (n + chunk - 1) / chunk;
-                for (uint32_t k = 0; k < chunks; ++k) {
-                    const size_t first = (size_t)k * chunk;
-                    const uint32_t cnt = (uint32_t)std::min<size_t>(chunk, n - first);
-                    cudaEvent_t in_done = ev[2 + 2 * k], traced = ev[3 + 2 * k];
-                    CUDA_CHECK(cudaMemcpyAsync(d_in + sizeof(fnd_ray) * first, rays + first, sizeof(fnd_ray) * cnt,
-                                               cudaMemcpyHostToDevice, ctx->copy_in));
-                    CUDA_CHECK(cudaEventRecord(in_done, ctx->copy_in));
-                    // odd chunks on the second compute stream, with the
-                    // counter 32 bytes further in the counter slot
-                    const bool odd = two && (k & 1u);
-                    cudaStream_t cs = odd ? ctx->compute2 : ctx->stream;
-                    CUDA_CHECK(cudaStreamWaitEvent(cs, in_done, 0));
-                    launch(reinterpret_cast<const float4*>(d_in + sizeof(fnd_ray) * first), cnt,
-                           d_out + hit_bytes * first, cs, ctx->d_counter + (odd ? 8 : 0));
-                    CUDA_CHECK(cudaEventRecord(traced, cs));
-                    CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_out, traced, 0));
-                    CUDA_CHECK(cudaMemcpyAsync(static_cast<char*>(out) + hit_bytes * first, d_out + hit_bytes * first,
-                                               hit_bytes * cnt, cudaMemcpyDeviceToHost, ctx->copy_out));
+                // on a failure part-way, the copies already queued on the
+                // library's streams still read and write the caller's host
+                // buffers: let them finish before the error returns
+                auto drain = [&] {
+                    cudaStreamSynchronize(ctx->copy_in);
+                    cudaStreamSynchronize(ctx->compute2);
+                    cudaStreamSynchronize(ctx->stream);
+                    cudaStreamSynchronize(ctx->copy_out);
+                };
+                try {
+                    cudaEvent_t* ev = ctx->pipe_ev;
+                    const bool two = ctx->trace_cfg.sort_bits == 0;
+                    // the copy and compute streams start after the context
+                    // stream's earlier work
+                    CUDA_CHECK(cudaEventRecord(ev[0], ctx->stream));
+                    CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_in, ev[0], 0));
+                    CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_out, ev[0], 0));
+                    if (two) CUDA_CHECK(cudaStreamWaitEvent(ctx->compute2, ev[0], 0));
+                    const uint32_t chunks = (n + chunk - 1) / chunk;
+                    for (uint32_t k = 0; k < chunks; ++k) {
+                        const size_t first = (size_t)k * chunk;
+                        const uint32_t cnt = (uint32_t)std::min<size_t>(chunk, n - first);
+                        cudaEvent_t in_done = ev[2 + 2 * k], traced = ev[3 + 2 * k];
+                        CUDA_CHECK(cudaMemcpyAsync(d_in + sizeof(fnd_ray) * first, rays + first,
+                                                   sizeof(fnd_ray) * cnt, cudaMemcpyHostToDevice, ctx->copy_in));
+                        CUDA_CHECK(cudaEventRecord(in_done, ctx->copy_in));
+                        // odd chunks on the second compute stream, with the
+                        // counter 32 bytes further in the counter slot
+                        const bool odd = two && (k & 1u);
+                        cudaStream_t cs = odd ? ctx->compute2 : ctx->stream;
+                        CUDA_CHECK(cudaStreamWaitEvent(cs, in_done, 0));
+                        launch(reinterpret_cast<const float4*>(d_in + sizeof(fnd_ray) * first), cnt,
+                               d_out + hit_bytes * first, cs, ctx->d_counter + (odd ? 8 : 0));
+                        CUDA_CHECK(cudaEventRecord(traced, cs));
+                        CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_out, traced, 0));
+                        CUDA_CHECK(cudaMemcpyAsync(static_cast<char*>(out) + hit_bytes * first,
+                                                   d_out + hit_bytes * first, hit_bytes * cnt,
+                                                   cudaMemcpyDeviceToHost, ctx->copy_out));
+                    }
+                    // the context stream (which the status read below waits
+                    // on) covers the last copy back
+                    CUDA_CHECK(cudaEventRecord(ev[1], ctx->copy_out));
+                    CUDA_CHECK(cudaStreamWaitEvent(ctx->stream, ev[1], 0));
+                } catch (...) {
+                    drain();
+                    throw;
                 }
-                // the context stream (which the status read below waits on)
-                // covers the last copy back
-                CUDA_CHECK(cudaEventRecord(ev[1], ctx->copy_out));
-                CUDA_CHECK(cudaStreamWaitEvent(ctx->stream, ev[1], 0));
                 copied_back = true;
             }
         }
