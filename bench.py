@@ -722,9 +722,12 @@ def main():
     if world > 1:
         dist.barrier()
     e2e_steps = max(3, args.steps // 4)
+    per_call = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        t1 = time.perf_counter()
         scene.closest(hr, ho)
+        per_call.append(time.perf_counter() - t1)
     e2e_s = time.perf_counter() - t0
     e2e_value = replicas.job_rate(n, e2e_steps, world, replicas.max_over_ranks(e2e_s, dist, "cuda"))
     # spot-check the end-to-end result against the device result
@@ -753,7 +756,9 @@ def main():
                                 " to 8-wide compressed nodes"),
                            roofline_bytes="algorithmic bytes counted by the oracle on the binary binned-SAH tree"),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8,
-                    "steps": e2e_steps, "matches_device_result": e2e_ok},
+                    "steps": e2e_steps, "matches_device_result": e2e_ok,
+                    "ms_per_call": {"min": 1e3 * min(per_call), "median": 1e3 * float(np.median(per_call)),
+                                    "max": 1e3 * max(per_call)}},
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,

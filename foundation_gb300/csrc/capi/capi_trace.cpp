@@ -507,7 +507,8 @@ namespace {
 // stream, each with its own work counter, so a chunk's blocks start on the
 // SMs the previous chunk's last blocks leave; in coherence order (which
 // shares the sort scratch) they all run on the context stream. Chunks of at
-// least 2^19 rays, 8 per call at 2^22 rays and above, at most 16 per call.
+// least 2^19 rays, 8 per call at 2^22 rays and above, plus a first chunk of a
+// quarter of that size, so at most 17 per call.
 // Per chunk the launch, its tail and the stream waits cost more than the
 // shorter uncovered first copy saves below 2^20 rays per chunk (measured:
 // 8.4M rays in 8 chunks 2.74 ms, in 16 chunks 2.91 ms per call).
@@ -615,10 +616,14 @@ int TraceImpl(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ray* rays, u
                     CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_in, ev[0], 0));
                     CUDA_CHECK(cudaStreamWaitEvent(ctx->copy_out, ev[0], 0));
                     if (two) CUDA_CHECK(cudaStreamWaitEvent(ctx->compute2, ev[0], 0));
-                    const uint32_t chunks = (n + chunk - 1) / chunk;
+                    // chunk 0 is a quarter of the others: its copy in is
+                    // the part of the copies no traversal covers
+                    const uint32_t c0 = chunk / 4;
+                    const uint32_t chunks = 1 + (n - c0 + chunk - 1) / chunk;
+                    CHECK(2 + 2 * (size_t)chunks <= sizeof(ctx->pipe_ev) / sizeof(ctx->pipe_ev[0]));
                     for (uint32_t k = 0; k < chunks; ++k) {
-                        const size_t first = (size_t)k * chunk;
-                        const uint32_t cnt = (uint32_t)std::min<size_t>(chunk, n - first);
+                        const size_t first = k == 0 ? 0 : (size_t)c0 + (size_t)(k - 1) * chunk;
+                        const uint32_t cnt = (uint32_t)std::min<size_t>(k == 0 ? c0 : chunk, n - first);
                         cudaEvent_t in_done = ev[2 + 2 * k], traced = ev[3 + 2 * k];
                         CUDA_CHECK(cudaMemcpyAsync(d_in + sizeof(fnd_ray) * first, rays + first,
                                                    sizeof(fnd_ray) * cnt, cudaMemcpyHostToDevice, ctx->copy_in));

@@ -53,8 +53,9 @@ struct fnd_rt_ctx {
     size_t d_out_cap = 0;
     // pipelined FND_MEM_HOST traces: copy streams (created on first use) and
     // events: [0] start, [1] end, then per chunk "rays in" and "traced"
+    // (at most 17 chunks: a short first chunk and 16 more)
     cudaStream_t copy_in = nullptr, copy_out = nullptr, compute2 = nullptr;
-    cudaEvent_t pipe_ev[2 + 2 * 16] = {};
+    cudaEvent_t pipe_ev[2 + 2 * 17] = {};
     int live_scenes = 0;
     Foundation::RT::TraceConfig trace_cfg{};  // launch shape of the traversal kernels
     // path-tracing state: path buffers (capacity paths) and the frame buffer

@@ -106,8 +106,8 @@ def test_pipelined_host_traces_match_device_traces(ctx):
     copy pipeline over two copy streams and two compute streams; the results
     must equal a device-buffer call's, with pinned and pageable host memory,
     for closest and any hits, in input and in coherence order, including a
-    short last chunk (2,500,000 rays: four chunks of 524,288 and one of
-    402,848)."""
+    short first and last chunk (2,500,000 rays: one chunk of 131,072, four of
+    524,288 and one of 271,776)."""
     import torch
     import foundation_gb300 as fg
     cs = S.cornell_scene(num_spheres=50)
