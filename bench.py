@@ -506,7 +506,7 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
     trace_ms = sum(timed(lambda: s.closest(rd, hd)) for _ in range(5)) / 5
     # the same scene built on the GPU (linear BVH + device collapse)
     t0 = time.perf_counter()
-    g = ctx.upload(tr.verts, tr.idx, gpu_build=True)
+    g = ctx.upload(tr.verts, tr.idx, gpu_build=True, sah_collapse=True)
     gpu_upload_s = time.perf_counter() - t0
     ginfo = g.info()
     for _ in range(2):
@@ -571,7 +571,7 @@ def instanced_terrain(fg, ctx, tr, W, H, cam, kw, ref, spp, timed):
     rad = 0.001 + g.next_f64() * 0.009
     cy = scenes.value_noise(cx, cz, 3) + 0.5 * rad
     t0 = time.perf_counter()
-    terrain = ctx.upload(tr.verts[:grid * grid], tr.idx[:n_terrain], gpu_build=True)
+    terrain = ctx.upload(tr.verts[:grid * grid], tr.idx[:n_terrain], gpu_build=True, sah_collapse=True)
     sphere = ctx.upload(sv.astype(np.float32), sf, margin_scale=64)
     inst = [(terrain, np.eye(3, 4, dtype=np.float32), 0)]
     for k in range(n_inst):

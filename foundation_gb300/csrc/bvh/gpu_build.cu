@@ -16,10 +16,15 @@
 //     finishes it): box, triangle count and the SAH decision
 //     cost(n) = min(N A, C_trav A + cost(l) + cost(r)), a subtree of at most
 //     max_leaf triangles becoming one leaf when that is not dearer;
-//  6. collapse to 8-wide nodes, one wide level per launch: the greedy rule of
-//     collapse.cpp (expand the largest-area internal child until 8), octant
-//     slots, margin inflation and outward quantisation in double precision
-//     as on the host, children and leaf triangles allocated with atomics.
+//     With the SAH-optimal collapse the same walk also computes, per node,
+//     the costs C(n, i) of representing its subtree by at most i roots (wide
+//     nodes or leaf slots of up to 4 triangles) and their decisions, as
+//     collapse.cpp does on the host;
+//  6. collapse to 8-wide nodes, one wide level per launch: the children by
+//     the greedy rule of collapse.cpp (expand the largest-area internal child
+//     until 8) or by those decisions, octant slots, margin inflation and
+//     outward quantisation in double precision as on the host, children and
+//     leaf triangles allocated with atomics.
 #include "gpu_build.hpp"
 
 #include <algorithm>
@@ -64,6 +69,12 @@ struct Buffers {
     uint32_t* status;
     uint32_t* counters;           // [0] nodes, [1] tris, [2] leaves, [4..] per-level queue counts
     uint2 *qa, *qb;               // collapse queues (binary ref, wide node)
+    // SAH-optimal collapse (null: greedy), per internal node k:
+    float* dpc;                   // [8 k + i - 1]: C(k, i), least cost of k's subtree as at most i roots
+    uint8_t* dpch;                // [8 k + i - 1], i >= 2: 0 = C(k, i - 1), else roots given to the left child
+    uint8_t* dpj;                 // roots given to the left child when k is a wide node
+    uint8_t* dpleaf;              // C(k, 1) is one leaf slot
+    float c_tri;                  // cost of a triangle test relative to a wide-node visit
 };
 
 __device__ __forceinline__ void atomic_min_f(float* a, float v) {
@@ -377,6 +388,20 @@ __device__ __forceinline__ RefBox ref_box(const Buffers& B, uint32_t ref) {
     return r;
 }
 
+// C(ref, 1..8) of a child: a single-triangle leaf costs c_tri x its half area
+// whatever the number of roots.
+__device__ __forceinline__ void dp_child(const Buffers& B, uint32_t ref, float c[8]) {
+    if (ref & kLeafRef) {
+        const uint32_t t = B.vals[ref & ~kLeafRef];
+        const float v = B.c_tri * half_area(B.blo[t], B.bhi[t]);
+        for (int i = 0; i < 8; ++i) c[i] = v;
+    } else {
+        const float4 a = __ldcg(reinterpret_cast<const float4*>(B.dpc + 8 * (size_t)ref));
+        const float4 b = __ldcg(reinterpret_cast<const float4*>(B.dpc + 8 * (size_t)ref) + 1);
+        c[0] = a.x, c[1] = a.y, c[2] = a.z, c[3] = a.w, c[4] = b.x, c[5] = b.y, c[6] = b.z, c[7] = b.w;
+    }
+}
+
 __global__ void __launch_bounds__(256) refit_kernel(uint32_t n, Buffers B, uint32_t max_leaf, float trav_cost) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || n < 2) return;
@@ -401,6 +426,50 @@ __global__ void __launch_bounds__(256) refit_kernel(uint32_t n, Buffers B, uint3
         B.nhi[p] = hi;
         B.ncount[p] = cnt | (leaf ? kLeafNode : 0u);
         B.ncost[p] = leaf ? (float)cnt * a : split;
+        if (B.dpc) {
+            // SAH-optimal collapse: wide node at cost a, leaf slot at c_tri a cnt
+            float cl[8], cr[8], sp[9];
+            uint8_t sj[9];
+            dp_child(B, B.left[p], cl);
+            dp_child(B, B.right[p], cr);
+            for (int i = 2; i <= 8; ++i) {
+                sp[i] = FLT_MAX;
+                sj[i] = 1;
+                for (int j = 1; j < i; ++j) {
+                    const float v = cl[j - 1] + cr[i - j - 1];
+                    if (v < sp[i]) {
+                        sp[i] = v;
+                        sj[i] = (uint8_t)j;
+                    }
+                }
+            }
+            float c[8];
+            const float node_cost = a + sp[8];
+            c[0] = node_cost;
+            uint8_t as_leaf = 0;
+            if (cnt <= (uint32_t)kMaxLeafTris) {
+                const float leaf_cost = B.c_tri * a * (float)cnt;
+                if (leaf_cost <= node_cost) {
+                    c[0] = leaf_cost;
+                    as_leaf = 1;
+                }
+            }
+            uint8_t ch[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int i = 2; i <= 8; ++i) {
+                if (sp[i] < c[i - 2]) {
+                    c[i - 1] = sp[i];
+                    ch[i - 1] = sj[i];
+                } else {
+                    c[i - 1] = c[i - 2];
+                }
+            }
+            float4* dc = reinterpret_cast<float4*>(B.dpc + 8 * (size_t)p);
+            dc[0] = make_float4(c[0], c[1], c[2], c[3]);
+            dc[1] = make_float4(c[4], c[5], c[6], c[7]);
+            for (int i = 0; i < 8; ++i) B.dpch[8 * (size_t)p + i] = ch[i];
+            B.dpj[p] = sj[8];
+            B.dpleaf[p] = as_leaf;
+        }
         p = B.parent_i[p];
     }
 }
@@ -425,9 +494,38 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
     for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < count; it += gridDim.x * blockDim.x) {
         const uint2 item = qin[it];
         uint32_t kids[kWidth];
+        bool dp_leaf[kWidth];
         int nk = 1;
         kids[0] = item.x;
+        if (B.dpc && !(item.x & kLeafRef)) {
+            // the children the SAH-optimal decisions give wide node item.x
+            uint2 st[16];
+            int sp = 0;
+            const uint32_t j = B.dpj[item.x];
+            st[sp++] = make_uint2(B.right[item.x], 8u - j);
+            st[sp++] = make_uint2(B.left[item.x], j);
+            nk = 0;
+            while (sp > 0) {
+                const uint2 e = st[--sp];
+                uint32_t k = e.y;
+                if (!(e.x & kLeafRef))
+                    while (k >= 2u && B.dpch[8 * (size_t)e.x + k - 1] == 0) --k;
+                if (!(e.x & kLeafRef) && k >= 2u && sp + 2 <= 16) {
+                    const uint32_t jj = B.dpch[8 * (size_t)e.x + k - 1];
+                    st[sp++] = make_uint2(B.right[e.x], k - jj);
+                    st[sp++] = make_uint2(B.left[e.x], jj);
+                } else if (nk < kWidth) {
+                    kids[nk] = e.x;
+                    dp_leaf[nk] = (e.x & kLeafRef) || B.dpleaf[e.x];
+                    nk++;
+                } else {
+                    atomicOr(B.status, 8u);  // more than 8 roots: malformed decisions
+                    break;
+                }
+            }
+        }
         for (;;) {
+            if (B.dpc && !(item.x & kLeafRef)) break;
             int pick = -1;
             float best = -1.0f;
             for (int c = 0; c < nk; ++c) {
@@ -464,7 +562,7 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
                 lo = __ldcg(B.nlo + kids[c]);
                 hi = __ldcg(B.nhi + kids[c]);
                 const uint32_t w = __ldcg(B.ncount + kids[c]);
-                is_leaf[c] = (w & kLeafNode) != 0u;
+                is_leaf[c] = (B.dpc && !(item.x & kLeafRef)) ? dp_leaf[c] : (w & kLeafNode) != 0u;
                 cnt[c] = w & ~kLeafNode;
                 first[c] = B.first[kids[c]];
             }
@@ -694,6 +792,13 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     B.counters = S.get<uint32_t>(4 + kMaxLevels + 2);
     B.qa = S.get<uint2>(n);
     B.qb = S.get<uint2>(n);
+    if (p.sah_collapse && n >= 2) {
+        B.dpc = S.get<float>(8ull * n);
+        B.dpch = S.get<uint8_t>(8ull * n);
+        B.dpj = S.get<uint8_t>(n);
+        B.dpleaf = S.get<uint8_t>(n);
+        B.c_tri = p.c_tri;
+    }
     float4* shade = nullptr;
     Check(cudaMalloc(&shade, 16ull * n), "cudaMalloc (shading normals)");
     out.d_tri_shade = shade;

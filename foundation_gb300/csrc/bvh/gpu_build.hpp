@@ -1,13 +1,13 @@
 // gpu_build.hpp — BVH construction on the GPU (gpu_build.cu).
 //
 // Same output format as the host builder + collapse (wide_bvh.hpp), built in
-// device memory: linear BVH over 30-bit Morton codes of the triangle
+// device memory: linear BVH over 63-bit Morton codes of the triangle
 // centroids (Karras, "Maximizing Parallelism in the Construction of BVHs,
 // Octrees, and k-d Trees", HPG 2012) with a stable LSD radix sort, a
 // bottom-up refit that also takes the SAH leaf decision (subtrees of at most
 // max_leaf triangles become one leaf when that is not more expensive), and
-// the greedy 8-wide collapse of collapse.cpp run level by level on the
-// device, with the same margin and outward quantisation. Hits are identical
+// the greedy or the SAH-optimal 8-wide collapse of collapse.cpp run level by
+// level on the device, with the same margin and outward quantisation. Hits are identical
 // to any other valid BVH over the same triangles; the tree itself differs
 // from the binned-SAH tree.
 #pragma once
@@ -24,6 +24,8 @@ struct GpuBuildParams {
     uint32_t max_leaf = 4;
     float trav_cost = 1.0f;
     float margin_scale = 1.0f;
+    bool sah_collapse = false;  // SAH-optimal collapse (collapse.hpp) instead of the greedy one
+    float c_tri = 0.3f;         // its cost of a triangle test relative to a wide-node visit
 };
 
 struct GpuBuildOutput {

@@ -128,7 +128,7 @@ namespace {
 // FND_BVH_GPU_BUILD: the vertices and indices go to the device once and the
 // tree is built there (bvh/gpu_build.cu).
 void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, uint32_t nv, const uint32_t* idx,
-                    uint32_t nt, const RT::BuildParams& bp, float margin_scale) {
+                    uint32_t nt, const RT::BuildParams& bp, float margin_scale, const RT::CollapseOptions& copt) {
     void *d_verts = nullptr, *d_idx = nullptr;
     RT::GpuBuildOutput go;
     try {
@@ -143,6 +143,8 @@ void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, ui
         gp.max_leaf = bp.max_leaf;
         gp.trav_cost = bp.trav_cost;
         gp.margin_scale = margin_scale;
+        gp.sah_collapse = copt.sah;
+        gp.c_tri = (float)copt.c_tri;
         RT::BuildWideGpu(static_cast<const float*>(d_verts), nv, static_cast<const uint32_t*>(d_idx), nt, gp, go,
                          ctx->stream);
         CUDA_CHECK(cudaFree(d_verts));
@@ -344,7 +346,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             return;
         }
         if (gpu_build) {
-            UploadGpuBuilt(ctx, scene.get(), verts, nv, idx, nt, bp, margin_scale);
+            UploadGpuBuilt(ctx, scene.get(), verts, nv, idx, nt, bp, margin_scale, copt);
             *out_scene = scene.release();
             ctx->live_scenes++;
             return;

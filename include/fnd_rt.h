@@ -116,8 +116,9 @@ enum { FND_BVH_SPATIAL_SPLITS = 1u };
 enum { FND_BVH_GPU_BUILD = 2u };
 /* Collapse the binary tree into 8-wide nodes by the SAH-optimal dynamic
  * programme (Ylitie, Karras & Laine 2017) instead of the greedy rule: fuller
- * nodes, small subtrees merged into leaf slots of up to 4 triangles. Host
- * builds only; hits are identical either way. */
+ * nodes, small subtrees merged into leaf slots of up to 4 triangles, on
+ * the host build and on FND_BVH_GPU_BUILD alike; hits are identical either
+ * way. */
 enum { FND_BVH_SAH_COLLAPSE = 4u };
 
 typedef struct fnd_rt_scene_info {

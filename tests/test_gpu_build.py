@@ -49,6 +49,14 @@ def test_gpu_built_scene_matches_oracle(ctx, case):
     assert np.array_equal(np.array(info["bounds_hi"], np.float32), hi)
     assert_same(g.closest(rays), b.closest(rays))
     assert np.array_equal(g.any(rays), b.any(rays))
+    # the SAH-optimal collapse on the device: fuller nodes, the same hits
+    gs = ctx.upload(sc.verts, sc.idx, gpu_build=True, sah_collapse=True)
+    si = gs.info()
+    assert 1 <= si["wide_depth"] <= 32 and si["num_refs"] == sc.num_tris
+    assert si["num_wide_nodes"] < info["num_wide_nodes"]
+    assert_same(gs.closest(rays), b.closest(rays))
+    assert np.array_equal(gs.any(rays), b.any(rays))
+    gs.close()
     g.close()
 
 
@@ -58,16 +66,20 @@ def test_gpu_build_tiny_and_degenerate(ctx):
         v = rng.uniform(-1, 1, (3 * n, 3)).astype(np.float32)
         f = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
         rays = S.incoherent_rays(4096, (-1, -1, -1), (1, 1, 1), seed=n)
-        g = ctx.upload(v, f, gpu_build=True)
-        assert_same(g.closest(rays), O.OracleBVH(v, f).closest(rays))
-        g.close()
+        ref = O.OracleBVH(v, f).closest(rays)
+        for sah in (False, True):
+            g = ctx.upload(v, f, gpu_build=True, sah_collapse=sah)
+            assert_same(g.closest(rays), ref)
+            g.close()
     # duplicates, a degenerate (zero-area) triangle, all centroids equal
     v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.5, 0.5, 0], [0.5, 0.5, 0], [0.5, 0.5, 0]], np.float32)
     f = np.array([[0, 1, 2]] * 40 + [[3, 4, 5]] * 3, np.uint32)
     rays = S.camera_rays(64, 64, eye=(0.3, 0.3, 2.0), target=(0.3, 0.3, 0.0))
-    g = ctx.upload(v, f, gpu_build=True)
-    assert_same(g.closest(rays), O.OracleBVH(v, f).closest(rays))
-    g.close()
+    ref = O.OracleBVH(v, f).closest(rays)
+    for sah in (False, True):
+        g = ctx.upload(v, f, gpu_build=True, sah_collapse=sah)
+        assert_same(g.closest(rays), ref)
+        g.close()
 
 
 def test_gpu_build_rejects_bad_input(ctx):
