@@ -32,7 +32,7 @@ STATUS_NAMES = {
     -9: "FND_ERR_IO",
 }
 FND_MEM_HOST, FND_MEM_DEVICE = 0, 1
-ABI_VERSION = 1
+ABI_VERSION = 2
 INVALID_ID = 0xFFFFFFFF
 
 HIT_DTYPE = np.dtype([("prim", np.uint32), ("t", np.float32)])

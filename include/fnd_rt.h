@@ -33,7 +33,9 @@
 extern "C" {
 #endif
 
-#define FND_RT_ABI_VERSION 1u
+/* 2: fnd_rt_bvh_desc gained collapse_tri_cost and fnd_cache_desc
+ * weight_average (both structs grew); version 1 callers are refused. */
+#define FND_RT_ABI_VERSION 2u
 #define FND_INVALID_ID 0xFFFFFFFFu
 
 typedef enum fnd_status {
