@@ -103,6 +103,11 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
     const int g_tail = ctx->sm_count * std::max(1, tail_occ);
     RT::TraceConfig cfg0 = ctx->trace_cfg;
     cfg0.sort_bits = 0;
+    // cache paths end in queries at the second interaction: what continues
+    // after it are specular chains, which the tail megakernel finishes
+    // whatever their number, so the later bounces are not enqueued at all
+    // (they would find empty queues)
+    const bool cache_tail = C.mode == 1 && tail_paths != 0;
     // two-level scenes: the instanced persistent kernel on the device queues
     auto trace = [&](RT::TraceLaunch& L, bool any, const RT::TraceConfig& cfg, int grid) -> cudaError_t {
         if (!two) return CApi::LaunchTraceOrdered(ctx, scene, L, any, false, cfg, grid);
@@ -166,10 +171,11 @@ void RunBounces(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const PT::PathBuffer
             T.C = C;
             T.q = nxt;
             T.bounce = b + 1;
-            T.threshold = tail_paths;
+            T.threshold = cache_tail && b == 1 ? 0xFFFFFFFFu : tail_paths;
             T.status = ctx->d_status;
             T.ray_stats = ctx->d_render_stats;
             CUDA_CHECK(PT::LaunchTail(T, g_tail, ctx->stream));
+            if (cache_tail && b == 1) break;
         }
     }
 }
