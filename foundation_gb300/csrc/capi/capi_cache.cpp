@@ -136,7 +136,11 @@ int fnd_rt_cache_create(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_ca
             ctx->cache->net.hi[a] = hi + pad;
         }
         try {
-            CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->cache->train_stream, cudaStreamNonBlocking));
+            // the highest priority: the training kernels take SMs at the render
+            // wave's kernel boundaries instead of waiting for the wave to end
+            int lo_prio = 0, hi_prio = 0;
+            CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+            CUDA_CHECK(cudaStreamCreateWithPriority(&ctx->cache->train_stream, cudaStreamNonBlocking, hi_prio));
             CUDA_CHECK(cudaEventCreateWithFlags(&ctx->cache->ev_start, cudaEventDisableTiming));
             CUDA_CHECK(cudaEventCreateWithFlags(&ctx->cache->ev_trained, cudaEventDisableTiming));
             EnsureCacheBuffers(ctx, 1024, 8);

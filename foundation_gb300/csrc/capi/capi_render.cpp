@@ -20,7 +20,12 @@ using Foundation::Core::Fail;
 
 namespace {
 
-constexpr uint32_t kDefaultWave = 1u << 22;  // 4,194,304 paths in flight
+// Paths in flight per wave: 33,554,432 (7.3 GB of path state). Every wave
+// pays its bounces' launches and the latency of each bounce's last rays, so
+// fewer, larger waves are faster: 1920x1080 x 64 spp takes 166.7 ms in waves
+// of 2^22 paths, 150.6 ms at 2^23, 142.1 ms at 2^24 and 137.2 ms at 2^25.
+// A render of fewer paths allocates only what it needs.
+constexpr uint32_t kDefaultWave = 1u << 25;
 
 size_t Align256(size_t x) { return (x + 255) & ~size_t(255); }
 

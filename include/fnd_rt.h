@@ -343,7 +343,8 @@ typedef struct fnd_render_desc {
     float sky[3];          /* constant radiance of escaping rays */
     float sun_dir[3];      /* towards the sun; zero vector: no sun */
     float sun_irradiance[3];
-    uint32_t wave_paths;   /* paths in flight per wave, 0: automatic */
+    uint32_t wave_paths;   /* paths in flight per wave (218 bytes of device state each),
+                              0: automatic (up to 2^25) */
     uint32_t tail_paths;   /* once at most this many paths of a wave remain, one
                               megakernel finishes them; 0: automatic */
 } fnd_render_desc;
