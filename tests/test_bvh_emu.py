@@ -188,3 +188,27 @@ def test_emulated_sah_collapse_matches_oracle(emu, case, spatial):
     assert np.array_equal(tbits, ref["t"].view(np.uint32))
     prim_a, _, _ = e.trace(rays, any_hit=True)
     assert np.array_equal((prim_a != 0xFFFFFFFF).astype(np.uint8), b.any(rays))
+
+
+def test_emulated_sah_collapse_small_and_degenerate(emu):
+    """The SAH-optimal collapse on trees of 1 to 33 triangles (a root that is
+    one leaf, leaves merged into the root), duplicates, a zero-area triangle
+    and coincident centroids: the oracle's hits."""
+    rng = np.random.default_rng(7)
+    cases = []
+    for n in (1, 2, 3, 4, 5, 9, 17, 33):
+        v = rng.uniform(-1, 1, (3 * n, 3)).astype(np.float32)
+        cases.append((v, np.arange(3 * n, dtype=np.uint32).reshape(n, 3)))
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.5, 0.5, 0], [0.5, 0.5, 0], [0.5, 0.5, 0]], np.float32)
+    cases.append((v, np.array([[0, 1, 2]] * 40 + [[3, 4, 5]] * 3, np.uint32)))
+    for v, f in cases:
+        rays = np.concatenate([S.incoherent_rays(2048, (-1, -1, -1), (1, 1, 1), seed=len(f)),
+                               S.camera_rays(32, 32, eye=(0.3, 0.3, 2.0), target=(0.3, 0.3, 0.0))])
+        for spatial in (0, 1):
+            e = Emu.__new__(Emu)
+            e.L, e.v, e.f = emu, v, f
+            e.h = emu.emu_build_sah_collapse(_p(v), len(v), _p(f), len(f), spatial, 0.3)
+            prim, tbits, _ = e.trace(rays)
+            ref = O.brute_closest(v, f, rays)
+            assert np.array_equal(prim, ref["prim"]), (len(f), spatial)
+            assert np.array_equal(tbits, ref["t"].view(np.uint32))
