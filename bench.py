@@ -415,7 +415,7 @@ def time_to_relmse_block(fg, torch, stream, local, ref_spp: int = 8192):
 
 
 def batched_block(fg, torch, stream, local, num_scenes: int = 256, reps: int = 5):
-    """Config 3: 256 triangle soups (log-uniform 1k..500k triangles, seed 2),
+    """Batched traversal: 256 triangle soups (log-uniform 1k..500k triangles, seed 2),
     each with a log-uniform 4k..1M ray batch (half camera, half random
     closest-hit rays) and as many any-hit shadow segments, all served by ONE
     persistent launch over the job table, replayed from a CUDA graph, launch
@@ -469,7 +469,7 @@ def batched_block(fg, torch, stream, local, num_scenes: int = 256, reps: int = 5
 
 
 def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 256, warmup_frames: int = 16):
-    """Config 5: heightfield terrain (2237^2 vertices, 8-octave value noise,
+    """Large scene: heightfield terrain (2237^2 vertices, 8-octave value noise,
     seed 3) plus 4,096 level-4 icospheres, 30,970,912 triangles, lit by a
     directional sun and a constant sky; 3840x2160, max depth 6, RR from
     bounce 3. Reported: the host build (binned SAH, SAH-optimal collapse),
@@ -558,7 +558,7 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
 
 
 def instanced_terrain(fg, ctx, tr, W, H, cam, kw, ref, spp, timed):
-    """The config-5 scene as a two-level scene: the terrain (built on the GPU)
+    """The large terrain scene as a two-level scene: the terrain (built on the GPU)
     as one instance and the 4,096 spheres as instances of one level-4
     icosphere; set-up time, device memory, and the plain 16-spp frame against
     the same reference as the flattened scene."""

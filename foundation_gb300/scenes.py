@@ -10,7 +10,7 @@ The reference renderer has no scene or mesh loader (its only geometry is the
 hard-coded 4-vertex quad of src/Renderer/Renderer.cpp:153-157); the scene
 shapes follow the workloads the path-tracer pass is measured on:
 
-* ``config1_scene``   unit icosphere subdivided 6 times (81,920 tris) plus
+* ``icosphere_scene`` unit icosphere subdivided 6 times (81,920 tris) plus
                       1,024 random triangles in [-2,2]^3 (seed 0)
 * ``camera_rays``     pinhole camera, glm lookAt convention (right-handed,
                       looking down -Z, as src/Renderer/Renderer.cpp:374-380)
@@ -151,7 +151,7 @@ def random_triangles(n: int, seed: int, lo: float, hi: float, stream_base: int =
     return v, f
 
 
-def config1_scene() -> Scene:
+def icosphere_scene() -> Scene:
     """Unit icosphere subdivided 6 times (81,920 tris) + 1,024 random
     triangles with vertices uniform in [-2,2]^3, seed 0: 82,944 triangles."""
     sv, sf = icosphere(6)

@@ -31,7 +31,7 @@ def assert_same(h, ref):
 @pytest.mark.parametrize("case", ["c1", "cornell", "soup"])
 def test_gpu_built_scene_matches_oracle(ctx, case):
     if case == "c1":
-        sc, rays = S.config1_scene(), S.camera_rays(512, 512)
+        sc, rays = S.icosphere_scene(), S.camera_rays(512, 512)
     elif case == "cornell":
         sc = S.cornell_scene()
         rays = np.concatenate([S.incoherent_rays(1 << 19, *sc.bounds, seed=1),

@@ -37,15 +37,15 @@ def test_golden_soup(ctx):
     sc.close()
 
 
-def test_config1_full_frame(ctx):
+def test_icosphere_full_frame(ctx):
     """1024x1024 primary rays on the icosphere + random-triangle scene."""
-    c1 = S.config1_scene()
+    c1 = S.icosphere_scene()
     rays = S.camera_rays(1024, 1024)
     sc = ctx.upload(c1.verts, c1.idx)
     h = sc.closest(rays)
     b = O.OracleBVH(c1.verts, c1.idx)
     assert_same(h, b.closest(rays))
-    g = np.load(os.path.join(GOLDEN, "config1_rows.npz"))
+    g = np.load(os.path.join(GOLDEN, "icosphere_rows.npz"))
     assert np.array_equal(h["prim"][g["sel"]], g["prim"])
     assert np.array_equal(sc.any(rays), b.any(rays))
     sc.close()
