@@ -48,11 +48,14 @@ PROFILES = os.path.join(ROOT, "profiles")
 # are those of any other tree.
 CORNELL_BVH = dict(spatial_splits=True, split_budget=8.0, sah_collapse=True)
 # Radiance cache of the cache blocks: 65,536 training paths per frame (the
-# workload's figure), 8 Adam steps of 16,384 samples at lr 1e-2, queries on
+# workload's figure), 6 Adam steps of 16,384 samples at lr 1e-2, queries on
 # the exponential moving average (0.98) of the iterates, GGX alpha below 0.05
-# counted as specular. Chosen on the Cornell time-to-relMSE workload over 3
-# seeds each: 3.32-3.68x, against 2.90-3.17x with 4 steps and no averaging.
-CACHE_SETTINGS = dict(train_paths=65536, train_steps=8, batch=16384, learning_rate=1e-2, weight_average=0.98,
+# counted as specular. Chosen on the Cornell time-to-relMSE workload, training
+# seeds 1, 3, 5 per setting (speed-up over the plain tracer in waves of 2^25
+# paths): 6 steps 3.18-3.32x over two runs; 4 / 5 / 7 / 8 / 12 steps 3.00 /
+# 3.00 / 3.14 / 3.07 / 2.82x (medians); around 6 steps, averages 0.95 / 0.97
+# / 0.99, batches of 12,288 / 20,480 and 12 / 24 warm-up frames were slower.
+CACHE_SETTINGS = dict(train_paths=65536, train_steps=6, batch=16384, learning_rate=1e-2, weight_average=0.98,
                       specular_alpha=0.05)
 # training-only frames before the first cache frame of the time-to-relMSE
 # block (8 / 16 / 24 / 32 measured over 3 seeds: 16 is the fastest)
@@ -330,10 +333,10 @@ def incoherent_1m_block(fg, torch, stream, local, n_rays=8_388_608):
 
 
 def cache_frames_block(fg, torch, stream, local, frames: int = 8):
-    """Radiance-cache frames at 1920x1080 on the Cornell scene (65,536
-    training paths and 8 Adam steps of 16,384 per frame): `frames`
-    training-only frames, then `frames` 1-spp cache frames, each timed with
-    CUDA events (the per-frame costs behind the time-to-relMSE block)."""
+    """Radiance-cache frames at 1920x1080 on the Cornell scene with
+    CACHE_SETTINGS: `frames` training-only frames, then `frames` 1-spp cache
+    frames, each timed with CUDA events (the per-frame costs behind the
+    time-to-relMSE block)."""
     from foundation_gb300 import scenes
     cs = scenes.cornell_scene()
     ctx = fg.Context(local, stream=stream.cuda_stream)
@@ -358,8 +361,9 @@ def cache_frames_block(fg, torch, stream, local, frames: int = 8):
               for f in range(frames)]
     st = ctx.render_stats()
     ctx.close()
-    return {"workload": "cornell200 1920x1080, cache frames (65,536 training paths, 8 x 16,384-sample steps, "
-                        "weight average 0.98)",
+    c = CACHE_SETTINGS
+    return {"workload": f"cornell200 1920x1080, cache frames ({c['train_paths']:,} training paths, "
+                        f"{c['train_steps']} x {c['batch']:,}-sample steps, weight average {c['weight_average']})",
             "train_only_ms": float(np.median(train)), "cache_frame_ms": float(np.median(render)),
             "extension_rays_last": st["extension_rays"], "shadow_rays_last": st["shadow_rays"]}
 
