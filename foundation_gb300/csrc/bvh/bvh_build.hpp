@@ -51,7 +51,10 @@ struct BuildParams {
 void BuildBinaryBvh(const float* tri, uint32_t nt, const BuildParams& params, BinaryBvh& out);
 
 // Binned SAH with spatial splits (sbvh_build.cpp): leaves may reference a
-// triangle more than once; out.prims holds the references.
+// triangle more than once; out.prims holds the references. The build threads
+// draw on one shared duplicate budget (max_refs_factor): while it lasts the
+// tree is a function of the triangle set only; once it runs out, which nodes
+// still split spatially depends on thread timing.
 void BuildBinarySbvh(const float* tri, uint32_t nt, const BuildParams& params, BinaryBvh& out);
 
 }  // namespace RT

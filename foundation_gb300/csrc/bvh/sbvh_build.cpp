@@ -10,7 +10,9 @@
 // clipping, intersected with the reference's current box), and a reference
 // crossing the chosen plane is duplicated into both children with clipped
 // boxes. The duplicates are capped (max_refs_factor x triangles extra
-// references); once the budget is used, nodes fall back to object splits.
+// references, one atomic count shared by the build threads); once the budget
+// is used, nodes fall back to object splits, so a build that exhausts it may
+// split different nodes from run to run.
 // Closest-hit results do not depend on the tree (ties break by triangle
 // index), so a duplicated reference cannot change any hit.
 #include <algorithm>

@@ -95,7 +95,10 @@ typedef struct fnd_rt_bvh_desc {
                                per triangle, [0, 16]; 0: default 2. The builder stops
                                splitting where the SAH gains nothing, so a large budget
                                is a cap rather than a target (a dense soup of 1M
-                               triangles settles near 6 references per triangle) */
+                               triangles settles near 6 references per triangle).
+                               Build threads share the budget, so when it runs out
+                               the tree can differ from one build to the next; hits
+                               never do. Below the cap the tree is reproducible */
     float margin_scale;     /* box inflation relative to the default (2^-16 of the scene
                                size), [1, 2^16]; 0: 1. A scene instanced at a scale far below
                                the world's needs more (fnd_rt_instances_upload checks it) */
