@@ -90,6 +90,18 @@ def workload(rank: int, n_rays: int, kind: str = "cornell"):
     return replicas.shard_workload(kind, rank, n_rays)
 
 
+L2_BYTES = 129 * 10**6  # GB300 L2
+
+
+def l2_note(n_rays: int) -> str:
+    """How the timed steps relate to L2: the default 8,388,608 rays (268 MB)
+    stream past it every step; a smaller --rays keeps them in it."""
+    mb = 32 * n_rays / 1e6
+    if 32 * n_rays > L2_BYTES:
+        return f"inputs larger than L2: {mb:.0f} MB of rays streamed per step per GPU"
+    return f"inputs within L2: {mb:.1f} MB of rays per step per GPU, no flush between steps"
+
+
 def config_block(sc, n_rays, world, kind: str = "cornell"):
     if kind == "soup1m":
         return {
@@ -98,7 +110,7 @@ def config_block(sc, n_rays, world, kind: str = "cornell"):
             "scene_tris": sc.num_tris,
             "rays_per_step_per_gpu": n_rays,
             "rays": "origins uniform in the cube, directions uniform on S^2",
-            "l2": "inputs larger than L2: 268 MB of rays streamed per step per GPU",
+            "l2": l2_note(n_rays),
             "parallelism": f"replicas x{world}",
         }
     return {
@@ -107,7 +119,7 @@ def config_block(sc, n_rays, world, kind: str = "cornell"):
         "scene_tris": sc.num_tris,
         "rays_per_step_per_gpu": n_rays,
         "rays": "origins uniform in the box, directions uniform on S^2",
-        "l2": "inputs larger than L2: 268 MB of rays streamed per step per GPU",
+        "l2": l2_note(n_rays),
         "parallelism": f"replicas x{world}",
     }
 
