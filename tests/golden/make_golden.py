@@ -41,13 +41,13 @@ def main():
                         prim=h["prim"], t=h["t"], occluded=a)
     # 2) first 4096 primary rays of the 1024x1024 icosphere workload; the
     #    scene itself is pinned by a digest of the generator output
-    c1 = scenes.icosphere_scene()
+    ico = scenes.icosphere_scene()
     r1 = scenes.camera_rays(1024, 1024)
-    b1 = oracle.OracleBVH(c1.verts, c1.idx)
+    b1 = oracle.OracleBVH(ico.verts, ico.idx)
     sel = np.concatenate([np.arange(4096), np.arange(512 * 1024, 512 * 1024 + 4096)])
     h1 = b1.closest(r1[sel])
     np.savez_compressed(os.path.join(OUT, "icosphere_rows.npz"), sel=sel, rays=r1[sel], prim=h1["prim"], t=h1["t"],
-                        scene_sha256=np.array(digest(c1.verts, c1.idx)),
+                        scene_sha256=np.array(digest(ico.verts, ico.idx)),
                         rays_sha256=np.array(digest(r1)))
     # 3) the Cornell-box scene digest and 2048 incoherent rays
     cs = scenes.cornell_scene()

@@ -62,7 +62,7 @@ class Emu:
 
 
 CASES = {
-    "c1_camera": lambda: (S.icosphere_scene(), S.camera_rays(128, 128)),
+    "icosphere_camera": lambda: (S.icosphere_scene(), S.camera_rays(128, 128)),
     "cornell_incoherent": lambda: (S.cornell_scene(), S.incoherent_rays(20000, (-1, 0, -1), (1, 2, 1), seed=1)),
     "cornell_camera": lambda: (S.cornell_scene(), S.camera_rays(160, 90, **S.CORNELL_CAMERA)),
     "soup": lambda: (S.soup_scene(50000), S.incoherent_rays(20000, (0, 0, 0), (1, 1, 1), seed=2)),

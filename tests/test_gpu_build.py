@@ -28,9 +28,9 @@ def assert_same(h, ref):
     assert np.array_equal(h["t"].view(np.uint32), ref["t"].view(np.uint32))
 
 
-@pytest.mark.parametrize("case", ["c1", "cornell", "soup"])
+@pytest.mark.parametrize("case", ["ico", "cornell", "soup"])
 def test_gpu_built_scene_matches_oracle(ctx, case):
-    if case == "c1":
+    if case == "ico":
         sc, rays = S.icosphere_scene(), S.camera_rays(512, 512)
     elif case == "cornell":
         sc = S.cornell_scene()

@@ -136,9 +136,9 @@ def test_pcg32_numpy_streams_match():
 
 # ---- BVH -----------------------------------------------------------------
 
-@pytest.mark.parametrize("name", ["c1", "soup", "cornell_small"])
+@pytest.mark.parametrize("name", ["ico", "soup", "cornell_small"])
 def test_bvh_invariants(name):
-    sc = {"c1": S.icosphere_scene, "soup": lambda: S.soup_scene(20000),
+    sc = {"ico": S.icosphere_scene, "soup": lambda: S.soup_scene(20000),
           "cornell_small": lambda: S.cornell_scene(num_spheres=10, level=2)}[name]()
     b = O.OracleBVH(sc.verts, sc.idx)
     assert b.validate() == 0
@@ -188,18 +188,18 @@ def test_golden_soup():
 
 def test_golden_generators_are_pinned():
     g = np.load(os.path.join(GOLDEN, "icosphere_rows.npz"))
-    c1 = S.icosphere_scene()
-    assert _sha(c1.verts, c1.idx) == str(g["scene_sha256"])
+    ico = S.icosphere_scene()
+    assert _sha(ico.verts, ico.idx) == str(g["scene_sha256"])
     assert _sha(S.camera_rays(1024, 1024)) == str(g["rays_sha256"])
     gc = np.load(os.path.join(GOLDEN, "cornell_rows.npz"))
     cs = S.cornell_scene()
     assert _sha(cs.verts, cs.idx, cs.tri_material, cs.materials) == str(gc["scene_sha256"])
-    assert cs.num_tris == 256012 and c1.num_tris == 82944
+    assert cs.num_tris == 256012 and ico.num_tris == 82944
 
 
 def test_golden_icosphere_rows():
     g = np.load(os.path.join(GOLDEN, "icosphere_rows.npz"))
-    c1 = S.icosphere_scene()
-    h = O.OracleBVH(c1.verts, c1.idx).closest(g["rays"])
+    ico = S.icosphere_scene()
+    h = O.OracleBVH(ico.verts, ico.idx).closest(g["rays"])
     assert np.array_equal(h["prim"], g["prim"])
     assert np.array_equal(h["t"].view(np.uint32), g["t"].view(np.uint32))

@@ -39,11 +39,11 @@ def test_golden_soup(ctx):
 
 def test_icosphere_full_frame(ctx):
     """1024x1024 primary rays on the icosphere + random-triangle scene."""
-    c1 = S.icosphere_scene()
+    ico = S.icosphere_scene()
     rays = S.camera_rays(1024, 1024)
-    sc = ctx.upload(c1.verts, c1.idx)
+    sc = ctx.upload(ico.verts, ico.idx)
     h = sc.closest(rays)
-    b = O.OracleBVH(c1.verts, c1.idx)
+    b = O.OracleBVH(ico.verts, ico.idx)
     assert_same(h, b.closest(rays))
     g = np.load(os.path.join(GOLDEN, "icosphere_rows.npz"))
     assert np.array_equal(h["prim"][g["sel"]], g["prim"])
