@@ -25,14 +25,16 @@ struct WideBvh {
 float SceneMargin(const float lo[3], const float hi[3]);
 
 struct CollapseOptions {
-    bool sah = false;     // SAH-optimal collapse instead of the greedy one
-    double c_node = 1.0;  // its cost of a wide-node visit per unit of half area
-    double c_tri = 0.3;   // and of a triangle test (the kernel's best of 0.05 - 1)
+    bool sah = false;       // SAH-optimal collapse instead of the greedy one
+    double c_node = 1.0;    // its cost of a wide-node visit per unit of half area
+    double c_tri = 0.3;     // and of a triangle test (the kernel's best of 0.05 - 1)
+    uint32_t threads = 0;   // host threads; 0: all cores. The output does not depend on it
 };
 
 // Greedy collapse (largest-surface-area internal child expanded first until 8
 // children) or SAH-optimal collapse (opt.sah), octant-ordered slot assignment,
-// 8-bit outward quantisation. margin_scale multiplies SceneMargin (a
+// 8-bit outward quantisation; wide nodes in breadth-first order, computed a
+// level at a time on opt.threads threads. margin_scale multiplies SceneMargin (a
 // bottom-level scene whose instances shrink it far below the world's size
 // needs a wider margin: its object-space ray origins lie further away, see
 // fnd_rt_instances_upload).

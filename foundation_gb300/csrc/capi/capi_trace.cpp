@@ -330,6 +330,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
                    FND_ERR_INVALID_ARG, "unknown BVH flags 0x%x", bvh ? bvh->flags : 0u);
         RT::CollapseOptions copt;
         copt.sah = bvh && (bvh->flags & FND_BVH_SAH_COLLAPSE);
+        copt.threads = bvh ? bvh->build_threads : 0u;
         copt.c_tri = bvh && bvh->collapse_tri_cost != 0.0f ? bvh->collapse_tri_cost : 0.3;
         CHECK_CODE(copt.c_tri > 0.0 && copt.c_tri <= 16.0, FND_ERR_INVALID_ARG, "collapse_tri_cost %g not in (0, 16]",
                    copt.c_tri);

@@ -174,6 +174,35 @@ emu_bvh* emu_build_sah_collapse(const float* verts, uint32_t nv, const uint32_t*
     return e;
 }
 
+// FNV-1a hash of the bytes of the wide tree (nodes, then the three plane
+// arrays) that e's binary tree collapses to on `threads` threads, by the
+// SAH-optimal rule (sah != 0) or the greedy one.
+uint64_t emu_collapse_hash(const emu_bvh* e, const float* verts, const uint32_t* idx, uint32_t nt, int sah,
+                           uint32_t threads) {
+    std::vector<float> tri(9 * (size_t)nt);
+    for (uint32_t t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) tri[9 * (size_t)t + 3 * k + c] = verts[3 * (size_t)idx[3 * (size_t)t + k] + c];
+    CollapseOptions o;
+    o.sah = sah != 0;
+    o.threads = threads;
+    WideBvh w;
+    CollapseToWide(e->bin, tri.data(), nt, w, 1.0f, o);
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; ++i) {
+            h ^= b[i];
+            h *= 1099511628211ull;
+        }
+    };
+    mix(w.nodes.data(), w.nodes.size() * sizeof(WideNode));
+    mix(w.v0.data(), 4 * w.v0.size());
+    mix(w.v1.data(), 4 * w.v1.size());
+    mix(w.v2.data(), 4 * w.v2.size());
+    return h;
+}
+
 // Leaf references (triangles, plus the duplicates spatial splits added).
 uint64_t emu_num_refs(const emu_bvh* e) { return e->bin.prims.size(); }
 

@@ -29,6 +29,8 @@ def emu(built):
     L.emu_num_refs.argtypes = [P]
     L.emu_build_sah_collapse.restype = P
     L.emu_build_sah_collapse.argtypes = [P, C.c_uint32, P, C.c_uint32, C.c_int, C.c_double]
+    L.emu_collapse_hash.restype = C.c_uint64
+    L.emu_collapse_hash.argtypes = [P, P, P, C.c_uint32, C.c_int, C.c_uint32]
     return L
 
 
@@ -212,3 +214,23 @@ def test_emulated_sah_collapse_small_and_degenerate(emu):
             ref = O.brute_closest(v, f, rays)
             assert np.array_equal(prim, ref["prim"]), (len(f), spatial)
             assert np.array_equal(tbits, ref["t"].view(np.uint32))
+
+
+@pytest.mark.parametrize("scene", ["soup", "cornell"])
+def test_collapse_independent_of_threads(emu, scene):
+    """The wide tree's bytes (nodes and triangle planes) are the same on 1, 2,
+    3 and 8 collapse threads, for both collapse rules and both builders: the
+    collapse lays the nodes out a level at a time, in the breadth-first order
+    of a one-by-one queue, and solves the SAH-optimal costs of independent
+    subtrees in parallel."""
+    sc = S.soup_scene(60000) if scene == "soup" else S.cornell_scene(num_spheres=40)
+    v = np.ascontiguousarray(sc.verts, np.float32)
+    f = np.ascontiguousarray(sc.idx, np.uint32)
+    for spatial in (0, 1):
+        h = emu.emu_build_sah_collapse(_p(v), len(v), _p(f), len(f), spatial, 0.3)
+        try:
+            for sah in (0, 1):
+                hashes = {emu.emu_collapse_hash(h, _p(v), _p(f), len(f), sah, t) for t in (1, 2, 3, 8)}
+                assert len(hashes) == 1, (scene, spatial, sah)
+        finally:
+            emu.emu_free(h)
