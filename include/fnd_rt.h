@@ -87,7 +87,9 @@ typedef struct fnd_rt_desc {
 typedef struct fnd_rt_bvh_desc {
     uint32_t sah_bins;      /* 2..64, default 32 */
     uint32_t max_leaf_tris; /* 1..4, default 4 */
-    uint32_t build_threads; /* 0: all host cores */
+    uint32_t build_threads; /* host threads of the build and the collapse; 0: all
+                               host cores. The tree does not depend on it, except
+                               when a spatial-split budget runs out (split_budget) */
     uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD, FND_BVH_SAH_COLLAPSE or 0 */
     float traversal_cost;   /* SAH cost of a traversal step relative to a triangle
                                test, (0, 64]; 0: default 1 (the reference tree) */
