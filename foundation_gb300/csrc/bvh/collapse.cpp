@@ -416,9 +416,9 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
     out.margin = margin;
     out.nodes.assign(1, WideNode{});
     const size_t nrefs = bin.prims.size();  // == nt unless spatial splits duplicated references
-    out.v0.assign(4 * nrefs, 0.0f);
-    out.v1.assign(4 * nrefs, 0.0f);
-    out.v2.assign(4 * nrefs, 0.0f);
+    out.v0 = PlaneVector(4 * nrefs);  // every element is written below
+    out.v1 = PlaneVector(4 * nrefs);
+    out.v2 = PlaneVector(4 * nrefs);
     out.depth = 0;
     out.leaves = 0;
     uint64_t next_tri = 0;
@@ -460,9 +460,11 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
                 out.v1[d + 0] = v[3];
                 out.v1[d + 1] = v[4];
                 out.v1[d + 2] = v[5];
+                out.v1[d + 3] = 0.0f;
                 out.v2[d + 0] = v[6];
                 out.v2[d + 1] = v[7];
                 out.v2[d + 2] = v[8];
+                out.v2[d + 3] = 0.0f;
             }
         });
         level.swap(next);

@@ -2,6 +2,9 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
+#include <new>
+#include <utility>
 #include <vector>
 
 #include "bvh_build.hpp"
@@ -10,9 +13,32 @@
 namespace Foundation {
 namespace RT {
 
+// Allocator whose value-initialisation (vector(n), resize(n)) leaves the
+// elements uninitialised: the collapse writes every plane element itself, on
+// several threads, instead of one thread zero-filling gigabytes first.
+template <class T>
+struct NoInitAllocator : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInitAllocator<U>;
+    };
+    NoInitAllocator() = default;
+    template <class U>
+    NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
+    template <class U>
+    void construct(U* p) noexcept {
+        ::new (static_cast<void*>(p)) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) {
+        ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+    }
+};
+using PlaneVector = std::vector<float, NoInitAllocator<float>>;
+
 struct WideBvh {
     std::vector<WideNode> nodes;
-    std::vector<float> v0, v1, v2;  // 4 floats per triangle each (see wide_bvh.hpp)
+    PlaneVector v0, v1, v2;  // 4 floats per triangle each (see wide_bvh.hpp)
     uint32_t depth = 0;             // wide levels on the longest root-to-leaf path
     uint32_t leaves = 0;
     float margin = 0.0f;            // absolute outward inflation of every box
