@@ -9,13 +9,23 @@ Mrays/s closest hit.
   value  rays / device time, rays and hits resident in HBM
   e2e    the same through the C ABI with pinned HOST buffers: every step
          copies the rays in and the hits out inside the timed region
-  roofline  algorithmic bytes per ray (counted by the CPU oracle on the
-         binary binned-SAH BVH: 32 B ray + 8 B hit + 32 B per node box fetched
-         + 36 B per triangle tested) x rays / average kernel time, against the
-         measured HBM copy bandwidth; an L2 read bandwidth measured here is
-         reported beside it because the 16 MB BVH stays L2-resident
+  roofline  the traversal kernel against the bound it hits: instruction
+         issue (warp instructions per ray from the committed ncu summary of
+         the workload x rays / kernel time, against 4 warp instructions per
+         cycle per SM at the SM clock sampled during the timed steps). Beside
+         it: its L2 bytes per ray against an L2 read bandwidth measured here
+         by a hand-written kernel (probe/l2_read.cu), its DRAM bytes against
+         the measured HBM copy peak, and the accounting figure: algorithmic
+         bytes per ray counted by the CPU oracle on the binary binned-SAH BVH
+         (32 B ray + 8 B hit + 32 B per node box fetched + 36 B per triangle
+         tested) x rays / kernel time, against the HBM peak
   cpu_baseline  the CPU oracle (scalar C++, all host threads) on the same
          workload, timed on this host
+
+Output: the measured blocks beyond the headline (path tracer, 1M-triangle
+soup, time to relMSE, batched and large scenes) go on one JSON line of their
+own, {"bench_blocks": ...}, printed first; the contract line comes last and
+carries their headline figures as scalar `target_*` keys.
 
 Multi-GPU: the pass does not exchange data between GPUs; N ranks trace N
 independent ray batches of the same size (replicas, weak scaling).
@@ -198,45 +208,42 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def profile_traffic(kind: str = "cornell"):
-    """dram bytes per launch of the traversal kernel from the committed ncu
-    summary of the workload (a line 'dram_bytes_per_launch: N'), or None."""
+def profile_figures(kind: str = "cornell") -> dict:
+    """Per-launch figures of the traversal kernel from the committed ncu
+    summary of the workload: its machine-readable lines `key: number`
+    (dram_bytes_per_launch, l2_bytes_per_launch, warp_inst_per_launch,
+    issue_active_pct, rays_per_launch)."""
     path = os.path.join(PROFILES, f"trace_closest_{kind}_incoherent.txt")
+    out = {}
     if not os.path.exists(path):
-        return None
+        return out
+    keys = ("dram_bytes_per_launch", "l2_bytes_per_launch", "warp_inst_per_launch", "issue_active_pct",
+            "rays_per_launch")
     for line in open(path):
-        if line.strip().startswith("dram_bytes_per_launch:"):
+        k, _, v = line.strip().partition(":")
+        if k in keys:
             try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+                out[k] = float(v.split()[0])
+            except (ValueError, IndexError):
+                pass
+    return out
 
 
-def l2_bandwidth_gbs(torch) -> dict:
-    """L2-resident bandwidth measured here (the peaks file has only HBM):
-    best of 20 of a 32 MB device copy (read + write bytes) and of a 64 MB
-    sum (read bytes), both far below the 129 MB L2."""
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-
-    def best_ms(fn):
-        for _ in range(3):
-            fn()
-        b = float("inf")
-        for _ in range(20):
-            s.record()
-            fn()
-            e.record()
-            e.synchronize()
-            b = min(b, s.elapsed_time(e))
-        return b
-    x = torch.ones(8 << 20, dtype=torch.float32, device="cuda")
-    y = torch.empty_like(x)
-    copy_ms = best_ms(lambda: y.copy_(x))
-    z = torch.ones(16 << 20, dtype=torch.float32, device="cuda")
-    sum_ms = best_ms(lambda: z.sum())
-    return {"copy_gbs": 2 * x.numel() * 4 / (copy_ms * 1e-3) / 1e9,
-            "sum_read_gbs": z.numel() * 4 / (sum_ms * 1e-3) / 1e9}
+def l2_read_bandwidth() -> dict:
+    """L2 read bandwidth of this GPU, measured by probe/l2_read.cu: a
+    persistent grid re-reads a 48 MB L2-resident buffer 64 times per launch
+    with 16-byte ld.global.cg loads; best of 10 launches (CUDA events)."""
+    import ctypes as C
+    from foundation_gb300 import _build
+    L = C.CDLL(_build.PROBE_PATH)
+    L.fnd_probe_l2_read.argtypes = [C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_uint64)]
+    L.fnd_probe_l2_read.restype = C.c_int
+    gbs, ms, nb = C.c_double(), C.c_double(), C.c_uint64()
+    if L.fnd_probe_l2_read(48 << 20, 64, 10, C.byref(gbs), C.byref(ms), C.byref(nb)) != 0:
+        raise RuntimeError("L2 bandwidth probe failed")
+    return {"gbs": gbs.value, "ms": ms.value, "bytes_per_launch": nb.value,
+            "method": "48 MB buffer re-read 64x per launch, 16 B ld.global.cg, persistent grid, best of 10"}
 
 
 def algorithmic_bytes_per_ray(sc, rays, sample=1 << 20):
@@ -639,6 +646,30 @@ def cpu_baseline(sc, rays):
             "single_core_mrays_s": n1 / dt1 / 1e6, "bvh_build_s": build_s, "integrator": integ}
 
 
+def target_figures(blocks: dict) -> dict:
+    """The headline figure of each measured block as a scalar key of the
+    contract line (the blocks themselves are on the line before)."""
+    out = {}
+    b = blocks.get("incoherent_1m_tris")
+    if b:
+        out["target_soup1m_mrays_s"] = b["best"]["mrays_s"]
+        out["target_soup1m_goal_mrays_s"] = b["target_mrays_s"]
+    b = blocks.get("time_to_relmse_1080p")
+    if b:
+        out["target_cache_speedup_to_relmse_1e3"] = b["speedup_cache_vs_plain"]
+        out["target_cache_speedup_goal"] = b["target_speedup"]
+    b = blocks.get("path_tracer")
+    if b:
+        out["path_tracer_1080p_64spp_ms"] = b["frame_ms"]
+    b = blocks.get("batched_256_scenes")
+    if b:
+        out["batched_256_scenes_grays_s"] = b["grays_s"]
+    b = blocks.get("large_scene_4k")
+    if b and "incoherent_mrays_s" in b:
+        out["large_scene_incoherent_mrays_s"] = b["incoherent_mrays_s"]
+    return out
+
+
 # ---------------------------------------------------------------------------
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
@@ -649,23 +680,23 @@ def run_reference(args):
     sc, rays = workload(0, args.rays, args.workload)
     b = oracle.OracleBVH(sc.verts, sc.idx)
     cores = os.cpu_count() or 1
-    sample = min(len(rays), 1 << 20)
+    # every step traces the whole step's rays, like the GPU arm
     for i in range(args.warmup):
-        b.closest(rays[:sample], threads=cores)
+        b.closest(rays, threads=cores)
     times = []
     for i in range(args.steps):
-        off = (i * sample) % max(1, len(rays) - sample + 1)
         t0 = time.perf_counter()
-        b.closest(rays[off:off + sample], threads=cores)
+        b.closest(rays, threads=cores)
         times.append(time.perf_counter() - t0)
     tot = sum(times)
-    value = sample * args.steps / tot / 1e6
+    value = len(rays) * args.steps / tot / 1e6
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config_block(sc, args.rays, 1, args.workload), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{sample} rays of the workload per step"},
+                             "sample": f"all {len(rays)} rays of the workload per step, scalar C++ oracle on "
+                                       f"{cores} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "mos9527/Foundation has no ray tracer; its arm is the CPU restatement of the path"}
     print(json.dumps(line), flush=True)
@@ -759,48 +790,73 @@ def main():
         peaks, peak_kind = measured_peaks()
         bpr, nodes, tris = algorithmic_bytes_per_ray(sc, rays)
         kern_ms = float(np.mean(per_step))
-        achieved = bpr * n / (kern_ms * 1e-3) / 1e9
-        traffic = profile_traffic(args.workload)
-        l2 = l2_bandwidth_gbs(torch)
-        l2_peak = max(l2.values())
+        kern_s = kern_ms * 1e-3
+        prof = profile_figures(args.workload)
+        l2 = l2_read_bandwidth()
+        # issue bound: 4 warp schedulers per SM, one instruction per cycle each
+        sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        issue_peak = 4 * sms * sm_mhz * 1e6 / 1e9  # G warp instructions / s
+        prof_rays = prof.get("rays_per_launch", float(n))
+        inst_per_ray = prof["warp_inst_per_launch"] / prof_rays if "warp_inst_per_launch" in prof else None
+        issue_achieved = inst_per_ray * n / kern_s / 1e9 if inst_per_ray else None
+        l2_bpr = prof["l2_bytes_per_launch"] / prof_rays if "l2_bytes_per_launch" in prof else None
+        traffic = prof["dram_bytes_per_launch"] * n / prof_rays if "dram_bytes_per_launch" in prof else None
+        algo_gbs = bpr * n / kern_s / 1e9
+        roofline = {
+            "bound": "issue", "achieved": issue_achieved, "peak": issue_peak, "unit": "G warp-inst/s",
+            "frac": issue_achieved / issue_peak if issue_achieved else None, "traffic": traffic,
+            "warp_inst_per_ray": inst_per_ray, "issue_active_ncu": prof.get("issue_active_pct"),
+            "peak_source": f"4 warp-inst/cycle/SM x {sms} SMs x {sm_mhz:g} MHz (median SM clock, timed steps)",
+            "kernel_ms_avg": kern_ms,
+            "l2_bytes_per_ray": l2_bpr, "l2_gbs": l2_bpr * n / kern_s / 1e9 if l2_bpr else None,
+            "l2_peak_gbs": l2["gbs"], "l2_frac": (l2_bpr * n / kern_s / 1e9) / l2["gbs"] if l2_bpr else None,
+            "hbm_gbs": traffic / kern_s / 1e9 if traffic else None, "hbm_peak_gbs": peaks["hbm_gbs"],
+            "hbm_frac": traffic / kern_s / 1e9 / peaks["hbm_gbs"] if traffic else None,
+            "hbm_peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
+            "accounting_bytes_per_ray": bpr, "accounting_gbs": algo_gbs,
+            "accounting_frac_of_hbm": algo_gbs / peaks["hbm_gbs"],
+            "profile": f"profiles/trace_closest_{args.workload}_incoherent.txt",
+        }
+        blocks_out = {
+            "bvh": ("binned SAH 32 bins, <=4 tris/leaf" +
+                    (f", spatial splits (split budget {args.split_budget:g})" if args.bvh == "spatial" else "") +
+                    (", SAH-optimal collapse" if args.collapse == "sah" else ", greedy collapse") +
+                    " to 8-wide compressed nodes"),
+            "scene_info": {k: info[k] for k in ("num_wide_nodes", "num_refs", "wide_depth", "node_bytes", "tri_bytes",
+                                                "build_ms", "collapse_ms")},
+            "roofline_detail": {"oracle_nodes_per_ray": nodes, "oracle_tris_per_ray": tris,
+                                "device_counters": counters, "l2_probe": l2, "profile_figures": prof,
+                                "accounting_note": "algorithmic bytes of the binary reference tree (32 B per "
+                                "binary node visit, 36 B per triangle test, 40 B of ray and hit); the wide tree "
+                                "fetches fewer bytes, from L1 and L2, so this figure is an accounting unit and "
+                                "not a position against HBM"},
+            "e2e_ms_per_call": {"min": 1e3 * min(per_call), "median": 1e3 * float(np.median(per_call)),
+                                "max": 1e3 * max(per_call)},
+        }
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(config_block(sc, n, world, args.workload),
-                           bvh=("binned SAH 32 bins, <=4 tris/leaf" +
-                                (f", spatial splits (split budget {args.split_budget:g})" if args.bvh == "spatial"
-                                 else "") +
-                                (", SAH-optimal collapse" if args.collapse == "sah" else ", greedy collapse") +
-                                " to 8-wide compressed nodes"),
-                           roofline_bytes="algorithmic bytes counted by the oracle on the binary binned-SAH tree"),
+            "config": config_block(sc, n, world, args.workload),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8,
-                    "steps": e2e_steps, "matches_device_result": e2e_ok,
-                    "ms_per_call": {"min": 1e3 * min(per_call), "median": 1e3 * float(np.median(per_call)),
-                                    "max": 1e3 * max(per_call)}},
+                    "steps": e2e_steps, "matches_device_result": e2e_ok},
             "gpu_launches": args.steps,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
-                         "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
-                         "algorithmic_bytes_per_ray": bpr, "oracle_nodes_per_ray": nodes,
-                         "oracle_tris_per_ray": tris, "kernel_ms_avg": kern_ms, "device_counters": counters,
-                         "l2_measured": l2, "frac_of_l2": achieved / l2_peak,
-                         "note": "achieved counts the algorithmic bytes of the binary reference tree (32 B per "
-                                 "binary node visit, 36 B per triangle test, 40 B of ray and hit); the wide tree "
-                                 "fetches fewer bytes and they hit L1/L2, so the DRAM traffic per launch is the rays "
-                                 "in and hits out only and the kernel is bound by instruction issue, not HBM"},
+            "roofline": roofline,
             "clocks": clk,
-            "scene_info": {k: info[k] for k in ("num_wide_nodes", "num_refs", "wide_depth", "node_bytes", "tri_bytes",
-                                                "build_ms", "collapse_ms")},
         }
         if not args.no_extra:
             blocks = {"path_tracer": path_tracer_block, "incoherent_1m_tris": incoherent_1m_block,
                       "time_to_relmse_1080p": time_to_relmse_block, "batched_256_scenes": batched_block,
                       "large_scene_4k": large_scene_block, "cache_frames": cache_frames_block}
             for name in [x for x in args.extra.split(",") if x]:
-                line[name] = blocks[name](fg, torch, stream, local)
+                blocks_out[name] = blocks[name](fg, torch, stream, local)
+            line.update(target_figures(blocks_out))
         if not args.no_cpu_baseline and world == 1:
-            line["cpu_baseline"] = cpu_baseline(sc, rays)
+            cb = cpu_baseline(sc, rays)
+            blocks_out["cpu_baseline_detail"] = cb
+            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps({"bench_blocks": blocks_out}), flush=True)
         print(json.dumps(line), flush=True)
     scene.close()
     ctx.close()

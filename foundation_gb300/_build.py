@@ -22,6 +22,9 @@ LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libfnd_rt.so")
 DEMO_PATH = os.path.join(LIB_DIR, "fnd_pass_demo")
 RENDERER = os.path.join(PKG, "renderer")
+# measurement kernels of the benchmark (not part of libfnd_rt.so)
+PROBE_SRC = os.path.join(PKG, "probe", "l2_read.cu")
+PROBE_PATH = os.path.join(LIB_DIR, "libfnd_probe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-pthread,-Wall",
@@ -102,7 +105,22 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if verbose:
             print(f"linked {LIB_PATH}", file=sys.stderr)
     _build_demo(force, verbose)
+    _build_probe(force, verbose)
     return LIB_PATH
+
+
+def _build_probe(force: bool, verbose: bool) -> None:
+    """The benchmark's L2 read-bandwidth kernel (probe/l2_read.cu)."""
+    if not force and os.path.exists(PROBE_PATH) and os.path.getmtime(PROBE_SRC) <= os.path.getmtime(PROBE_PATH):
+        return
+    tmp = PROBE_PATH + f".tmp{os.getpid()}"
+    cmd = [nvcc(), *ARCH, *COMMON, "-shared", PROBE_SRC, "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"probe build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, PROBE_PATH)
+    if verbose:
+        print(f"linked {PROBE_PATH}", file=sys.stderr)
 
 
 def _build_demo(force: bool, verbose: bool) -> None:

@@ -21,8 +21,16 @@
 //    or on several streams) race on the array and must be serialised by the
 //    caller;
 //  * the first call on a device resolves the array's device address
-//    (cudaGetSymbolAddress, which may load the module), so that first call
-//    should be made before any stream capture begins.
+//    (cudaGetSymbolAddress). Under lazy module loading that is also when the
+//    driver loads the module and reserves the array, so make the first call
+//    at set-up time, while device memory is still free, and before any
+//    stream capture begins. A failed set-up is not remembered: the next call
+//    tries again;
+//  * it launches with the context's launch shape (fnd_rt_set_trace_config /
+//    fnd_rt_tune) without the coherence sort, whose scratch would need an
+//    allocation; results do not depend on the shape;
+//  * the call is synchronous (it returns once the hits are in `out`) and
+//    leaves the caller's current device as it found it.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -40,34 +48,48 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// Device address of g_noalloc_scratch and launch shape, resolved once per
-// device with that device current. Host code must not use the symbol itself
-// as a pointer: on the host it names a stand-in, not device memory.
+// Device address of g_noalloc_scratch, resolved once per device with that
+// device current. Host code must not use the symbol itself as a pointer: on
+// the host it names a stand-in, not device memory.
 struct DeviceScratch {
-    std::once_flag once;
-    cudaError_t err = cudaSuccess;
+    std::mutex mu;
+    bool ready = false;
     unsigned char* ptr = nullptr;
-    int grid = 0;
 };
 DeviceScratch g_scratch[kMaxDevices];
 
-DeviceScratch& SetUp(int device) {
+// Only a successful set-up is kept; a failure (for example no device memory
+// left for the array when the module loads) clears the CUDA error it left
+// and throws, and the next call tries again.
+unsigned char* ScratchFor(int device) {
     DeviceScratch& s = g_scratch[device];
-    std::call_once(s.once, [&] {
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (!s.ready) {
         void* p = nullptr;
-        s.err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (s.err != cudaSuccess) return;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            Foundation::CApi::CudaCheck(e, "no-allocation scratch set-up (cudaGetSymbolAddress)");
+        }
         s.ptr = static_cast<unsigned char*>(p);
-        int sms = 0, blocks = 0;
-        s.err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        if (s.err != cudaSuccess) return;
-        s.err = Foundation::RT::TraceOccupancy(0, &blocks);
-        if (s.err != cudaSuccess) return;
-        s.grid = sms * (blocks > 0 ? blocks : 1);
-    });
-    if (s.err != cudaSuccess) Foundation::CApi::CudaCheck(s.err, "no-allocation scratch set-up");
-    return s;
+        s.ready = true;
+    }
+    return s.ptr;
 }
+
+// Restores the calling thread's current device on scope exit.
+struct DeviceRestore {
+    int prev = -1;
+    DeviceRestore() {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            (void)cudaGetLastError();
+            prev = -1;
+        }
+    }
+    ~DeviceRestore() {
+        if (prev >= 0) (void)cudaSetDevice(prev);
+    }
+};
 
 }  // namespace
 
@@ -88,16 +110,26 @@ extern "C" int fnd_rt_trace_closest_noalloc(const fnd_rt_scene* scene, const fnd
                    n, kNoAllocMaxRays);
         CHECK_CODE(ctx->device >= 0 && ctx->device < kMaxDevices, FND_ERR_NO_DEVICE, "device ordinal %d",
                    ctx->device);
+        DeviceRestore restore;
         CUDA_CHECK(cudaSetDevice(ctx->device));
-        DeviceScratch& s = SetUp(ctx->device);
+        unsigned char* scratch = ScratchFor(ctx->device);
         if (n == 0) return;
         cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-        uint32_t* counter = reinterpret_cast<uint32_t*>(s.ptr);
+        uint32_t* counter = reinterpret_cast<uint32_t*>(scratch);
         uint32_t* status = counter + 1;
-        unsigned char* d_rays = s.ptr + kHeaderBytes;
+        unsigned char* d_rays = scratch + kHeaderBytes;
         unsigned char* d_hits = d_rays + kRayBytes;
+        // the context's launch shape, in input order (the coherence sort
+        // needs scratch of its own)
+        RT::TraceConfig cfg = ctx->trace_cfg;
+        cfg.sort_bits = 0;
+        int blocks = 0;
+        CUDA_CHECK(RT::TraceOccupancyFor(cfg, 0, &blocks));
+        blocks = blocks > 0 ? blocks : 1;
+        if (cfg.blocks_per_sm > 0 && cfg.blocks_per_sm < blocks) blocks = cfg.blocks_per_sm;
+        const int grid = ctx->sm_count * blocks;
         // the previous call's counter and status must not leak into this one
-        CUDA_CHECK(cudaMemsetAsync(s.ptr, 0, kHeaderBytes, st));
+        CUDA_CHECK(cudaMemsetAsync(scratch, 0, kHeaderBytes, st));
         CUDA_CHECK(cudaMemcpyAsync(d_rays, rays, sizeof(fnd_ray) * (size_t)n, cudaMemcpyHostToDevice, st));
         RT::TraceLaunch L{};
         L.scene = scene->view;
@@ -107,12 +139,12 @@ extern "C" int fnd_rt_trace_closest_noalloc(const fnd_rt_scene* scene, const fnd
         L.counter = counter;
         L.status = status;
         L.refill_min = ctx->refill_min;
-        CUDA_CHECK(RT::LaunchTrace(L, false, false, s.grid, st));
+        CUDA_CHECK(RT::LaunchTraceConfigured(L, false, false, cfg, grid, st));
         CUDA_CHECK(cudaMemcpyAsync(out, d_hits, sizeof(fnd_hit) * (size_t)n, cudaMemcpyDeviceToHost, st));
         uint32_t h_status = 0;
         CUDA_CHECK(cudaMemcpyAsync(&h_status, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
-        CHECK_CODE(h_status == 0, (h_status & RT::kStatusStackOverflow) ? FND_ERR_STACK_OVERFLOW : FND_ERR_INVALID_SCENE,
-                   "device status 0x%x after the no-allocation trace", h_status);
+        const int code = RT::StatusCode(h_status);
+        CHECK_CODE(code == FND_OK, code, "device status 0x%x after the no-allocation trace", h_status);
     });
 }

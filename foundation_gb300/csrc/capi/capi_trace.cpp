@@ -91,10 +91,7 @@ int ReadStatus(fnd_rt_ctx* ctx) {
     if (s == 0) return FND_OK;
     CUDA_CHECK(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
     CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
-    if (s & RT::kStatusStackOverflow) return FND_ERR_STACK_OVERFLOW;
-    if (s & RT::kStatusTimeout) return FND_ERR_TIMEOUT;
-    if (s & RT::kStatusBadIndex) return FND_ERR_INVALID_SCENE;
-    return FND_ERR_CUDA;
+    return RT::StatusCode(s);
 }
 
 }  // namespace CApi

@@ -67,8 +67,7 @@ __global__ void __launch_bounds__(kBlock) generate_kernel(const PathBuffers B, c
     const uint64_t g = wave_base + i;
     const uint32_t pixel = (uint32_t)(g % npix);
     const uint32_t sample = (uint32_t)(g / npix) + R.sample_offset;
-    Pcg32 rng;
-    rng.seed(R.seed * 0x9E3779B97F4A7C15ull + pixel, sample);
+    Pcg32 rng = camera_path_rng(R.seed, pixel, sample);
     const float a = rng.uniform(), b = rng.uniform();
     const uint32_t px = pixel % R.width, py = pixel / R.width;
     const float sx = (2.0f * ((float)px + a) / (float)R.width - 1.0f) * R.tan_half * R.aspect;
@@ -77,7 +76,7 @@ __global__ void __launch_bounds__(kBlock) generate_kernel(const PathBuffers B, c
     B.ext_rays[0][2 * (size_t)i] = make_float4(R.eye[0], R.eye[1], R.eye[2], 0.0f);
     B.ext_rays[0][2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7F800000));
     B.ext_path[0][i] = i;
-    B.rng[i] = make_uint4((uint32_t)rng.state, (uint32_t)(rng.state >> 32), sample, pixel);
+    B.rng[i] = pack_rng(rng, sample, pixel);
     B.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
 }
 
@@ -98,9 +97,7 @@ __global__ void __launch_bounds__(kBlock) shade_kernel(const PathBuffers B, cons
         const float4 r1 = B.ext_rays[cur][2 * (size_t)j + 1];
         const float4 beta4 = B.beta[slot];
         const uint4 rs = B.rng[slot];
-        Pcg32 rng;
-        rng.state = (uint64_t)rs.x | ((uint64_t)rs.y << 32);
-        rng.inc = ((uint64_t)rs.z << 1) | 1u;
+        Pcg32 rng = unpack_rng(rs);
         const uint32_t pixel = rs.w & ~kQueryNextFlag;
         VertexIn in;
         in.o = xyz(r0);
@@ -145,7 +142,7 @@ __global__ void __launch_bounds__(kBlock) shade_kernel(const PathBuffers B, cons
                 make_float4(v.next_d.x, v.next_d.y, v.next_d.z, __int_as_float(0x7F800000));
             B.ext_path[nxt][kn] = slot;
             B.beta[slot] = make_float4(v.beta.x, v.beta.y, v.beta.z, v.pdf);
-            B.rng[slot] = make_uint4((uint32_t)rng.state, (uint32_t)(rng.state >> 32), rs.z, pixel | flags);
+            B.rng[slot] = pack_rng(rng, rs.z, pixel | flags);
         }
     }
 }

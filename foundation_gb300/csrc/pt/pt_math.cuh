@@ -45,6 +45,42 @@ struct Pcg32 {
     __device__ __forceinline__ float uniform() { return (float)(next() >> 8) * (1.0f / 16777216.0f); }
 };
 
+// The generator streams of the path tracer. Every path owns one stream,
+// chosen by its frame seed, pixel and sample, so a path's samples do not
+// depend on which kernel (wavefront stage, tail or training megakernel)
+// draws them.
+//  * camera path (pixel, sample) of a frame seeded frame_seed:
+//    initstate = frame_seed * 0x9E3779B97F4A7C15 + pixel, sequence = sample;
+//  * training path i of a round seeded round_seed (its pixel drawn by the
+//    round's hash): initstate = frame_seed * 0x9E3779B97F4A7C15 + pixel +
+//    0x5851F42D4C957F2D * (i + 1), sequence = 2^30 + (round_seed mod 2^30),
+//    so training streams never share a sequence with camera samples below
+//    2^30.
+__device__ __forceinline__ Pcg32 camera_path_rng(uint64_t frame_seed, uint32_t pixel, uint32_t sample) {
+    Pcg32 g;
+    g.seed(frame_seed * 0x9E3779B97F4A7C15ull + pixel, sample);
+    return g;
+}
+__device__ __forceinline__ Pcg32 training_path_rng(uint64_t frame_seed, uint32_t pixel, uint32_t i,
+                                                   uint32_t round_seed) {
+    Pcg32 g;
+    g.seed(frame_seed * 0x9E3779B97F4A7C15ull + pixel + 0x5851F42D4C957F2Dull * (i + 1ull),
+           0x40000000u + (round_seed & 0x3FFFFFFFu));
+    return g;
+}
+// A camera path's generator in its 16-byte path record: (state low, state
+// high, sequence, w). The increment is rebuilt from the sequence (the
+// sample index), so the record holds the stream exactly.
+__device__ __forceinline__ uint4 pack_rng(const Pcg32& g, uint32_t sequence, uint32_t w) {
+    return make_uint4((uint32_t)g.state, (uint32_t)(g.state >> 32), sequence, w);
+}
+__device__ __forceinline__ Pcg32 unpack_rng(uint4 rec) {
+    Pcg32 g;
+    g.state = (uint64_t)rec.x | ((uint64_t)rec.y << 32);
+    g.inc = ((uint64_t)rec.z << 1) | 1u;
+    return g;
+}
+
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
 __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }

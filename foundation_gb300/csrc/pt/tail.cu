@@ -71,8 +71,7 @@ __global__ void __launch_bounds__(kTailBlock) tail_kernel(const TailArgs A) {
                         const float4 r1 = B.ext_rays[A.q][2 * (size_t)j + 1];
                         const float4 b4 = B.beta[slot];
                         const uint4 rs = B.rng[slot];
-                        rng.state = (uint64_t)rs.x | ((uint64_t)rs.y << 32);
-                        rng.inc = ((uint64_t)rs.z << 1) | 1u;
+                        rng = unpack_rng(rs);
                         pixel = rs.w & ~kQueryNextFlag;
                         flags = rs.w & kQueryNextFlag;
                         o = tl_xyz(r0);

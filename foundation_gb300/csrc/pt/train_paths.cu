@@ -54,9 +54,7 @@ __global__ void __launch_bounds__(kBlock) training_paths_kernel(const TrainPaths
     if (valid) {
         const uint32_t npix = R.width * R.height;
         const uint32_t pixel = hash32(A.seed ^ hash32(i)) % npix;
-        Pcg32 rng;
-        rng.seed(R.seed * 0x9E3779B97F4A7C15ull + pixel + 0x5851F42D4C957F2Dull * (i + 1ull),
-                 0x40000000u + (A.seed & 0x3FFFFFFFu));
+        Pcg32 rng = training_path_rng(R.seed, pixel, i, A.seed);
         const float a = rng.uniform(), b = rng.uniform();
         const uint32_t px = pixel % R.width, py = pixel / R.width;
         const float sx = (2.0f * ((float)px + a) / (float)R.width - 1.0f) * R.tan_half * R.aspect;

@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../../include/fnd_rt.h"
+
 namespace Foundation {
 namespace RT {
 
@@ -12,6 +14,18 @@ namespace RT {
 constexpr uint32_t kStatusStackOverflow = 1u;
 constexpr uint32_t kStatusTimeout = 2u;
 constexpr uint32_t kStatusBadIndex = 4u;  // node / triangle index outside the scene arrays
+
+// The fnd_status a latched status word reports (the first that applies):
+// stack overflow, then a timed-out wait, then a bad index; an unknown bit
+// is reported as a CUDA failure. Every entry point that reads a status word
+// maps it through here.
+inline int StatusCode(uint32_t bits) {
+    if (bits == 0u) return FND_OK;
+    if (bits & kStatusStackOverflow) return FND_ERR_STACK_OVERFLOW;
+    if (bits & kStatusTimeout) return FND_ERR_TIMEOUT;
+    if (bits & kStatusBadIndex) return FND_ERR_INVALID_SCENE;
+    return FND_ERR_CUDA;
+}
 
 constexpr int kMaxStack = 64;  // node-group + triangle-group entries per ray
 

@@ -533,9 +533,16 @@ int fnd_rt_cache_adam_step(fnd_rt_ctx* ctx, const float* grad, float learning_ra
  * about 2.5 MiB, which every GPU that loads this library holds until the
  * process exits; a call takes at most 65,536 rays and larger n is rejected
  * with FND_ERR_INVALID_ARG. The first call on a device resolves the array's
- * address (set-up), so make it before any stream capture. All calls share
- * the array: calls that overlap on the GPU race, so serialise them.
- * stream: cudaStream_t, or NULL for the scene context's stream. Synchronous. */
+ * address (set-up; under lazy module loading the driver may reserve the array
+ * only then), so make that first call at set-up time, while device memory is
+ * still free, and before any stream capture; a set-up that failed is retried
+ * by the next call. All calls share the array and it keeps the last call's
+ * contents (the work counter and status word are cleared at the start of each
+ * call): calls that overlap on the GPU race, so serialise them. The launch
+ * uses the context's launch shape without the coherence sort.
+ * stream: cudaStream_t, or NULL for the scene context's stream. Synchronous:
+ * returns once the hits are in `out`; the caller's current device is left
+ * unchanged. */
 int fnd_rt_trace_closest_noalloc(const fnd_rt_scene* scene, const fnd_ray* rays, uint32_t n, fnd_hit* out,
                                  void* stream);
 

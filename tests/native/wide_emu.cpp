@@ -352,4 +352,33 @@ void emu_trace_single(const emu_bvh* e, const float* rays, uint64_t n, uint32_t*
     }
 }
 
+// RT::trace_single over caller-made node and triangle arrays (planes: v0[nt],
+// v1[nt], v2[nt] as float4), closest hit; *status_out receives the status
+// word the traversal latched (it starts at 0).
+void emu_trace_single_raw(const void* nodes, uint32_t num_nodes, const float* planes, uint32_t num_tris,
+                          const float* rays, uint64_t n, uint32_t* hits, uint32_t* status_out) {
+    DeviceScene sc{};
+    sc.nodes = static_cast<const uint4*>(nodes);
+    const float4* pl = reinterpret_cast<const float4*>(planes);
+    sc.v0 = pl;
+    sc.v1 = pl + num_tris;
+    sc.v2 = pl + 2 * (size_t)num_tris;
+    sc.num_nodes = num_nodes;
+    sc.num_tris = num_tris;
+    uint32_t status = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* rp = rays + 8 * i;
+        const RayState r = setup_ray(float4{rp[0], rp[1], rp[2], rp[3]}, float4{rp[4], rp[5], rp[6], rp[7]});
+        float t = r.tmax;
+        uint32_t p = FND_INVALID_ID;
+        const bool h = trace_single<false>(sc, r, t, p, &status);
+        hits[2 * i] = h ? p : FND_INVALID_ID;
+        hits[2 * i + 1] = h ? __float_as_uint(t) : 0x7F800000u;
+    }
+    *status_out = status;
+}
+
+// The fnd_status every entry point reports for a latched status word.
+int emu_status_code(uint32_t bits) { return StatusCode(bits); }
+
 }  // extern "C"

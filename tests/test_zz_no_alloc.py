@@ -74,3 +74,31 @@ def test_noalloc_rejects_batches_over_the_limit(built):
         assert lib.fnd_rt_trace_closest_noalloc(scene.handle, _p(ok), len(ok), _p(out_ok), None) == 0
         assert (out_ok["prim"] == 0).all() and (out_ok["t"] == 1.0).all()
         scene.close()
+
+
+def test_noalloc_on_a_caller_stream_and_empty_batch(built):
+    """A caller-supplied stream (not the context's) under a non-default
+    launch shape gives the same hits, and n == 0 returns success without
+    touching the buffers."""
+    import torch
+    import foundation_gb300 as fg
+    from foundation_gb300 import rt
+    lib = rt.load()
+    with fg.Context(0) as ctx:
+        cs = S.cornell_scene()
+        scene = ctx.upload(cs.verts, cs.idx, spatial_splits=True, split_budget=8.0, sah_collapse=True)
+        rays = S.incoherent_rays(40000, *cs.bounds, seed=5)
+        ref = scene.closest(rays)
+        # a launch shape other than the default (64-thread blocks, short stack 4)
+        ctx.set_trace_config(block=64, short_stack=4, refill_min=16)
+        side = torch.cuda.Stream(device=0)
+        out = np.empty(len(rays), fg.HIT_DTYPE)
+        rc = lib.fnd_rt_trace_closest_noalloc(scene.handle, _p(rays), len(rays), _p(out), C.c_void_p(side.cuda_stream))
+        assert rc == 0, lib.fnd_rt_last_error(ctx.handle)
+        assert np.array_equal(out["prim"], ref["prim"])
+        assert np.array_equal(out["t"].view(np.uint32), ref["t"].view(np.uint32))
+        empty = np.empty(1, fg.HIT_DTYPE)
+        empty["prim"] = 7
+        assert lib.fnd_rt_trace_closest_noalloc(scene.handle, None, 0, _p(empty), None) == 0
+        assert empty["prim"][0] == 7
+        scene.close()
