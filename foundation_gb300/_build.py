@@ -126,7 +126,7 @@ def _build_probe(force: bool, verbose: bool) -> None:
 def _build_demo(force: bool, verbose: bool) -> None:
     """The C++ path-tracer pass (renderer/) and its headless driver, linked
     against libfnd_rt.so with an $ORIGIN rpath."""
-    srcs = sorted(glob.glob(os.path.join(RENDERER, "*.cpp"))) + [os.path.join(CSRC, "core", "core.cpp")]
+    srcs = sorted(glob.glob(os.path.join(RENDERER, "*.cpp")))
     deps = srcs + glob.glob(os.path.join(RENDERER, "*.hpp")) + _headers() + [LIB_PATH]
     if not force and os.path.exists(DEMO_PATH) and \
             all(os.path.getmtime(d) <= os.path.getmtime(DEMO_PATH) for d in deps):

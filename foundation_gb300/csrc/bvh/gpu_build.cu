@@ -714,7 +714,7 @@ double Ms(std::chrono::steady_clock::time_point t0) {
 
 void Check(cudaError_t e, const char* what) {
     if (e != cudaSuccess)
-        Core::Fail(e == cudaErrorMemoryAllocation ? FND_ERR_OUT_OF_MEMORY : FND_ERR_CUDA, "%s: %s", what,
+        RtCore::Fail(e == cudaErrorMemoryAllocation ? FND_ERR_OUT_OF_MEMORY : FND_ERR_CUDA, "%s: %s", what,
                    cudaGetErrorString(e));
 }
 

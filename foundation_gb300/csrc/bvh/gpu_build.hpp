@@ -40,7 +40,7 @@ struct GpuBuildOutput {
 };
 
 // d_verts: 3 * nv floats, d_idx: 3 * nt indices, both device memory. Fails
-// (Core::FndError) on invalid input: FND_ERR_INVALID_ARG for an index out of
+// (RtCore::FndError) on invalid input: FND_ERR_INVALID_ARG for an index out of
 // range or a non-finite coordinate, FND_ERR_INVALID_SCENE when the tree is
 // deeper than the traversal stack allows. Temporary buffers are freed.
 void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint32_t nt, const GpuBuildParams& p,

@@ -30,7 +30,7 @@ struct InstanceTop {
 // FP32. False for a singular or non-finite transform.
 bool InstanceInverse(const float* m, float inv[12]);
 
-// Builds the top level; fails (Core::FndError) on a singular transform.
+// Builds the top level; fails (RtCore::FndError) on a singular transform.
 void BuildInstanceTop(const InstanceInput* in, uint32_t n, InstanceTop& out);
 
 // Largest |coordinate| of the world box's corners mapped by `inv` (FP64 of the

@@ -133,7 +133,7 @@ RT::TraceConfig RunTuner(fnd_rt_ctx* ctx, uint32_t reps,
     cudaEventDestroy(e1);
     if (table_n) *table_n = std::min(k, table_cap);
     const int s = CApi::ReadStatus(ctx);
-    if (s != FND_OK) Core::Fail(s, "device status %d while tuning", s);
+    if (s != FND_OK) RtCore::Fail(s, "device status %d while tuning", s);
     return best;
 }
 

@@ -10,7 +10,7 @@
 
 using namespace Foundation;
 using Foundation::CApi::Guard;
-using Foundation::Core::Fail;
+using Foundation::RtCore::Fail;
 
 namespace Foundation {
 namespace CApi {

@@ -16,7 +16,7 @@
 
 using namespace Foundation;
 using Foundation::CApi::Guard;
-using Foundation::Core::Fail;
+using Foundation::RtCore::Fail;
 
 namespace {
 

@@ -19,8 +19,8 @@
 #include "context.hpp"
 
 using namespace Foundation;
-using Foundation::Core::Fail;
-using Foundation::Core::FndError;
+using Foundation::RtCore::Fail;
+using Foundation::RtCore::FndError;
 
 namespace {
 

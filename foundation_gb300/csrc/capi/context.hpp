@@ -74,7 +74,6 @@ struct fnd_rt_ctx {
     fnd_render_stats last_render{};
     FndCacheState* cache = nullptr;
     std::string last_error;
-    Foundation::Core::HeapAllocator allocator;
 };
 
 struct fnd_rt_scene {
@@ -114,7 +113,7 @@ int Guard(fnd_rt_ctx* ctx, F&& body) {
         body();
         err->clear();
         return FND_OK;
-    } catch (const Foundation::Core::FndError& e) {
+    } catch (const Foundation::RtCore::FndError& e) {
         *err = e.what();
         LOG_RUNTIME(FndRt, ERR, "%s", e.what());
         return e.code();

@@ -4,7 +4,7 @@
 #include <mutex>
 
 namespace Foundation {
-namespace Core {
+namespace RtCore {
 
 int LogLevel() {
     static const int level = [] {
@@ -26,5 +26,5 @@ void LogWrite(const char* tag, int level, const char* fmt, ...) {
     std::fprintf(stderr, "[%s] [%s] %s\n", tag, names[level < 0 ? 0 : (level > 3 ? 3 : level)], buf);
 }
 
-}  // namespace Core
+}  // namespace RtCore
 }  // namespace Foundation

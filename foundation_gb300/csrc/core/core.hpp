@@ -1,6 +1,7 @@
-// core.hpp — host-side conventions of the Foundation codebase, restated
-// without its third-party dependencies (spdlog, fmt and mimalloc are not
-// available here):
+// core.hpp — host-side conventions inside libfnd_rt.so, in the shape of the
+// Foundation codebase but in a namespace of their own (Foundation::RtCore),
+// so the library's symbols never meet the host application's
+// Foundation::Core (its Allocator, BugCheck, logging) in one process:
 //  * CHECK(expr): the reference routes a failed check to BugCheck and
 //    terminates (src/Core/Core.hpp:17, src/Core/Core.cpp:7-10). Inside this
 //    library a failed check throws FndError instead, and the C ABI layer turns
@@ -9,9 +10,8 @@
 //  * LOG_RUNTIME(TAG, level, fmt, ...): tagged logging in the shape of
 //    src/Core/Logging.hpp:34-35, printf-style, to stderr, filtered by the
 //    FND_LOG_LEVEL environment variable (0 = off, 1 = err, 2 = warn, 3 = info).
-//  * Allocator: the polymorphic host allocator interface of
-//    src/Core/Allocator/Allocator.hpp:17-41 (Allocate / Deallocate /
-//    GetUsedMemory), with a counting heap implementation.
+// The C++ pass that a Foundation build compiles (renderer/) takes the
+// application's Foundation::Core::Allocator instead (renderer/FoundationCore.hpp).
 #pragma once
 
 #include <atomic>
@@ -27,7 +27,7 @@
 #include "../../../include/fnd_rt.h"
 
 namespace Foundation {
-namespace Core {
+namespace RtCore {
 
 class FndError : public std::runtime_error {
 public:
@@ -50,43 +50,7 @@ private:
 int LogLevel();
 void LogWrite(const char* tag, int level, const char* fmt, ...);
 
-class Allocator {
-public:
-    using size_type = std::size_t;
-    using pointer = void*;
-    virtual ~Allocator() = default;
-    virtual pointer Allocate(size_type size, size_t alignment) = 0;
-    virtual void Deallocate(pointer ptr, size_type size) = 0;
-    virtual size_type GetUsedMemory() const noexcept = 0;
-};
-
-// Heap allocator that counts live bytes (thread-safe counter). Every block is
-// 64-byte aligned; larger alignments are rejected.
-class HeapAllocator final : public Allocator {
-public:
-    static constexpr size_t kAlign = 64;
-    pointer Allocate(size_type size, size_t alignment) override {
-        CHECK_ALIGN(alignment);
-        void* p = ::operator new(size ? size : 1, std::align_val_t(kAlign), std::nothrow);
-        if (!p) Fail(FND_ERR_OUT_OF_MEMORY, "host allocation of %zu bytes failed", size);
-        m_used.fetch_add(size, std::memory_order_relaxed);
-        return p;
-    }
-    void Deallocate(pointer ptr, size_type size) override {
-        if (!ptr) return;
-        ::operator delete(ptr, std::align_val_t(kAlign));
-        m_used.fetch_sub(size, std::memory_order_relaxed);
-    }
-    size_type GetUsedMemory() const noexcept override { return m_used.load(std::memory_order_relaxed); }
-
-private:
-    static void CHECK_ALIGN(size_t alignment) {
-        if (alignment > kAlign) Fail(FND_ERR_INVALID_ARG, "alignment %zu above %zu", alignment, kAlign);
-    }
-    std::atomic<size_type> m_used{0};
-};
-
-}  // namespace Core
+}  // namespace RtCore
 }  // namespace Foundation
 
 #define FND_STR2(x) #x
@@ -94,12 +58,12 @@ private:
 #define CHECK(expr)                                                                                         \
     do {                                                                                                    \
         if (!(expr))                                                                                        \
-            ::Foundation::Core::Fail(FND_ERR_INVALID_ARG, "Check Failed: " #expr " (" __FILE__ ":" FND_STR( \
+            ::Foundation::RtCore::Fail(FND_ERR_INVALID_ARG, "Check Failed: " #expr " (" __FILE__ ":" FND_STR( \
                                                               __LINE__) ")");                               \
     } while (0)
 #define CHECK_CODE(expr, code, ...)                                    \
     do {                                                               \
-        if (!(expr)) ::Foundation::Core::Fail((code), __VA_ARGS__);    \
+        if (!(expr)) ::Foundation::RtCore::Fail((code), __VA_ARGS__);    \
     } while (0)
 
 #define FND_LOG_ERR 1
@@ -107,6 +71,6 @@ private:
 #define FND_LOG_INFO 3
 #define LOG_RUNTIME(TAG, LEVEL, ...)                                                                  \
     do {                                                                                              \
-        if (::Foundation::Core::LogLevel() >= FND_LOG_##LEVEL)                                        \
-            ::Foundation::Core::LogWrite(#TAG, FND_LOG_##LEVEL, __VA_ARGS__);                         \
+        if (::Foundation::RtCore::LogLevel() >= FND_LOG_##LEVEL)                                        \
+            ::Foundation::RtCore::LogWrite(#TAG, FND_LOG_##LEVEL, __VA_ARGS__);                         \
     } while (0)

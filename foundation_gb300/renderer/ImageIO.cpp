@@ -9,10 +9,11 @@
 
 #include <array>
 #include <cstdio>
+#include <stdexcept>
+#include <string>
 #include <vector>
 
-#include "../../include/fnd_rt.h"
-#include "../csrc/core/core.hpp"
+#include "FoundationCore.hpp"
 
 namespace Foundation {
 namespace Renderer {
@@ -58,13 +59,13 @@ void Chunk(std::FILE* f, const char type[4], const std::vector<uint8_t>& data) {
 void WritePfm(const char* path, std::span<const float> rgb, uint32_t w, uint32_t h) {
     CHECK(rgb.size() >= 3ull * w * h);
     std::FILE* f = std::fopen(path, "wb");
-    CHECK_CODE(f != nullptr, FND_ERR_IO, "cannot write %s", path);
+    if (f == nullptr) throw std::runtime_error(std::string("cannot write ") + path);
     std::fprintf(f, "PF\n%u %u\n-1.0\n", w, h);
     bool ok = true;
     for (uint32_t y = 0; y < h; ++y)  // PFM rows run bottom to top
         ok = ok && std::fwrite(&rgb[3 * (size_t)(h - 1 - y) * w], sizeof(float), 3 * (size_t)w, f) == 3 * (size_t)w;
     ok = (std::fclose(f) == 0) && ok;
-    CHECK_CODE(ok, FND_ERR_IO, "write to %s failed", path);
+    if (!ok) throw std::runtime_error(std::string("write to ") + path + " failed");
 }
 
 void WritePng(const char* path, std::span<const uint8_t> rgba, uint32_t w, uint32_t h) {
@@ -98,13 +99,13 @@ void WritePng(const char* path, std::span<const uint8_t> rgba, uint32_t w, uint3
     Put32(ihdr, h);
     ihdr.insert(ihdr.end(), {8, 6, 0, 0, 0});  // 8-bit, RGBA, deflate, filter method 0, no interlace
     std::FILE* f = std::fopen(path, "wb");
-    CHECK_CODE(f != nullptr, FND_ERR_IO, "cannot write %s", path);
+    if (f == nullptr) throw std::runtime_error(std::string("cannot write ") + path);
     static const uint8_t sig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
     std::fwrite(sig, 1, 8, f);
     Chunk(f, "IHDR", ihdr);
     Chunk(f, "IDAT", z);
     Chunk(f, "IEND", {});
-    CHECK_CODE(std::fclose(f) == 0, FND_ERR_IO, "write to %s failed", path);
+    if (std::fclose(f) != 0) throw std::runtime_error(std::string("write to ") + path + " failed");
 }
 
 }  // namespace Renderer

@@ -1,16 +1,29 @@
 // ObjLoader.cpp — see ObjLoader.hpp.
 #include "ObjLoader.hpp"
 
+#include <cstdarg>
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <map>
 #include <sstream>
-
-#include "../csrc/core/core.hpp"
+#include <stdexcept>
 
 namespace Foundation {
 namespace Renderer {
 namespace {
+
+// A malformed or unreadable file: std::runtime_error with the formatted
+// message (the exception the reference's constructors throw on failures,
+// src/Platform/RHI/Vulkan/Device.cpp:195,203).
+[[noreturn]] void IoFail(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    throw std::runtime_error(buf);
+}
 
 std::string DirOf(const std::string& p) {
     const size_t s = p.find_last_of('/');
@@ -28,7 +41,7 @@ fnd_material DefaultMaterial() {
 
 void LoadMtl(const std::string& path, std::map<std::string, uint32_t>& names, std::vector<fnd_material>& mats) {
     std::ifstream in(path);
-    if (!in) Core::Fail(FND_ERR_IO, "cannot open material library %s", path.c_str());
+    if (!in) IoFail("cannot open material library %s", path.c_str());
     std::string line;
     fnd_material* cur = nullptr;
     bool metallic = false;
@@ -75,7 +88,7 @@ int64_t ParseIndex(const std::string& tok, int64_t nverts) {
 
 ObjScene LoadObj(const std::string& path) {
     std::ifstream in(path);
-    if (!in) Core::Fail(FND_ERR_IO, "cannot open %s", path.c_str());
+    if (!in) IoFail("cannot open %s", path.c_str());
     ObjScene s;
     std::map<std::string, uint32_t> names;
     uint32_t current = 0;
@@ -94,7 +107,7 @@ ObjScene LoadObj(const std::string& path) {
                 fnd_quad_light q{};
                 ss >> q.corner[0] >> q.corner[1] >> q.corner[2] >> q.edge_u[0] >> q.edge_u[1] >> q.edge_u[2] >>
                     q.edge_v[0] >> q.edge_v[1] >> q.edge_v[2] >> q.radiance[0] >> q.radiance[1] >> q.radiance[2];
-                if (!ss) Core::Fail(FND_ERR_IO, "%s:%zu: malformed quad_light", path.c_str(), lineno);
+                if (!ss) IoFail("%s:%zu: malformed quad_light", path.c_str(), lineno);
                 s.lights.push_back(q);
             }
             continue;
@@ -102,7 +115,7 @@ ObjScene LoadObj(const std::string& path) {
         if (key[0] == '#') continue;
         if (key == "v") {
             float x, y, z;
-            if (!(ss >> x >> y >> z)) Core::Fail(FND_ERR_IO, "%s:%zu: malformed vertex", path.c_str(), lineno);
+            if (!(ss >> x >> y >> z)) IoFail("%s:%zu: malformed vertex", path.c_str(), lineno);
             s.verts.insert(s.verts.end(), {x, y, z});
         } else if (key == "f") {
             std::vector<int64_t> poly;
@@ -110,10 +123,10 @@ ObjScene LoadObj(const std::string& path) {
             const int64_t nv = (int64_t)(s.verts.size() / 3);
             while (ss >> tok) {
                 const int64_t i = ParseIndex(tok, nv);
-                if (i < 0 || i >= nv) Core::Fail(FND_ERR_IO, "%s:%zu: face index out of range", path.c_str(), lineno);
+                if (i < 0 || i >= nv) IoFail("%s:%zu: face index out of range", path.c_str(), lineno);
                 poly.push_back(i);
             }
-            if (poly.size() < 3) Core::Fail(FND_ERR_IO, "%s:%zu: face with fewer than 3 vertices", path.c_str(), lineno);
+            if (poly.size() < 3) IoFail("%s:%zu: face with fewer than 3 vertices", path.c_str(), lineno);
             if (s.materials.empty()) {
                 s.materials.push_back(DefaultMaterial());
                 have_default = true;
@@ -138,7 +151,7 @@ ObjScene LoadObj(const std::string& path) {
             std::string name;
             ss >> name;
             auto it = names.find(name);
-            if (it == names.end()) Core::Fail(FND_ERR_IO, "%s:%zu: unknown material %s", path.c_str(), lineno, name.c_str());
+            if (it == names.end()) IoFail("%s:%zu: unknown material %s", path.c_str(), lineno, name.c_str());
             current = it->second;
         }
     }

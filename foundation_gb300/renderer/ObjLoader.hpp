@@ -17,7 +17,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/fnd_rt.h"
+#include <fnd_rt.h>
 
 namespace Foundation {
 namespace Renderer {
@@ -30,7 +30,7 @@ struct ObjScene {
     std::vector<fnd_quad_light> lights;
 };
 
-// Throws Core::FndError (FND_ERR_IO / FND_ERR_INVALID_ARG) on failure.
+// Throws std::runtime_error on an unreadable or malformed file.
 ObjScene LoadObj(const std::string& path);
 
 }  // namespace Renderer

@@ -2,6 +2,8 @@
 #include "PathTracerPass.hpp"
 
 #include <cstring>
+#include <stdexcept>
+#include <string>
 
 namespace Foundation {
 namespace Renderer {
@@ -25,8 +27,12 @@ PathTracerPass::~PathTracerPass() {
     if (m_frame) m_allocator->Deallocate(m_frame, m_frame_bytes);
 }
 
+// A failed library call is a failed check in the application's idiom:
+// BugCheck with the call, its fnd_status and the library's message.
 void PathTracerPass::Check(int rc, const char* what) const {
-    if (rc != FND_OK) Core::Fail(rc, "%s failed (%d): %s", what, rc, fnd_rt_last_error(m_ctx));
+    if (rc != FND_OK)
+        Core::BugCheck(std::runtime_error(std::string(what) + " failed (" + std::to_string(rc) +
+                                          "): " + fnd_rt_last_error(m_ctx)));
 }
 
 void PathTracerPass::SetScene(const SceneDesc& s) {

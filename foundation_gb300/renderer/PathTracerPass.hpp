@@ -13,8 +13,9 @@
 #include <span>
 #include <string>
 
-#include "../../include/fnd_rt.h"
-#include "../csrc/core/core.hpp"
+#include <fnd_rt.h>
+
+#include "FoundationCore.hpp"
 
 namespace Foundation {
 namespace Renderer {
