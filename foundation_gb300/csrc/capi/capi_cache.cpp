@@ -37,11 +37,12 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
     const uint32_t qcap = std::max(query_cap, c.query_cap), scap = std::max(samples, c.sample_cap);
     const size_t P = NRC::kNumParams;
     const size_t sizes[] = {
-        sizeof(uint16_t) * NRC::kFwdElems, sizeof(uint16_t) * NRC::kBwdElems,
+        sizeof(uint16_t) * NRC::kFwdElems, sizeof(uint16_t) * NRC::kUFwdElems,
         4 * P, 4 * P, 4 * P, 4 * P,            // master, m, v, grad
         sizeof(double) * 4,                    // loss
         sizeof(NRC::TrainSample) * scap, sizeof(float4) * scap, sizeof(NRC::CachePoint) * qcap, 256,
         sizeof(uint16_t) * NRC::kFwdElems, 4 * P,  // weight average: query image, fp32 average
+        sizeof(uint16_t) * NRC::kUBwdElems,        // tcgen05 backward images
     };
     size_t total = 0;
     for (size_t sz : sizes) total += Align256(sz);
@@ -55,7 +56,7 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
     };
     NRC::Net net = c.net;
     net.fwd = reinterpret_cast<uint16_t*>(take(sizes[0]));
-    net.bwd = reinterpret_cast<uint16_t*>(take(sizes[1]));
+    net.ufwd = reinterpret_cast<uint16_t*>(take(sizes[1]));
     net.master = reinterpret_cast<float*>(take(sizes[2]));
     net.adam_m = reinterpret_cast<float*>(take(sizes[3]));
     net.adam_v = reinterpret_cast<float*>(take(sizes[4]));
@@ -65,11 +66,13 @@ void EnsureCacheBuffers(fnd_rt_ctx* ctx, uint32_t query_cap, uint32_t max_depth)
     net.fwd_avg = averaging ? reinterpret_cast<uint16_t*>(take(sizes[11])) : nullptr;
     net.avg = averaging ? reinterpret_cast<float*>(take(sizes[12])) : nullptr;
     net.avg_decay = c.desc.weight_average;
+    net.ubwd = reinterpret_cast<uint16_t*>(take(sizes[13]));
     if (c.d_block) {
         if (c.train_stream) CUDA_CHECK(cudaStreamSynchronize(c.train_stream));
         // keep the trained state: copy the network, moments and images across
         CUDA_CHECK(cudaMemcpyAsync(net.fwd, c.net.fwd, sizes[0], cudaMemcpyDeviceToDevice, ctx->stream));
-        CUDA_CHECK(cudaMemcpyAsync(net.bwd, c.net.bwd, sizes[1], cudaMemcpyDeviceToDevice, ctx->stream));
+        CUDA_CHECK(cudaMemcpyAsync(net.ufwd, c.net.ufwd, sizes[1], cudaMemcpyDeviceToDevice, ctx->stream));
+        CUDA_CHECK(cudaMemcpyAsync(net.ubwd, c.net.ubwd, sizes[13], cudaMemcpyDeviceToDevice, ctx->stream));
         CUDA_CHECK(cudaMemcpyAsync(net.master, c.net.master, 4 * P, cudaMemcpyDeviceToDevice, ctx->stream));
         CUDA_CHECK(cudaMemcpyAsync(net.adam_m, c.net.adam_m, 4 * P, cudaMemcpyDeviceToDevice, ctx->stream));
         CUDA_CHECK(cudaMemcpyAsync(net.adam_v, c.net.adam_v, 4 * P, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -292,7 +295,7 @@ int fnd_rt_cache_gradient(fnd_rt_ctx* ctx, const float* features, const float* t
         CUDA_CHECK(cudaMemcpyAsync(d, features, in_b, cudaMemcpyHostToDevice, ctx->stream));
         CUDA_CHECK(cudaMemcpyAsync(d + in_b, targets, t_b, cudaMemcpyHostToDevice, ctx->stream));
         CUDA_CHECK(NRC::GradRaw(c.net, reinterpret_cast<const float*>(d), reinterpret_cast<const float*>(d + in_b), n,
-                                ctx->stream));
+                                ctx->d_status, ctx->stream));
         double l = 0.0;
         CUDA_CHECK(cudaMemcpyAsync(grad, c.net.grad, 4ull * NRC::kNumParams, cudaMemcpyDeviceToHost, ctx->stream));
         CUDA_CHECK(cudaMemcpyAsync(&l, c.net.loss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

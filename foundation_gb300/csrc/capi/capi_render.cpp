@@ -408,11 +408,13 @@ int fnd_rt_render(fnd_rt_ctx* ctx, const fnd_rt_scene* scene, const fnd_render_d
             T.sample_count = cs.counters + 1;
             T.sample_cap = cs.sample_cap;
             T.status = ctx->d_status;
-            CUDA_CHECK(PT::LaunchTrainingPaths(T, ts));
-            const int grid_train = std::max(1, std::min<int>((int)((cd.batch + 63) / 64), ctx->sm_count));
+            T.fetch = cs.counters + 2;
+            int& occ = ctx->train_paths_blocks_per_sm[scene->two_level ? 1 : 0];
+            if (occ == 0) occ = PT::TrainingPathsBlocksPerSm(scene->two_level);
+            CUDA_CHECK(PT::LaunchTrainingPaths(T, ctx->sm_count * occ, ts));
             for (uint32_t st = 0; st < cd.train_steps; ++st)
                 CUDA_CHECK(NRC::TrainStep(cs.net, cs.samples, cs.targets, cs.counters + 1, cd.batch,
-                                          Mix32(tseed, st + 1), cd.learning_rate, grid_train, ts));
+                                          Mix32(tseed, st + 1), cd.learning_rate, ctx->d_status, ts));
             CUDA_CHECK(cudaEventRecord(cs.ev_trained, ts));
             cs.frames++;
             if (train_only) {

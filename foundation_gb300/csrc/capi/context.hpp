@@ -69,6 +69,7 @@ struct fnd_rt_ctx {
     size_t rgb_cap = 0;
     unsigned long long* d_render_stats = nullptr;  // [0] extension rays, [1] shadow rays
     int tail_blocks_per_sm[2] = {0, 0};            // occupancy of the tail megakernel, one- / two-level (0: not queried)
+    int train_paths_blocks_per_sm[2] = {0, 0};     // occupancy of the training-path megakernel (0: not queried)
     void* d_sort = nullptr;                        // coherence-order scratch (rt/ray_sort.hpp)
     size_t d_sort_cap = 0;
     fnd_render_stats last_render{};

@@ -101,8 +101,12 @@ struct TrainPathsArgs {
     uint32_t* sample_count;
     uint32_t sample_cap;
     uint32_t* status;
+    uint32_t* fetch;  // path-fetch counter (zeroed by the launch)
 };
-cudaError_t LaunchTrainingPaths(const TrainPathsArgs& A, cudaStream_t s);
+// grid: the persistent grid (SMs x TrainingPathsBlocksPerSm), capped at the
+// blocks the paths need.
+cudaError_t LaunchTrainingPaths(const TrainPathsArgs& A, int grid, cudaStream_t s);
+int TrainingPathsBlocksPerSm(bool two_level);
 
 constexpr uint32_t kQueryNextFlag = 0x80000000u;  // in PathBuffers::rng.w
 
