@@ -474,29 +474,5 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
     (void)nt;
 }
 
-uint32_t IndexTrianglePlanes(const WideBvh& w, uint32_t nt, std::vector<float>& v0, std::vector<float>& v1,
-                             std::vector<float>& v2, std::vector<uint32_t>& index) {
-    const size_t nrefs = w.v0.size() / 4;
-    std::vector<uint32_t> slot(nt, 0xFFFFFFFFu);
-    index.resize(nrefs);
-    v0.clear();
-    v1.clear();
-    v2.clear();
-    uint32_t count = 0;
-    for (size_t r = 0; r < nrefs; ++r) {
-        uint32_t id;
-        std::memcpy(&id, &w.v0[4 * r + 3], 4);
-        if (id >= nt) RtCore::Fail(FND_ERR_INVALID_SCENE, "triangle reference %zu names triangle %u of %u", r, id, nt);
-        if (slot[id] == 0xFFFFFFFFu) {
-            slot[id] = count++;
-            v0.insert(v0.end(), &w.v0[4 * r], &w.v0[4 * r] + 4);
-            v1.insert(v1.end(), &w.v1[4 * r], &w.v1[4 * r] + 4);
-            v2.insert(v2.end(), &w.v2[4 * r], &w.v2[4 * r] + 4);
-        }
-        index[r] = slot[id];
-    }
-    return count;
-}
-
 }  // namespace RT
 }  // namespace Foundation

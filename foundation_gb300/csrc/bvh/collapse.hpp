@@ -67,13 +67,5 @@ struct CollapseOptions {
 void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh& out, float margin_scale = 1.0f,
                     const CollapseOptions& opt = CollapseOptions{});
 
-// Triangle planes stored once per triangle: the references of w (leaf
-// order) are mapped to the first reference of their triangle, whose planes
-// take the next slot, so the planes stay in leaf order of first use. index
-// gets one slot per reference; v0 / v1 / v2 get 4 floats per slot. Returns
-// the slot count (the distinct triangles the leaves hold).
-uint32_t IndexTrianglePlanes(const WideBvh& w, uint32_t nt, std::vector<float>& v0, std::vector<float>& v1,
-                             std::vector<float>& v2, std::vector<uint32_t>& index);
-
 }  // namespace RT
 }  // namespace Foundation

@@ -111,8 +111,6 @@ int fnd_rt_instances_upload(fnd_rt_ctx* ctx, const fnd_rt_instance* instances, u
             scene->view.v2 = reinterpret_cast<const float4*>(tris + 32ull * n);
             scene->view.num_nodes = I.num_wide_nodes;
             scene->view.num_tris = n;
-            scene->view.tri_index = nullptr;  // the top level's leaves are the instances themselves
-            scene->view.num_planes = n;
         }
         // shading records by global id: world normals of every instance's triangles
         {

@@ -185,8 +185,6 @@ void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, ui
     scene->view.v2 = reinterpret_cast<const float4*>(tris + 2 * plane);
     scene->view.num_nodes = scene->info.num_wide_nodes;
     scene->view.num_tris = scene->info.num_refs;
-    scene->view.tri_index = nullptr;
-    scene->view.num_planes = scene->info.num_refs;
 }
 
 }  // namespace
@@ -325,7 +323,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         CHECK_CODE(bp.max_leaf >= 1 && bp.max_leaf <= 4, FND_ERR_INVALID_ARG, "max_leaf_tris %u not in [1, 4]",
                    bp.max_leaf);
         CHECK_CODE(!bvh || (bvh->flags & ~(uint32_t)(FND_BVH_SPATIAL_SPLITS | FND_BVH_GPU_BUILD |
-                                                     FND_BVH_SAH_COLLAPSE | FND_BVH_INDEXED_TRIANGLES)) == 0,
+                                                     FND_BVH_SAH_COLLAPSE)) == 0,
                    FND_ERR_INVALID_ARG, "unknown BVH flags 0x%x", bvh ? bvh->flags : 0u);
         RT::CollapseOptions copt;
         copt.sah = bvh && (bvh->flags & FND_BVH_SAH_COLLAPSE);
@@ -427,14 +425,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         I.wide_depth = wide.depth;
         I.node_bytes = wide.nodes.size() * sizeof(RT::WideNode);
         I.num_refs = (uint32_t)bin.prims.size();
-        // planes once per triangle plus an index per reference when the
-        // tree repeats triangles (or on request)
-        const bool indexed = (bvh && (bvh->flags & FND_BVH_INDEXED_TRIANGLES)) ||
-                             (uint64_t)I.num_refs * 2 >= (uint64_t)nt * 3;
-        std::vector<float> u0, u1, u2;
-        std::vector<uint32_t> tindex;
-        const uint32_t nplanes = indexed ? RT::IndexTrianglePlanes(wide, nt, u0, u1, u2, tindex) : I.num_refs;
-        I.tri_bytes = 3ull * 16ull * nplanes + (indexed ? 4ull * I.num_refs : 0ull);
+        I.tri_bytes = 3ull * 16ull * I.num_refs;
         for (int a = 0; a < 3; ++a) {
             I.bounds_lo[a] = wide.lo[a];
             I.bounds_hi[a] = wide.hi[a];
@@ -445,14 +436,11 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             CUDA_CHECK(cudaMalloc(&scene->d_nodes, I.node_bytes));
             CUDA_CHECK(cudaMalloc(&scene->d_tris, I.tri_bytes));
             char* tris = static_cast<char*>(scene->d_tris);
-            const size_t plane = 16ull * nplanes;
+            const size_t plane = 16ull * I.num_refs;
             CUDA_CHECK(cudaMemcpy(scene->d_nodes, wide.nodes.data(), I.node_bytes, cudaMemcpyHostToDevice));
-            CUDA_CHECK(cudaMemcpy(tris, indexed ? u0.data() : wide.v0.data(), plane, cudaMemcpyHostToDevice));
-            CUDA_CHECK(cudaMemcpy(tris + plane, indexed ? u1.data() : wide.v1.data(), plane, cudaMemcpyHostToDevice));
-            CUDA_CHECK(
-                cudaMemcpy(tris + 2 * plane, indexed ? u2.data() : wide.v2.data(), plane, cudaMemcpyHostToDevice));
-            if (indexed)
-                CUDA_CHECK(cudaMemcpy(tris + 3 * plane, tindex.data(), 4ull * I.num_refs, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(tris, wide.v0.data(), plane, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(tris + plane, wide.v1.data(), plane, cudaMemcpyHostToDevice));
+            CUDA_CHECK(cudaMemcpy(tris + 2 * plane, wide.v2.data(), plane, cudaMemcpyHostToDevice));
             CUDA_CHECK(cudaMalloc(&scene->d_tri_shade, 16ull * nt));
             CUDA_CHECK(cudaMemcpy(scene->d_tri_shade, scene->tri_shade.data(), 16ull * nt, cudaMemcpyHostToDevice));
             std::vector<float>().swap(scene->tri_shade);  // the device copy is the only one kept
@@ -466,15 +454,13 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         }
         I.upload_ms = MsSince(t0);
         char* tris = static_cast<char*>(scene->d_tris);
-        const size_t plane = 16ull * nplanes;
+        const size_t plane = 16ull * I.num_refs;
         scene->view.nodes = static_cast<const uint4*>(scene->d_nodes);
         scene->view.v0 = reinterpret_cast<const float4*>(tris);
         scene->view.v1 = reinterpret_cast<const float4*>(tris + plane);
         scene->view.v2 = reinterpret_cast<const float4*>(tris + 2 * plane);
         scene->view.num_nodes = I.num_wide_nodes;
         scene->view.num_tris = I.num_refs;
-        scene->view.tri_index = indexed ? reinterpret_cast<const uint32_t*>(tris + 3 * plane) : nullptr;
-        scene->view.num_planes = nplanes;
         *out_scene = scene.release();
         ctx->live_scenes++;
     });

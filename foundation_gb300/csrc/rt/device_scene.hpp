@@ -29,11 +29,6 @@ inline int StatusCode(uint32_t bits) {
 
 constexpr int kMaxStack = 64;  // node-group + triangle-group entries per ray
 
-// A scene as the kernels see it. Triangle references (leaf slots) number
-// num_tris. Without tri_index, reference r's planes are v0/v1/v2[r] (a
-// spatial-split tree repeats a triangle's planes in every leaf that holds
-// it); with tri_index, the planes are stored once per triangle and
-// reference r reads planes tri_index[r] < num_planes.
 struct DeviceScene {
     const uint4* nodes;  // 5 uint4 per WideNode
     const float4* v0;    // (x, y, z, original index bits)
@@ -41,11 +36,9 @@ struct DeviceScene {
     const float4* v2;
     uint32_t num_nodes;
     uint32_t num_tris;
-    const uint32_t* tri_index;  // null: planes in reference order
-    uint32_t num_planes;        // with tri_index: entries of v0 / v1 / v2
 };
 
-// One instance of a two-level scene (120 bytes): its bottom-level scene, the
+// One instance of a two-level scene (104 bytes): its bottom-level scene, the
 // world-to-object transform (row-major 3x4, FP32 rounding of the FP64
 // inverse of the instance transform) and the hit id of its triangle 0.
 struct InstanceRec {
@@ -54,7 +47,7 @@ struct InstanceRec {
     uint32_t prim_offset;
     uint32_t pad[3];
 };
-static_assert(sizeof(InstanceRec) == 120, "instance record layout");
+static_assert(sizeof(InstanceRec) == 104, "instance record layout");
 
 }  // namespace RT
 }  // namespace Foundation

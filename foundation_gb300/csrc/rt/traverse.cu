@@ -184,8 +184,6 @@ struct CoopShared {
     float t[kBlock];         // per warp: hit t of the pair at a position
     uint32_t pid[kBlock];    // per warp: hit id of the pair at a position
     const float4* planes[kMulti ? 3 * kBlock : 1];  // [a * kBlock + tid]: vertex plane a of the lane's scene
-    const uint32_t* tindex[kMulti ? kBlock : 1];    // [tid]: the lane's scene's triangle index (or null)
-    uint32_t nplanes[kMulti ? kBlock : 1];          // [tid]: its plane count
 };
 
 template <int kBlock, bool kMulti>
@@ -197,8 +195,6 @@ __device__ __forceinline__ void coop_store_ray(CoopShared<kBlock, kMulti>* cs, c
         cs->planes[threadIdx.x] = sc.v0;
         cs->planes[kBlock + threadIdx.x] = sc.v1;
         cs->planes[2 * kBlock + threadIdx.x] = sc.v2;
-        cs->tindex[threadIdx.x] = sc.tri_index;
-        cs->nplanes[threadIdx.x] = sc.num_planes;
     }
 }
 
@@ -207,7 +203,7 @@ template <int kKind, bool kStats, int kBlock, bool kMulti>
 __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_ok, bool any_hit, uint32_t tg_base,
                                                uint32_t& tg_mask, float& best_t, uint32_t& best_p,
                                                uint32_t& ng_group, int& sp, CoopShared<kBlock, kMulti>* cs,
-                                               unsigned long long& st_tris, uint32_t& st_wtri, uint32_t* status) {
+                                               unsigned long long& st_tris, uint32_t& st_wtri) {
     if (__ballot_sync(kFull, mine_ok && tg_mask != 0u) == 0u) return;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t wbase = threadIdx.x & ~31u;
@@ -238,7 +234,7 @@ __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_
         float t = 0.0f;
         uint32_t pid = 0;
         if (lane < np) {
-            uint32_t ti = obase + select_bit(omask, lane - q);
+            const uint32_t ti = obase + select_bit(omask, lane - q);
             const float4 a = cs->ray[wbase + owner];
             const float4 b = cs->ray[kBlock + wbase + owner];
             RayState rq;
@@ -251,26 +247,14 @@ __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_
             rq.Sz = b.z;
             rq.kz = __float_as_int(b.w);
             const float4 *p0 = sc.v0, *p1 = sc.v1, *p2 = sc.v2;
-            const uint32_t* tidx = sc.tri_index;
-            uint32_t nplanes = sc.num_planes;
             if constexpr (kMulti) {
                 p0 = cs->planes[wbase + owner];
                 p1 = cs->planes[kBlock + wbase + owner];
                 p2 = cs->planes[2 * kBlock + wbase + owner];
-                tidx = cs->tindex[wbase + owner];
-                nplanes = cs->nplanes[wbase + owner];
             }
-            bool ok = true;
-            if (tidx) {  // planes stored once per triangle
-                ti = __ldg(tidx + ti);
-                ok = ti < nplanes;
-                if (!ok) atomicOr(status, kStatusBadIndex);
-            }
-            if (ok) {
-                const float4 v0 = __ldg(p0 + ti);
-                hit = intersect_tri(rq, v0, __ldg(p1 + ti), __ldg(p2 + ti), qt, t);
-                pid = __float_as_uint(v0.w);
-            }
+            const float4 v0 = __ldg(p0 + ti);
+            hit = intersect_tri(rq, v0, __ldg(p1 + ti), __ldg(p2 + ti), qt, t);
+            pid = __float_as_uint(v0.w);
             if (kStats) {
                 st_tris++;
                 if (lane == 0u) st_wtri++;
@@ -436,7 +420,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
         // ---- its triangles, tested by the whole warp ------------------------
         if constexpr (kCoop) {
             coop_triangles<kKind, kStats, kBlock, kMulti>(sc, active && !overflow, any_hit, tg_base, tg_mask, best_t,
-                                                          best_p, ng_group, sp, s_coop, st_tris, st_wtri, C.status);
+                                                          best_p, ng_group, sp, s_coop, st_tris, st_wtri);
             if (!active) continue;
         }
         // ---- its triangles (or, on the top level, its instances) ------------
@@ -473,17 +457,9 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                     break;
                 }
             }
-            uint32_t pi = ti;
-            if (sc.tri_index) {
-                pi = __ldg(sc.tri_index + ti);
-                if (pi >= sc.num_planes) {
-                    atomicOr(C.status, kStatusBadIndex);
-                    continue;
-                }
-            }
-            const float4 v0 = __ldg(sc.v0 + pi);
-            const float4 v1 = __ldg(sc.v1 + pi);
-            const float4 v2 = __ldg(sc.v2 + pi);
+            const float4 v0 = __ldg(sc.v0 + ti);
+            const float4 v1 = __ldg(sc.v1 + ti);
+            const float4 v2 = __ldg(sc.v2 + ti);
             if (kStats) {
                 st_tris++;
                 if (lane == (uint32_t)__ffs(__activemask()) - 1u) st_wtri++;

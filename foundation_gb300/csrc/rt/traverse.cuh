@@ -337,14 +337,7 @@ __device__ __forceinline__ bool trace_single(const DeviceScene& sc, const RaySta
         while (tg_mask) {
             const uint32_t k = (uint32_t)__ffs(tg_mask) - 1u;
             tg_mask &= tg_mask - 1u;
-            uint32_t ti = tg_base + k;
-            if (sc.tri_index) {
-                ti = __ldg(sc.tri_index + ti);
-                if (ti >= sc.num_planes) {
-                    atomicOr(status, kStatusBadIndex);
-                    continue;
-                }
-            }
+            const uint32_t ti = tg_base + k;
             const float4 v0 = __ldg(sc.v0 + ti);
             float t;
             if (intersect_tri(r, v0, __ldg(sc.v1 + ti), __ldg(sc.v2 + ti), best_t, t)) {

@@ -44,7 +44,6 @@ RENDER_ACCUMULATE = 1
 BVH_SPATIAL_SPLITS = 1
 BVH_GPU_BUILD = 2
 BVH_SAH_COLLAPSE = 4
-BVH_INDEXED_TRIANGLES = 8
 RENDER_CACHE = 2
 RENDER_WAVEFRONT = 4
 RENDER_TRAIN_ONLY = 8
@@ -292,9 +291,9 @@ class Context:
     def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0,
                spatial_splits: bool = False, traversal_cost: float = 0.0, gpu_build: bool = False,
                split_budget: float = 0.0, margin_scale: float = 0.0, sah_collapse: bool = False,
-               collapse_tri_cost: float = 0.0, indexed_triangles: bool = False) -> "Scene":
+               collapse_tri_cost: float = 0.0) -> "Scene":
         return Scene(self, verts, idx, bins, max_leaf, threads, spatial_splits, traversal_cost, gpu_build,
-                     split_budget, margin_scale, sah_collapse, collapse_tri_cost, indexed_triangles)
+                     split_budget, margin_scale, sah_collapse, collapse_tri_cost)
 
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
@@ -443,13 +442,13 @@ class Context:
 class Scene:
     def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0, spatial_splits=False,
                  traversal_cost=0.0, gpu_build=False, split_budget=0.0, margin_scale=0.0, sah_collapse=False,
-                 collapse_tri_cost=0.0, indexed_triangles=False):
+                 collapse_tri_cost=0.0):
         self._h = None
         self.ctx = ctx
         v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
         flags = ((BVH_SPATIAL_SPLITS if spatial_splits else 0) | (BVH_GPU_BUILD if gpu_build else 0) |
-                 (BVH_SAH_COLLAPSE if sah_collapse else 0) | (BVH_INDEXED_TRIANGLES if indexed_triangles else 0))
+                 (BVH_SAH_COLLAPSE if sah_collapse else 0))
         bd = _BvhDesc(bins, max_leaf, threads, flags, traversal_cost, split_budget, margin_scale, collapse_tri_cost)
         h = C.c_void_p()
         _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),

@@ -90,8 +90,7 @@ typedef struct fnd_rt_bvh_desc {
     uint32_t build_threads; /* host threads of the build and the collapse; 0: all
                                host cores. The tree does not depend on it, except
                                when a spatial-split budget runs out (split_budget) */
-    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD, FND_BVH_SAH_COLLAPSE,
-                               FND_BVH_INDEXED_TRIANGLES or 0 */
+    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD, FND_BVH_SAH_COLLAPSE or 0 */
     float traversal_cost;   /* SAH cost of a traversal step relative to a triangle
                                test, (0, 64]; 0: default 1 (the reference tree) */
     float split_budget;     /* FND_BVH_SPATIAL_SPLITS: references the splits may add,
@@ -128,13 +127,6 @@ enum { FND_BVH_GPU_BUILD = 2u };
  * the host build and on FND_BVH_GPU_BUILD alike; hits are identical either
  * way. */
 enum { FND_BVH_SAH_COLLAPSE = 4u };
-/* Store each triangle's planes once and give every leaf reference a 4-byte
- * index to them, instead of one 48-byte plane record per reference. A host
- * build does this by itself when the references are at least 1.5 x the
- * triangles (spatial splits on a dense scene: the 1M-triangle soup at split
- * budget 8 holds 6.4 references per triangle, and its tree shrinks from 427 to
- * 121 MB, within L2); this flag forces it. Hits are identical either way. */
-enum { FND_BVH_INDEXED_TRIANGLES = 8u };
 
 typedef struct fnd_rt_scene_info {
     uint32_t num_tris;
@@ -144,7 +136,7 @@ typedef struct fnd_rt_scene_info {
     uint32_t wide_depth;
     uint32_t num_leaves;
     uint64_t node_bytes; /* device bytes of the wide nodes */
-    uint64_t tri_bytes;  /* device bytes of the triangle arrays (planes + reference index) */
+    uint64_t tri_bytes;  /* device bytes of the triangle arrays */
     double sah_cost;     /* SAH cost of the binary tree (C_trav = C_isect = 1) */
     double build_ms;     /* binary binned-SAH build, host */
     double collapse_ms;  /* collapse + compression + triangle re-layout, host */

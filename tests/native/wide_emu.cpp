@@ -378,35 +378,6 @@ void emu_trace_single_raw(const void* nodes, uint32_t num_nodes, const float* pl
     *status_out = status;
 }
 
-// The same rays through RT::trace_single over the indexed triangle layout
-// (planes once per triangle, an index per reference: the product's
-// IndexTrianglePlanes). out_planes receives the plane count, *status_out the
-// status word.
-void emu_trace_single_indexed(const emu_bvh* e, uint32_t nt, const float* rays, uint64_t n, uint32_t* hits, int any,
-                              uint32_t* out_planes, uint32_t* status_out) {
-    std::vector<float> u0, u1, u2;
-    std::vector<uint32_t> index;
-    const uint32_t np = IndexTrianglePlanes(e->wide, nt, u0, u1, u2, index);
-    DeviceScene sc = e->view;
-    sc.v0 = reinterpret_cast<const float4*>(u0.data());
-    sc.v1 = reinterpret_cast<const float4*>(u1.data());
-    sc.v2 = reinterpret_cast<const float4*>(u2.data());
-    sc.tri_index = index.data();
-    sc.num_planes = np;
-    uint32_t status = 0;
-    for (uint64_t i = 0; i < n; ++i) {
-        const float* rp = rays + 8 * i;
-        const RayState r = setup_ray(float4{rp[0], rp[1], rp[2], rp[3]}, float4{rp[4], rp[5], rp[6], rp[7]});
-        float t = r.tmax;
-        uint32_t p = FND_INVALID_ID;
-        const bool h = any ? trace_single<true>(sc, r, t, p, &status) : trace_single<false>(sc, r, t, p, &status);
-        hits[2 * i] = h ? p : FND_INVALID_ID;
-        hits[2 * i + 1] = h ? __float_as_uint(t) : 0x7F800000u;
-    }
-    *out_planes = np;
-    *status_out = status;
-}
-
 // The fnd_status every entry point reports for a latched status word.
 int emu_status_code(uint32_t bits) { return StatusCode(bits); }
 

@@ -166,38 +166,6 @@ def test_emulated_spatial_split_bvh_matches_oracle(emu, case, budget):
     assert np.array_equal((prim_a != 0xFFFFFFFF).astype(np.uint8), b.any(rays))
 
 
-@pytest.mark.parametrize("budget", [0.0, 8.0])
-@pytest.mark.parametrize("case", ["soup", "cornell_incoherent"])
-def test_emulated_indexed_triangles_match_oracle(emu, case, budget):
-    """Planes stored once per triangle with an index per leaf reference (the
-    layout of duplicated spatial-split trees, FND_BVH_INDEXED_TRIANGLES):
-    the product's per-thread traversal over it gives the oracle's hits, every
-    triangle of the scene gets exactly one plane slot, and no status bit is
-    latched."""
-    sc, rays = CASES[case]()
-    v = np.ascontiguousarray(sc.verts, np.float32)
-    f = np.ascontiguousarray(sc.idx, np.uint32)
-    e = Emu.__new__(Emu)
-    e.L, e.v, e.f = emu, v, f
-    e.h = emu.emu_build_sbvh(_p(v), len(v), _p(f), len(f), budget) if budget else \
-        emu.emu_build(_p(v), len(v), _p(f), len(f), 0)
-    emu.emu_trace_single_indexed.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int,
-                                             C.c_void_p, C.c_void_p]
-    b = O.OracleBVH(sc.verts, sc.idx)
-    for any_hit in (0, 1):
-        hits = np.zeros((len(rays), 2), np.uint32)
-        npl = np.zeros(1, np.uint32)
-        st = np.zeros(1, np.uint32)
-        emu.emu_trace_single_indexed(e.h, len(f), _p(rays), len(rays), _p(hits), any_hit, _p(npl), _p(st))
-        assert int(st[0]) == 0 and int(npl[0]) == len(f)
-        if any_hit:
-            assert np.array_equal((hits[:, 0] != 0xFFFFFFFF).astype(np.uint8), b.any(rays))
-        else:
-            ref = b.closest(rays)
-            assert np.array_equal(hits[:, 0], ref["prim"])
-            assert np.array_equal(hits[:, 1], ref["t"].view(np.uint32))
-
-
 @pytest.mark.parametrize("spatial", [0, 1])
 @pytest.mark.parametrize("case", ["soup", "cornell_incoherent"])
 def test_emulated_sah_collapse_matches_oracle(emu, case, spatial):

@@ -140,15 +140,13 @@ def test_tail_megakernel_matches_wavefront(ctx, cache):
 
 def test_render_does_not_depend_on_the_tree(ctx):
     """Closest and any hits do not depend on the tree, so neither do the
-    paths: the binned-SAH tree, the spatial-split tree (split budget 8), the
-    GPU-built tree and the spatial-split tree over indexed triangle planes
-    give the same extension and shadow ray counts and images equal up to the
-    order of the frame-buffer additions."""
+    paths: the binned-SAH tree, the spatial-split tree (split budget 8) and
+    the GPU-built tree give the same extension and shadow ray counts and
+    images equal up to the order of the frame-buffer additions."""
     cs = S.cornell_scene(num_spheres=60)
     kw = dict(seed=11, sky=(0.05, 0.06, 0.08))
     imgs, stats = [], []
-    for bvh in (dict(), dict(spatial_splits=True, split_budget=8.0), dict(gpu_build=True),
-                dict(spatial_splits=True, split_budget=8.0, indexed_triangles=True)):
+    for bvh in (dict(), dict(spatial_splits=True, split_budget=8.0), dict(gpu_build=True)):
         s = ctx.upload(cs.verts, cs.idx, **bvh)
         s.set_materials(cs.tri_material, S.material_records(cs))
         s.set_lights(S.light_records(cs))

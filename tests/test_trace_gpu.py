@@ -101,52 +101,6 @@ def test_soup_1m_tris(ctx):
     ss.close()
 
 
-def test_indexed_triangles_exact(ctx):
-    """Planes stored once per triangle with an index per leaf reference:
-    forced on the Cornell scene (whose spatial-split tree repeats only 6% of
-    its triangles, so it is not indexed by default), and chosen by itself for
-    the 1M-triangle soup at split budget 8; same hits as the oracle, in the
-    persistent kernel and in the batched launch."""
-    import torch
-    import foundation_gb300 as fg
-    cs = S.cornell_scene(num_spheres=40)
-    b = O.OracleBVH(cs.verts, cs.idx)
-    ir = S.incoherent_rays(1 << 18, *cs.bounds, seed=4)
-    direct = ctx.upload(cs.verts, cs.idx, spatial_splits=True, split_budget=8.0, sah_collapse=True)
-    ix = ctx.upload(cs.verts, cs.idx, spatial_splits=True, split_budget=8.0, sah_collapse=True,
-                    indexed_triangles=True)
-    di, ii = direct.info(), ix.info()
-    assert di["tri_bytes"] == 48 * di["num_refs"]
-    assert ii["tri_bytes"] == 48 * len(cs.idx) + 4 * ii["num_refs"]
-    ref = b.closest(ir)
-    assert_same(ix.closest(ir), ref)
-    assert np.array_equal(ix.any(ir), b.any(ir))
-    # the batched launch: an indexed and a direct scene in one job table
-    rd = torch.from_numpy(ir).cuda()
-    outs = [torch.empty(2 * len(ir), dtype=torch.int32, device="cuda") for _ in range(2)]
-    occ = torch.empty(len(ir), dtype=torch.uint8, device="cuda")
-    batch = fg.Batch(ctx, [(ix, rd, outs[0], 0), (direct, rd, outs[1], 0), (ix, rd, occ, 1)])
-    batch.launch()
-    ctx.sync()
-    for o in outs:
-        h = o.cpu().numpy().view(np.uint32)
-        assert np.array_equal(h[0::2], ref["prim"])
-        assert np.array_equal(h[1::2], ref["t"].view(np.uint32))
-    assert np.array_equal(occ.cpu().numpy(), b.any(ir))
-    batch.close()
-    direct.close()
-    ix.close()
-    so = S.soup_scene(1 << 20)
-    ss = ctx.upload(so.verts, so.idx, spatial_splits=True, split_budget=8.0, sah_collapse=True)
-    info = ss.info()
-    assert info["tri_bytes"] == 48 * len(so.idx) + 4 * info["num_refs"]  # indexed by itself
-    rays = S.incoherent_rays(1 << 18, (0, 0, 0), (1, 1, 1), seed=7)
-    bs = O.OracleBVH(so.verts, so.idx)
-    assert_same(ss.closest(rays), bs.closest(rays))
-    assert np.array_equal(ss.any(rays), bs.any(rays))
-    ss.close()
-
-
 def test_pipelined_host_traces_match_device_traces(ctx):
     """Host-buffer calls of more than 2^19 rays run as a chunked copy / trace /
     copy pipeline over two copy streams and two compute streams; the results
