@@ -130,10 +130,13 @@ def test_pipelined_host_traces_match_device_traces(ctx):
         ctx.sync()
         dev = hd.cpu().numpy().view(np.uint32)
         occ = od.cpu().numpy()
-        for h in (sc.closest(rays), sc.closest(pr, ph)):
+        # twice in a row, and pageable rays with pinned hits
+        for h in (sc.closest(rays), sc.closest(pr, ph), sc.closest(pr, ph), sc.closest(rays, ph)):
             assert np.array_equal(h["prim"], dev[0::2])
             assert np.array_equal(h["t"].view(np.uint32), dev[1::2])
         assert np.array_equal(sc.any(rays), occ)
+        po = fg.PinnedBuffer(n)
+        assert np.array_equal(sc.any(pr, po.view(np.uint8, (n,))), occ)
     ctx.set_trace_config()
     sc.close()
 
