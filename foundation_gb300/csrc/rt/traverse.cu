@@ -184,22 +184,24 @@ struct CoopShared {
     float t[kBlock];         // per warp: hit t of the pair at a position
     uint32_t pid[kBlock];    // per warp: hit id of the pair at a position
     const float4* planes[kMulti ? 3 * kBlock : 1];  // [a * kBlock + tid]: vertex plane a of the lane's scene
+    uint32_t prim_off[kMulti ? kBlock : 1];         // [tid]: hit-id offset of the lane's scene (instances)
 };
 
 template <int kBlock, bool kMulti>
 __device__ __forceinline__ void coop_store_ray(CoopShared<kBlock, kMulti>* cs, const RayState& r,
-                                               const DeviceScene& sc) {
+                                               const DeviceScene& sc, uint32_t prim_off = 0u) {
     cs->ray[threadIdx.x] = make_float4(r.ox, r.oy, r.oz, r.tmin);
     cs->ray[kBlock + threadIdx.x] = make_float4(r.nSx, r.nSy, r.Sz, __int_as_float(r.kz));
     if constexpr (kMulti) {
         cs->planes[threadIdx.x] = sc.v0;
         cs->planes[kBlock + threadIdx.x] = sc.v1;
         cs->planes[2 * kBlock + threadIdx.x] = sc.v2;
+        cs->prim_off[threadIdx.x] = prim_off;
     }
 }
 
 // All 32 lanes of the warp call this; lanes without a ray pass mine_ok = false.
-template <int kKind, bool kStats, int kBlock, bool kMulti>
+template <int kKind, bool kStats, int kBlock, bool kMulti, bool kOffsets = false>
 __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_ok, bool any_hit, uint32_t tg_base,
                                                uint32_t& tg_mask, float& best_t, uint32_t& best_p,
                                                uint32_t& ng_group, int& sp, CoopShared<kBlock, kMulti>* cs,
@@ -255,6 +257,7 @@ __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_
             const float4 v0 = __ldg(p0 + ti);
             hit = intersect_tri(rq, v0, __ldg(p1 + ti), __ldg(p2 + ti), qt, t);
             pid = __float_as_uint(v0.w);
+            if constexpr (kOffsets) pid += cs->prim_off[wbase + owner];  // global id of an instance's triangle
             if (kStats) {
                 st_tris++;
                 if (lane == 0u) st_wtri++;
@@ -300,7 +303,9 @@ template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLe
           bool kMulti = false>
 __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack,
                                                  CoopShared<kBlock, kMulti>* s_coop = nullptr) {
-    static_assert(!(kCoop && kTwoLevel), "the top level of a two-level scene holds instances, not triangles");
+    // two-level cooperative rounds: each lane's planes and hit-id offset
+    // come from its own slot (the lanes of a warp sit in different instances)
+    static_assert(!(kCoop && kTwoLevel) || kMulti, "two-level cooperative rounds need per-lane scenes");
     static_assert((kShort & (kShort - 1)) == 0, "short stack size must be a power of two");
     uint2 l_stack[kMaxStack - kShort];
     const int tid = threadIdx.x;
@@ -419,8 +424,41 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
         }
         // ---- its triangles, tested by the whole warp ------------------------
         if constexpr (kCoop) {
-            coop_triangles<kKind, kStats, kBlock, kMulti>(sc, active && !overflow, any_hit, tg_base, tg_mask, best_t,
-                                                          best_p, ng_group, sp, s_coop, st_tris, st_wtri);
+            if constexpr (kTwoLevel) {
+                // a top-level leaf holds instances: the lane enters the first
+                // valid one by itself (resume order as in the per-lane loop
+                // below) and publishes its object-space ray for the rounds
+                while (active && !overflow && !in_blas && tg_mask) {
+                    const uint32_t k = (uint32_t)__ffs(tg_mask) - 1u;
+                    tg_mask &= tg_mask - 1u;
+                    const uint32_t iid = __float_as_uint(__ldg(cur.v0 + tg_base + k).w);
+                    if (iid >= src.num_inst) {
+                        atomicOr(C.status, kStatusBadIndex);
+                        continue;
+                    }
+                    overflow = ((ng_group & 0xFFu) && !push(make_uint2(ng_base, ng_group))) ||
+                               (tg_mask && !push(make_uint2(tg_base | kTriGroupFlag, tg_mask))) ||
+                               !push(make_uint2(kInstanceMarker, 0u));
+                    if (overflow) break;
+                    const InstanceRec& I = src.inst[iid];
+                    float inv[12];
+                    for (int q = 0; q < 12; ++q) inv[q] = __ldg(I.inv + q);
+                    float4 r0, r1, o0, o1;
+                    src.load(ray_id, r0, r1, ln);
+                    instance_ray(inv, r0, r1, o0, o1);
+                    r = setup_ray(o0, o1);
+                    cur = I.blas;
+                    prim_off = __ldg(&I.prim_offset);
+                    in_blas = true;
+                    ng_base = 0;
+                    ng_group = cur.num_nodes ? (1u << 8) | (1u << r.oct) : 0u;
+                    tg_mask = 0;
+                    coop_store_ray<kBlock, kMulti>(s_coop, r, cur, prim_off);
+                }
+            }
+            coop_triangles<kKind, kStats, kBlock, kMulti, kTwoLevel>(sc, active && !overflow, any_hit, tg_base,
+                                                                     tg_mask, best_t, best_p, ng_group, sp, s_coop,
+                                                                     st_tris, st_wtri);
             if (!active) continue;
         }
         // ---- its triangles (or, on the top level, its instances) ------------
@@ -574,6 +612,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) batch_kernel(const 
 template <bool kAny>
 __global__ void __launch_bounds__(128, 6) instanced_trace_kernel(const InstancedLaunch L) {
     __shared__ uint2 s_stack[8 * 128];
+    __shared__ CoopShared<128, true> s_coop;
     InstancedSource src;
     src.scene = L.tlas;
     src.inst = L.inst;
@@ -584,7 +623,7 @@ __global__ void __launch_bounds__(128, 6) instanced_trace_kernel(const Instanced
     src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
     if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
     const Common C{L.counter, L.status, nullptr, 8u, 0u};
-    persistent_trace<InstancedSource, kAny ? 1 : 0, false, 8, 128, true>(src, C, s_stack);
+    persistent_trace<InstancedSource, kAny ? 1 : 0, false, 8, 128, true, true, true>(src, C, s_stack, &s_coop);
 }
 
 __global__ void fill_miss_kernel(uint2* hits, uint8_t* occluded, uint32_t cap, const uint32_t* n_dev) {
