@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstring>
 #include <memory>
 #include <vector>
 
@@ -46,6 +47,8 @@ int fnd_rt_instances_upload(fnd_rt_ctx* ctx, const fnd_rt_instance* instances, u
             r.blas = instances[i].scene->view;
             std::copy(&top.inv[12 * (size_t)i], &top.inv[12 * (size_t)i] + 12, r.inv);
             r.prim_offset = instances[i].prim_offset;
+            static const float kId[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+            r.flags = std::memcmp(r.inv, kId, sizeof(kId)) == 0 ? RT::kInstanceIdentity : 0u;  // bit for bit
         }
         // each bottom level's margin must cover object-space origins of rays
         // that start inside the world box (its margin covers origins within

@@ -45,8 +45,13 @@ struct InstanceRec {
     DeviceScene blas;
     float inv[12];
     uint32_t prim_offset;
-    uint32_t pad[3];
+    uint32_t flags;  // kInstanceIdentity: inv is [I | 0] bit for bit
+    uint32_t pad[2];
 };
+// An identity instance keeps the world ray and its set-up (the transform
+// would change at most the sign of zero components); the oracle's instanced
+// brute force makes the same choice.
+constexpr uint32_t kInstanceIdentity = 1u;
 static_assert(sizeof(InstanceRec) == 104, "instance record layout");
 
 }  // namespace RT

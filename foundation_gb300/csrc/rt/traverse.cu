@@ -302,7 +302,8 @@ __device__ __forceinline__ void coop_triangles(const DeviceScene& sc, bool mine_
 template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLevel = false, bool kCoop = false,
           bool kMulti = false>
 __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack,
-                                                 CoopShared<kBlock, kMulti>* s_coop = nullptr) {
+                                                 CoopShared<kBlock, kMulti>* s_coop = nullptr,
+                                                 RayState* s_world = nullptr) {
     // two-level cooperative rounds: each lane's planes and hit-id offset
     // come from its own slot (the lanes of a warp sit in different instances)
     static_assert(!(kCoop && kTwoLevel) || kMulti, "two-level cooperative rounds need per-lane scenes");
@@ -323,7 +324,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
     unsigned long long st_nodes = 0, st_tris = 0;
     uint32_t st_wnode = 0, st_wtri = 0;  // warp steps, counted by the lowest active lane
     // two-level state: the arrays the lane traverses now, and its instance
-    bool in_blas = false;
+    bool in_blas = false, moved = false;  // moved: r holds an object-space ray, the world one is in s_world
     DeviceScene cur{};
     uint32_t prim_off = 0;
 
@@ -334,6 +335,29 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
         s_stack[s] = e;
         sp++;
         return true;
+    };
+    // two-level: descend into instance I (from the top level, r the world
+    // ray). Its object-space ray replaces r, and the world ray's set-up
+    // waits in s_world for the return; an identity instance keeps r.
+    auto enter_instance = [&](const InstanceRec& I) {
+        if constexpr (kTwoLevel) {
+            if (!(__ldg(&I.flags) & kInstanceIdentity)) {
+                float inv[12];
+                for (int q = 0; q < 12; ++q) inv[q] = __ldg(I.inv + q);
+                float4 r0, r1, o0, o1;
+                src.load(ray_id, r0, r1, ln);
+                instance_ray(inv, r0, r1, o0, o1);
+                s_world[tid] = r;
+                r = setup_ray(o0, o1);
+                moved = true;
+            }
+            cur = I.blas;
+            prim_off = __ldg(&I.prim_offset);
+            in_blas = true;
+            ng_base = 0;
+            ng_group = cur.num_nodes ? (1u << 8) | (1u << r.oct) : 0u;
+            tg_mask = 0;
+        }
     };
 
     for (;;) {
@@ -365,6 +389,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                     active = true;
                     if constexpr (kTwoLevel) {
                         in_blas = false;
+                        moved = false;
                         cur = src.scene;
                         prim_off = 0;
                     }
@@ -441,18 +466,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                                !push(make_uint2(kInstanceMarker, 0u));
                     if (overflow) break;
                     const InstanceRec& I = src.inst[iid];
-                    float inv[12];
-                    for (int q = 0; q < 12; ++q) inv[q] = __ldg(I.inv + q);
-                    float4 r0, r1, o0, o1;
-                    src.load(ray_id, r0, r1, ln);
-                    instance_ray(inv, r0, r1, o0, o1);
-                    r = setup_ray(o0, o1);
-                    cur = I.blas;
-                    prim_off = __ldg(&I.prim_offset);
-                    in_blas = true;
-                    ng_base = 0;
-                    ng_group = cur.num_nodes ? (1u << 8) | (1u << r.oct) : 0u;
-                    tg_mask = 0;
+                    enter_instance(I);
                     coop_store_ray<kBlock, kMulti>(s_coop, r, cur, prim_off);
                 }
             }
@@ -480,18 +494,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                                !push(make_uint2(kInstanceMarker, 0u));
                     if (overflow) break;
                     const InstanceRec& I = src.inst[iid];
-                    float inv[12];
-                    for (int q = 0; q < 12; ++q) inv[q] = __ldg(I.inv + q);
-                    float4 r0, r1, o0, o1;
-                    src.load(ray_id, r0, r1, ln);
-                    instance_ray(inv, r0, r1, o0, o1);
-                    r = setup_ray(o0, o1);
-                    cur = I.blas;
-                    prim_off = __ldg(&I.prim_offset);
-                    in_blas = true;
-                    ng_base = 0;
-                    ng_group = cur.num_nodes ? (1u << 8) | (1u << r.oct) : 0u;
-                    tg_mask = 0;
+                    enter_instance(I);
                     break;
                 }
             }
@@ -528,9 +531,8 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
                 if constexpr (kTwoLevel) {
                     if (e.x == kInstanceMarker) {
                         // back to the top level: the world ray again
-                        float4 r0, r1;
-                        src.load(ray_id, r0, r1, ln);
-                        r = setup_ray(r0, r1);
+                        if (moved) r = s_world[tid];
+                        moved = false;
                         cur = src.scene;
                         prim_off = 0;
                         in_blas = false;
@@ -610,9 +612,10 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) batch_kernel(const 
 }
 
 template <bool kAny>
-__global__ void __launch_bounds__(128, 6) instanced_trace_kernel(const InstancedLaunch L) {
+__global__ void __launch_bounds__(128, 8) instanced_trace_kernel(const InstancedLaunch L) {
     __shared__ uint2 s_stack[8 * 128];
     __shared__ CoopShared<128, true> s_coop;
+    __shared__ RayState s_world[128];
     InstancedSource src;
     src.scene = L.tlas;
     src.inst = L.inst;
@@ -623,7 +626,8 @@ __global__ void __launch_bounds__(128, 6) instanced_trace_kernel(const Instanced
     src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
     if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
     const Common C{L.counter, L.status, nullptr, 8u, 0u};
-    persistent_trace<InstancedSource, kAny ? 1 : 0, false, 8, 128, true, true, true>(src, C, s_stack, &s_coop);
+    persistent_trace<InstancedSource, kAny ? 1 : 0, false, 8, 128, true, true, true>(src, C, s_stack, &s_coop,
+                                                                                     s_world);
 }
 
 __global__ void fill_miss_kernel(uint2* hits, uint8_t* occluded, uint32_t cap, const uint32_t* n_dev) {

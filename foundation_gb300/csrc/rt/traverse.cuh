@@ -427,14 +427,18 @@ __device__ __forceinline__ bool trace_two_level(const DeviceScene& tlas, const I
                 continue;
             }
             const InstanceRec& I = inst[id];
-            float inv[12];
-            for (int q = 0; q < 12; ++q) inv[q] = __ldg(I.inv + q);
-            float4 o0, o1;
-            instance_ray(inv, r0, r1, o0, o1);
+            RayState ro = r;  // an identity instance keeps the world ray
+            if (!(__ldg(&I.flags) & kInstanceIdentity)) {
+                float inv[12];
+                for (int q = 0; q < 12; ++q) inv[q] = __ldg(I.inv + q);
+                float4 o0, o1;
+                instance_ray(inv, r0, r1, o0, o1);
+                ro = setup_ray(o0, o1);
+            }
             const DeviceScene blas = I.blas;
             float t = best_t;
             uint32_t p;
-            if (trace_single<kAny>(blas, setup_ray(o0, o1), t, p, status)) {
+            if (trace_single<kAny>(blas, ro, t, p, status)) {
                 const uint32_t gid = __ldg(&I.prim_offset) + p;
                 if (kAny) {
                     best_t = t;

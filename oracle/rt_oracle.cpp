@@ -16,6 +16,7 @@
 #include <atomic>
 #include <cfloat>
 #include <chrono>
+#include <cstring>
 #include <numeric>
 #include <thread>
 #include <vector>
@@ -494,7 +495,16 @@ static void inverse34(const float* m, float* out) {
     for (int k = 0; k < 12; ++k) out[k] = (float)inv[k];
 }
 
+// An instance whose FP32 inverse is exactly [I | 0] (bit for bit, so no
+// negative zeros) keeps the world ray unchanged: the library skips its
+// transform, which would only turn -0 components into +0.
+static bool identity34(const float* inv) {
+    static const float kId[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    return std::memcmp(inv, kId, sizeof(kId)) == 0;
+}
+
 static Ray instance_ray(const float* inv, const Ray& r) {
+    if (identity34(inv)) return r;
     Ray o = r;
     for (int i = 0; i < 3; ++i) {
         const float* m = inv + 4 * i;

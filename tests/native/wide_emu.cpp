@@ -307,6 +307,8 @@ emu_two* emu_instances(const emu_bvh* const* blas, const float* transforms, cons
         t->recs[i].blas = blas[i]->view;
         std::memcpy(t->recs[i].inv, &t->top.inv[12 * (size_t)i], 48);
         t->recs[i].prim_offset = offsets[i];
+        static const float kId[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};  // the library's identity rule
+        t->recs[i].flags = std::memcmp(t->recs[i].inv, kId, sizeof(kId)) == 0 ? kInstanceIdentity : 0u;
     }
     t->tlas.nodes = reinterpret_cast<const uint4*>(t->top.wide.nodes.data());
     t->tlas.v0 = reinterpret_cast<const float4*>(t->top.wide.v0.data());
