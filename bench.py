@@ -496,7 +496,8 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
     seed 3) plus 4,096 level-4 icospheres, 30,970,912 triangles, lit by a
     directional sun and a constant sky; 3840x2160, max depth 6, RR from
     bounce 3. Reported: the host build (binned SAH, SAH-optimal collapse),
-    incoherent closest-hit throughput on the scene, the plain tracer's 16-spp
+    incoherent closest-hit throughput on the scene and on the trees built on
+    the GPU (Karras hierarchy; locally-ordered clustering), the plain tracer's 16-spp
     frame, and the radiance cache
     (training-only warm-up frames, then 1-spp frames) given the same wall
     time; both scored by relMSE against a plain render of `ref_spp` spp."""
@@ -539,6 +540,15 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
         g.closest(rd, hd)
     gpu_trace_ms = sum(timed(lambda: g.closest(rd, hd)) for _ in range(5)) / 5
     g.close()
+    # built on the GPU by locally-ordered clustering instead
+    t0 = time.perf_counter()
+    g = ctx.upload(tr.verts, tr.idx, gpu_build=True, sah_collapse=True, cluster=True)
+    cl_upload_s = time.perf_counter() - t0
+    cinfo = g.info()
+    for _ in range(2):
+        g.closest(rd, hd)
+    cl_trace_ms = sum(timed(lambda: g.closest(rd, hd)) for _ in range(5)) / 5
+    g.close()
     s.closest(rd, hd)
     flat_hits = hd.clone()
     ref = CV.render_reference(ctx, s, W, H, cam, ref_spp, chunk=16, seed=9001, **kw)
@@ -572,6 +582,9 @@ def large_scene_block(fg, torch, stream, local, spp: int = 16, ref_spp: int = 25
             "gpu_build": {"upload_s": gpu_upload_s, "build_ms": ginfo["build_ms"], "collapse_ms": ginfo["collapse_ms"],
                           "wide_nodes": ginfo["num_wide_nodes"],
                           "incoherent_mrays_s": n_rays / (gpu_trace_ms * 1e-3) / 1e6},
+            "gpu_build_clustered": {"upload_s": cl_upload_s, "build_ms": cinfo["build_ms"],
+                                    "collapse_ms": cinfo["collapse_ms"], "wide_nodes": cinfo["num_wide_nodes"],
+                                    "incoherent_mrays_s": n_rays / (cl_trace_ms * 1e-3) / 1e6},
             "reference_spp": ref_spp, "est_reference_relmse": r_plain * spp / ref_spp,
             "plain": {"spp": spp, "ms": plain_ms, "relmse": r_plain, "extension_rays": st["extension_rays"],
                       "shadow_rays": st["shadow_rays"],
@@ -678,6 +691,8 @@ def target_figures(blocks: dict) -> dict:
     b = blocks.get("large_scene_4k")
     if b and "incoherent_mrays_s" in b:
         out["large_scene_incoherent_mrays_s"] = b["incoherent_mrays_s"]
+        if "gpu_build_clustered" in b:
+            out["large_scene_gpu_built_mrays_s"] = b["gpu_build_clustered"]["incoherent_mrays_s"]
         if "incoherent_mrays_s" in b.get("instanced", {}):
             out["large_scene_two_level_mrays_s"] = b["instanced"]["incoherent_mrays_s"]
     return out

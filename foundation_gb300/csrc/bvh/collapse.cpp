@@ -138,6 +138,9 @@ public:
         for (size_t i = top.size(); i-- > 0;) Solve(top[i]);
     }
 
+    // C(root, 1): the cost of the whole wide tree.
+    float RootCost() const { return m_cost[0]; }
+
     // The children of a wide node made of binary node n.
     void NodeKids(uint32_t n, Kid* kids, int& nk) const {
         nk = 0;
@@ -413,6 +416,13 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
         out.hi[i] = root.hi[i];
     }
     const float margin = SceneMargin(root.lo, root.hi) * margin_scale;
+    if (sah) {
+        const double ra = (double)(root.hi[0] - root.lo[0]) * (root.hi[1] - root.lo[1]) +
+                          (double)(root.hi[1] - root.lo[1]) * (root.hi[2] - root.lo[2]) +
+                          (double)(root.hi[2] - root.lo[2]) * (root.hi[0] - root.lo[0]);
+        LOG_RUNTIME(FndRt, INFO, "SAH-optimal collapse: wide-tree cost %.4f (root half-area normalised)",
+                    ra > 0.0 ? sah->RootCost() / ra : 0.0);
+    }
     out.margin = margin;
     out.nodes.assign(1, WideNode{});
     const size_t nrefs = bin.prims.size();  // == nt unless spatial splits duplicated references

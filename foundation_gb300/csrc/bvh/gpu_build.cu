@@ -2,16 +2,19 @@
 //
 //  1. prep: per triangle its box, its shading normal, input validation, and
 //     the scene box / centroid box (warp-reduced float atomics);
-//  2. 63-bit Morton code of each centroid on a 2^21 x 2^21 x 2^21 grid over
-//     the centroid box (dense scenes keep a spatial order far below the
-//     triangle size);
+//  2. 63-bit Morton code of each centroid on a grid of 2^21 cubic cells per
+//     axis over the centroid box's largest extent (dense scenes keep a
+//     spatial order far below the triangle size);
 //  3. stable LSD radix sort of (code, triangle) in eight 8-bit passes: per
 //     2,048-element warp tile a digit histogram, one exclusive scan over the
 //     digit-major counts, then a scatter in which each warp ranks its
 //     elements in order with __match_any_sync;
 //  4. Karras (2012): internal node i of the n-1 finds its key range and
 //     split by binary searches on the common-prefix length of the sorted
-//     keys (ties between equal codes broken by sorted position);
+//     keys (ties between equal codes broken by sorted position); or
+//     locally-ordered clustering of the sorted triangles (Meister & Bittner
+//     2018), rounds of mutual-nearest-neighbour merges within a window of
+//     the cluster array;
 //  5. refit from the leaves upwards (the second thread to reach a node
 //     finishes it): box, triangle count and the SAH decision
 //     cost(n) = min(N A, C_trav A + cost(l) + cost(r)), a subtree of at most
@@ -60,7 +63,6 @@ struct Buffers {
     uint32_t* sums;               // scan tile sums
     uint32_t *left, *right;       // internal node children (kLeafRef | sorted index for leaves)
     uint32_t *parent_i, *parent_l;
-    uint32_t* first;              // internal node: first sorted leaf of its range
     float4 *nlo, *nhi;            // internal node boxes
     uint32_t* ncount;             // triangle count | kLeafNode
     float* ncost;
@@ -176,6 +178,9 @@ __device__ __forceinline__ unsigned long long spread3(unsigned long long v) {
     return v;
 }
 
+// The grid's cells are cubes: every axis is scaled by the centroid box's
+// largest extent, so a flat scene's thin axis takes few of the code's bits
+// and the first splits of the order are along the long axes.
 __global__ void __launch_bounds__(256) morton_kernel(uint32_t nt, Buffers B) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nt) return;
@@ -183,9 +188,9 @@ __global__ void __launch_bounds__(256) morton_kernel(uint32_t nt, Buffers B) {
     const float c[3] = {__fmul_rn(0.5f, __fadd_rn(lo.x, hi.x)), __fmul_rn(0.5f, __fadd_rn(lo.y, hi.y)),
                         __fmul_rn(0.5f, __fadd_rn(lo.z, hi.z))};
     unsigned long long q[3];
+    const float emax = fmaxf(fmaxf(B.bounds[9] - B.bounds[6], B.bounds[10] - B.bounds[7]), B.bounds[11] - B.bounds[8]);
     for (int a = 0; a < 3; ++a) {
-        const float e = B.bounds[9 + a] - B.bounds[6 + a];
-        const float u = e > 0.0f ? (c[a] - B.bounds[6 + a]) * (2097152.0f / e) : 0.0f;
+        const float u = emax > 0.0f ? (c[a] - B.bounds[6 + a]) * (2097152.0f / emax) : 0.0f;
         q[a] = (unsigned long long)fminf(fmaxf(u, 0.0f), 2097151.0f);
     }
     B.keys[t] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
@@ -218,27 +223,28 @@ __global__ void __launch_bounds__(32 * kSortWarps) hist_kernel(const unsigned lo
     for (uint32_t d = lane; d < 256; d += 32) cnt[(size_t)d * units + u] = s_cnt[warp][d];
 }
 
-__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t& total, uint32_t* s_warp) {
+template <typename T>
+__device__ __forceinline__ T block_exclusive(T v, T& total, T* s_warp) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t incl = v;
+    T incl = v;
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t x = __shfl_up_sync(kFull, incl, o);
+        const T x = __shfl_up_sync(kFull, incl, o);
         if ((int)lane >= o) incl += x;
     }
     if (lane == 31) s_warp[warp] = incl;
     __syncthreads();
     const uint32_t nw = blockDim.x >> 5;
     if (warp == 0) {
-        uint32_t w = lane < nw ? s_warp[lane] : 0u;
+        T w = lane < nw ? s_warp[lane] : T(0);
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t x = __shfl_up_sync(kFull, w, o);
+            const T x = __shfl_up_sync(kFull, w, o);
             if ((int)lane >= o) w += x;
         }
         if (lane < nw) s_warp[lane] = w;
     }
     __syncthreads();
     total = s_warp[nw - 1];
-    const uint32_t before = warp ? s_warp[warp - 1] : 0u;
+    const T before = warp ? s_warp[warp - 1] : T(0);
     __syncthreads();
     return before + incl - v;
 }
@@ -349,7 +355,6 @@ __global__ void __launch_bounds__(256) hierarchy_kernel(int n, Buffers B) {
     const uint32_t rc = hi == gamma + 1 ? (kLeafRef | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
     B.left[i] = lc;
     B.right[i] = rc;
-    B.first[i] = (uint32_t)lo;
     if (lc & kLeafRef)
         B.parent_l[gamma] = (uint32_t)i;
     else
@@ -363,6 +368,192 @@ __global__ void __launch_bounds__(256) hierarchy_kernel(int n, Buffers B) {
 __host__ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
     const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
     return dx * dy + dy * dz + dz * dx;
+}
+
+// ---- hierarchy by locally-ordered clustering (Meister & Bittner 2018) -----------
+// Clusters start as the sorted single triangles. Each round, every cluster
+// finds the neighbour within r positions of the current cluster array whose
+// merged box has the least half area (ties: the nearer-to-the-front
+// neighbour, which orders every pair by (area, lower index, higher index)
+// alike from both ends); mutual neighbours merge into a new internal node at
+// the lower position, and the array is compacted in order. The least pair of
+// a round is always mutual, so every round of two or more clusters merges at
+// least one pair. Internal nodes are numbered down from n - 2 in creation
+// order, so the last merge, the root, is node 0 as in the Karras tree, and
+// the same refit and collapse follow.
+constexpr int kPlocBlock = 256;
+constexpr int kPlocMaxRadius = 64;
+constexpr uint32_t kPlocItems = 16;
+constexpr uint32_t kPlocTile = kPlocBlock * kPlocItems;  // clusters per scan tile
+
+struct PlocState {
+    uint32_t count;      // clusters
+    uint32_t next_node;  // internal nodes 0 .. next_node - 1 are still to be made
+};
+
+__global__ void __launch_bounds__(kPlocBlock) ploc_init_kernel(uint32_t n, Buffers B, uint32_t* __restrict__ cref,
+                                                               float4* __restrict__ lo, float4* __restrict__ hi,
+                                                               PlocState* st) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *st = PlocState{n, n - 1u};
+    if (i >= n) return;
+    const uint32_t t = B.vals[i];
+    cref[i] = kLeafRef | i;
+    lo[i] = B.blo[t];
+    hi[i] = B.bhi[t];
+}
+
+__global__ void __launch_bounds__(kPlocBlock) ploc_nn_kernel(const PlocState* __restrict__ st,
+                                                             const float4* __restrict__ lo,
+                                                             const float4* __restrict__ hi, uint32_t* __restrict__ nn,
+                                                             int r) {
+    __shared__ float4 s_lo[kPlocBlock + 2 * kPlocMaxRadius], s_hi[kPlocBlock + 2 * kPlocMaxRadius];
+    const int count = (int)st->count;
+    const int b0 = (int)(blockIdx.x * kPlocBlock);
+    if (b0 >= count) return;
+    for (int k = threadIdx.x; k < kPlocBlock + 2 * r; k += kPlocBlock) {
+        const int g = b0 - r + k;
+        if (g >= 0 && g < count) {
+            s_lo[k] = lo[g];
+            s_hi[k] = hi[g];
+        }
+    }
+    __syncthreads();
+    const int i = b0 + (int)threadIdx.x;
+    if (i >= count) return;
+    const int li = (int)threadIdx.x + r;
+    const float4 alo = s_lo[li], ahi = s_hi[li];
+    float best = __int_as_float(0x7F800000);
+    int bj = i;
+    const int jlo = max(0, i - r), jhi = min(count - 1, i + r);
+    for (int j = jlo; j <= jhi; ++j) {
+        if (j == i) continue;
+        const int lj = j - b0 + r;
+        // the lower position's box first, so both ends compute the same bits
+        const float4 plo = j < i ? s_lo[lj] : alo, phi = j < i ? s_hi[lj] : ahi;
+        const float4 qlo = j < i ? alo : s_lo[lj], qhi = j < i ? ahi : s_hi[lj];
+        const float dx = fmaxf(phi.x, qhi.x) - fminf(plo.x, qlo.x);
+        const float dy = fmaxf(phi.y, qhi.y) - fminf(plo.y, qlo.y);
+        const float dz = fmaxf(phi.z, qhi.z) - fminf(plo.z, qlo.z);
+        // overflowing extents compare as +inf, so the order stays total
+        const float d = fminf(dx * dy + dy * dz + dz * dx, __int_as_float(0x7F800000));
+        if (d < best || bj == i) {
+            best = d;
+            bj = j;
+        }
+    }
+    nn[i] = (uint32_t)bj;
+}
+
+// per cluster i with neighbour j: merges here (mutual, i < j), survives
+// (not mutual, or the merge's lower end)
+__device__ __forceinline__ void ploc_flags(const uint32_t* __restrict__ nn, uint32_t i, uint32_t& j, bool& merge,
+                                           bool& survive) {
+    j = nn[i];
+    const bool mutual = j != i && nn[j] == i;
+    merge = mutual && i < j;
+    survive = !mutual || i < j;
+}
+
+// per tile: (merges << 32) | survivors
+__global__ void __launch_bounds__(kPlocBlock) ploc_count_kernel(const PlocState* __restrict__ st,
+                                                                const uint32_t* __restrict__ nn,
+                                                                unsigned long long* __restrict__ tsum) {
+    __shared__ unsigned long long s_warp[32];
+    const uint32_t count = st->count;
+    if (blockIdx.x * kPlocTile >= count) return;
+    const uint32_t base = blockIdx.x * kPlocTile + threadIdx.x * kPlocItems;
+    unsigned long long v = 0;
+    for (uint32_t k = 0; k < kPlocItems; ++k) {
+        const uint32_t i = base + k;
+        if (i >= count) break;
+        uint32_t j;
+        bool merge, survive;
+        ploc_flags(nn, i, j, merge, survive);
+        v += (merge ? (1ull << 32) : 0ull) + (survive ? 1ull : 0ull);
+    }
+    unsigned long long total;
+    block_exclusive(v, total, s_warp);
+    if (threadIdx.x == 0) tsum[blockIdx.x] = total;
+}
+
+// exclusive scan of the tile sums (one block, 4,096 tiles at a time), and
+// the next round's state
+__global__ void __launch_bounds__(1024) ploc_scan_kernel(const PlocState* __restrict__ st, PlocState* __restrict__ next,
+                                                         unsigned long long* __restrict__ tsum) {
+    __shared__ unsigned long long s_warp[32];
+    const uint32_t count = st->count;
+    const uint32_t tiles = (count + kPlocTile - 1) / kPlocTile;
+    unsigned long long carry = 0;
+    for (uint32_t c0 = 0; c0 < tiles; c0 += 4 * 1024) {
+        const uint32_t k = c0 + 4u * threadIdx.x;
+        unsigned long long c[4], v = 0;
+        for (uint32_t j = 0; j < 4; ++j) {
+            c[j] = k + j < tiles ? tsum[k + j] : 0ull;
+            v += c[j];
+        }
+        unsigned long long total;
+        unsigned long long run = carry + block_exclusive(v, total, s_warp);
+        for (uint32_t j = 0; j < 4; ++j) {
+            if (k + j < tiles) tsum[k + j] = run;
+            run += c[j];
+        }
+        carry += total;
+    }
+    if (threadIdx.x == 0) *next = PlocState{(uint32_t)carry, st->next_node - (uint32_t)(carry >> 32)};
+}
+
+__device__ __forceinline__ void ploc_set_parent(const Buffers& B, uint32_t ref, uint32_t node) {
+    if (ref & kLeafRef)
+        B.parent_l[ref & ~kLeafRef] = node;
+    else
+        B.parent_i[ref] = node;
+}
+
+__global__ void __launch_bounds__(kPlocBlock) ploc_merge_kernel(
+    const PlocState* __restrict__ st, const unsigned long long* __restrict__ tsum, const uint32_t* __restrict__ nn,
+    const uint32_t* __restrict__ cin, const float4* __restrict__ lin, const float4* __restrict__ hin,
+    uint32_t* __restrict__ cout, float4* __restrict__ lout, float4* __restrict__ hout, Buffers B) {
+    __shared__ unsigned long long s_warp[32];
+    const uint32_t count = st->count, next_node = st->next_node;
+    if (blockIdx.x * kPlocTile >= count) return;
+    const uint32_t base = blockIdx.x * kPlocTile + threadIdx.x * kPlocItems;
+    uint32_t jj[kPlocItems], merge_bits = 0, survive_bits = 0;
+    unsigned long long v = 0;
+    for (uint32_t k = 0; k < kPlocItems; ++k) {
+        const uint32_t i = base + k;
+        bool merge = false, survive = false;
+        jj[k] = i;
+        if (i < count) ploc_flags(nn, i, jj[k], merge, survive);
+        merge_bits |= (merge ? 1u : 0u) << k;
+        survive_bits |= (survive ? 1u : 0u) << k;
+        v += (merge ? (1ull << 32) : 0ull) + (survive ? 1ull : 0ull);
+    }
+    unsigned long long total;
+    unsigned long long run = tsum[blockIdx.x] + block_exclusive(v, total, s_warp);
+    for (uint32_t k = 0; k < kPlocItems; ++k) {
+        if (!(survive_bits >> k & 1u)) continue;
+        const uint32_t i = base + k, at = (uint32_t)run;
+        if (merge_bits >> k & 1u) {
+            const uint32_t j = jj[k];
+            const uint32_t node = next_node - 1u - (uint32_t)(run >> 32);
+            const uint32_t a = cin[i], b = cin[j];
+            B.left[node] = a;
+            B.right[node] = b;
+            ploc_set_parent(B, a, node);
+            ploc_set_parent(B, b, node);
+            const float4 al = lin[i], ah = hin[i], bl = lin[j], bh = hin[j];
+            cout[at] = node;
+            lout[at] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.0f);
+            hout[at] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.0f);
+            run += (1ull << 32) + 1ull;
+        } else {
+            cout[at] = cin[i];
+            lout[at] = lin[i];
+            hout[at] = hin[i];
+            run += 1ull;
+        }
+    }
 }
 
 struct RefBox {
@@ -546,7 +737,7 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
         // subtraction rounds back), node box
         float clo[kWidth][3], chi[kWidth][3];
         float nlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, nhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-        uint32_t first[kWidth], cnt[kWidth];
+        uint32_t cnt[kWidth];
         bool is_leaf[kWidth];
         for (int c = 0; c < nk; ++c) {
             float4 lo, hi;
@@ -555,7 +746,6 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
                 const uint32_t t = B.vals[sk];
                 lo = B.blo[t];
                 hi = B.bhi[t];
-                first[c] = sk;
                 cnt[c] = 1;
                 is_leaf[c] = true;
             } else {
@@ -564,7 +754,6 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
                 const uint32_t w = __ldcg(B.ncount + kids[c]);
                 is_leaf[c] = (B.dpc && !(item.x & kLeafRef)) ? dp_leaf[c] : (w & kLeafNode) != 0u;
                 cnt[c] = w & ~kLeafNode;
-                first[c] = B.first[kids[c]];
             }
             const float l3[3] = {lo.x, lo.y, lo.z}, h3[3] = {hi.x, hi.y, hi.z};
             for (int a = 0; a < 3; ++a) {
@@ -626,6 +815,7 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
             step[a] = ldexp(1.0, e);
         }
         uint32_t n_int = 0, n_tri = 0;
+        bool bad_tree = false;
         for (int c = 0; c < nk; ++c) {
             if (is_leaf[c])
                 n_tri += cnt[c];
@@ -654,8 +844,21 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
             }
             if (is_leaf[c]) {
                 nd.meta[s] = (uint8_t)(kMetaLeafFlag | ((cnt[c] - 1u) << 5) | tri_off);
-                for (uint32_t i = 0; i < cnt[c]; ++i) {
-                    const uint32_t t = B.vals[first[c] + i];
+                // the leaf's triangles: its binary subtree's leaves, left to right
+                // (a Morton-order range for the Karras tree, not for clusters)
+                uint32_t st[2 * kMaxLeafTris];
+                int sp = 0;
+                st[sp++] = kids[c];
+                uint32_t i = 0;
+                for (int step = 0; sp > 0 && i < cnt[c] && step < 4 * kMaxLeafTris; ++step) {
+                    const uint32_t ref = st[--sp];
+                    if (!(ref & kLeafRef)) {
+                        if (sp + 2 > 2 * kMaxLeafTris) break;
+                        st[sp++] = B.right[ref];
+                        st[sp++] = B.left[ref];
+                        continue;
+                    }
+                    const uint32_t t = B.vals[ref & ~kLeafRef];
                     const size_t d = (size_t)tri_base + tri_off + i;
                     float v[9];
                     for (int k = 0; k < 3; ++k)
@@ -663,7 +866,9 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
                     A.v0[d] = make_float4(v[0], v[1], v[2], __uint_as_float(t));
                     A.v1[d] = make_float4(v[3], v[4], v[5], 0.0f);
                     A.v2[d] = make_float4(v[6], v[7], v[8], 0.0f);
+                    i++;
                 }
+                if (i != cnt[c]) bad_tree = true;
                 tri_off += cnt[c];
                 leaves++;
             } else {
@@ -675,6 +880,7 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
             }
         }
         if (bad) atomicOr(B.status, 4u);
+        if (bad_tree) atomicOr(B.status, 8u);
         if (leaves) atomicAdd(counters + 2, leaves);
         A.nodes[item.y] = nd;
     }
@@ -753,6 +959,62 @@ void RadixSort(Buffers& B, uint32_t n, cudaStream_t s) {
     // eight passes: the sorted data is back in keys / vals
 }
 
+// The clustering rounds of ploc_*_kernel. Each round's grids are sized by
+// the cluster count read back one round late (an upper bound: counts only
+// fall), so the host never waits for the round it has just queued.
+void PlocHierarchy(Buffers& B, uint32_t n, int r, cudaStream_t s) {
+    Scratch S;
+    uint32_t* cref[2] = {S.get<uint32_t>(n), S.get<uint32_t>(n)};
+    float4* lo[2] = {S.get<float4>(n), S.get<float4>(n)};
+    float4* hi[2] = {S.get<float4>(n), S.get<float4>(n)};
+    uint32_t* nn = S.get<uint32_t>(n);
+    unsigned long long* tsum = S.get<unsigned long long>((n + kPlocTile - 1) / kPlocTile);
+    PlocState* st = S.get<PlocState>(2);
+    PlocState* h = nullptr;  // one pinned slot per round in flight
+    Check(cudaHostAlloc(reinterpret_cast<void**>(&h), 2 * sizeof(PlocState), cudaHostAllocDefault),
+          "cudaHostAlloc (cluster counts)");
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    struct Release {
+        PlocState* h;
+        cudaEvent_t* ev;
+        ~Release() {
+            for (int k = 0; k < 2; ++k)
+                if (ev[k]) cudaEventDestroy(ev[k]);
+            cudaFreeHost(h);
+        }
+    } release{h, ev};
+    for (int k = 0; k < 2; ++k) Check(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming), "event");
+    ploc_init_kernel<<<(n + kPlocBlock - 1) / kPlocBlock, kPlocBlock, 0, s>>>(n, B, cref[0], lo[0], hi[0], st);
+    uint32_t bound = n, last = n, launched = 0;
+    int cur = 0;
+    bool done = false, stuck = false;
+    // every round of two or more clusters merges a pair: at most n - 1 rounds
+    for (uint32_t round = 0; !done && round <= n; ++round) {
+        launched = round + 1;
+        const uint32_t tiles = (bound + kPlocTile - 1) / kPlocTile;
+        ploc_nn_kernel<<<(bound + kPlocBlock - 1) / kPlocBlock, kPlocBlock, 0, s>>>(st + cur, lo[cur], hi[cur], nn, r);
+        ploc_count_kernel<<<tiles, kPlocBlock, 0, s>>>(st + cur, nn, tsum);
+        ploc_scan_kernel<<<1, 1024, 0, s>>>(st + cur, st + (cur ^ 1), tsum);
+        ploc_merge_kernel<<<tiles, kPlocBlock, 0, s>>>(st + cur, tsum, nn, cref[cur], lo[cur], hi[cur],
+                                                       cref[cur ^ 1], lo[cur ^ 1], hi[cur ^ 1], B);
+        Check(cudaMemcpyAsync(h + (round & 1), st + (cur ^ 1), sizeof(PlocState), cudaMemcpyDeviceToHost, s),
+              "cluster count");
+        Check(cudaEventRecord(ev[round & 1], s), "event");
+        cur ^= 1;
+        if (round == 0) continue;
+        Check(cudaEventSynchronize(ev[(round - 1) & 1]), "clustering round");
+        const uint32_t c = h[(round - 1) & 1].count;
+        done = c <= 1;
+        stuck = c >= last;  // no merge in a round of two or more clusters
+        if (stuck) break;
+        last = bound = c;
+    }
+    Check(cudaStreamSynchronize(s), "clustering");
+    const PlocState fin = h[(launched - 1) & 1];
+    CHECK_CODE(!stuck && done && fin.count == 1 && fin.next_node == 0, FND_ERR_INVALID_SCENE,
+               "GPU build: clustering stopped at %u clusters", fin.count);
+}
+
 }  // namespace
 
 void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint32_t nt, const GpuBuildParams& p,
@@ -761,6 +1023,8 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
                kGpuBuildMaxTris, nt);
     CHECK_CODE(p.max_leaf >= 1 && p.max_leaf <= (uint32_t)kMaxLeafTris, FND_ERR_INVALID_ARG, "max_leaf %u",
                p.max_leaf);
+    CHECK_CODE(p.ploc_radius <= (uint32_t)kPlocMaxRadius, FND_ERR_INVALID_ARG, "clustering radius %u above %d",
+               p.ploc_radius, kPlocMaxRadius);
     int dev = 0, sms = 0;
     Check(cudaGetDevice(&dev), "cudaGetDevice");
     Check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
@@ -781,7 +1045,6 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     B.right = S.get<uint32_t>(n);
     B.parent_i = S.get<uint32_t>(n);
     B.parent_l = S.get<uint32_t>(n);
-    B.first = S.get<uint32_t>(n);
     B.nlo = S.get<float4>(n);
     B.nhi = S.get<float4>(n);
     B.ncount = S.get<uint32_t>(n);
@@ -825,7 +1088,10 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     morton_kernel<<<g256, 256, 0, s>>>(n, B);
     RadixSort(B, n, s);
     if (n >= 2) {
-        hierarchy_kernel<<<(n - 1 + 255) / 256, 256, 0, s>>>((int)n, B);
+        if (p.ploc_radius)
+            PlocHierarchy(B, n, (int)p.ploc_radius, s);
+        else
+            hierarchy_kernel<<<(n - 1 + 255) / 256, 256, 0, s>>>((int)n, B);
         refit_kernel<<<g256, 256, 0, s>>>(n, B, p.max_leaf, p.trav_cost);
     }
     Check(cudaGetLastError(), "hierarchy launch");
@@ -835,10 +1101,11 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     const uint32_t one[2] = {1u, 0u};  // one wide node (the root), level-0 queue of one item
     Check(cudaMemcpyAsync(B.counters + 0, &one[0], 4, cudaMemcpyHostToDevice, s), "root count");
     Check(cudaMemcpyAsync(B.counters + 4, &one[0], 4, cudaMemcpyHostToDevice, s), "queue count");
-    float root_cost = 0.0f;
+    float root_cost = 0.0f, wide_cost = 0.0f;
     float4 rlo{}, rhi{};
     if (n >= 2) {
         Check(cudaMemcpyAsync(&root_cost, B.ncost, 4, cudaMemcpyDeviceToHost, s), "cost readback");
+        if (B.dpc) Check(cudaMemcpyAsync(&wide_cost, B.dpc, 4, cudaMemcpyDeviceToHost, s), "cost readback");
         Check(cudaMemcpyAsync(&rlo, B.nlo, 16, cudaMemcpyDeviceToHost, s), "root box");
         Check(cudaMemcpyAsync(&rhi, B.nhi, 16, cudaMemcpyDeviceToHost, s), "root box");
     }
@@ -885,6 +1152,9 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     out.num_binary_nodes = 2 * n - 1;
     const float ra = n >= 2 ? half_area(rlo, rhi) : 0.0f;
     out.sah_cost = n >= 2 && ra > 0.0f ? (double)root_cost / (double)ra : 0.0;
+    if (B.dpc)
+        LOG_RUNTIME(FndRt, INFO, "SAH-optimal collapse: wide-tree cost %.4f (root half-area normalised)",
+                    ra > 0.0f ? (double)wide_cost / (double)ra : 0.0);
     // exact-size node array
     void* exact = nullptr;
     Check(cudaMalloc(&exact, sizeof(WideNode) * (size_t)out.num_nodes), "cudaMalloc (wide nodes)");

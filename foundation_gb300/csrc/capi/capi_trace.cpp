@@ -125,7 +125,8 @@ namespace {
 // FND_BVH_GPU_BUILD: the vertices and indices go to the device once and the
 // tree is built there (bvh/gpu_build.cu).
 void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, uint32_t nv, const uint32_t* idx,
-                    uint32_t nt, const RT::BuildParams& bp, float margin_scale, const RT::CollapseOptions& copt) {
+                    uint32_t nt, const RT::BuildParams& bp, float margin_scale, const RT::CollapseOptions& copt,
+                    uint32_t cluster_radius) {
     void *d_verts = nullptr, *d_idx = nullptr;
     RT::GpuBuildOutput go;
     try {
@@ -142,6 +143,7 @@ void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, ui
         gp.margin_scale = margin_scale;
         gp.sah_collapse = copt.sah;
         gp.c_tri = (float)copt.c_tri;
+        gp.ploc_radius = cluster_radius;
         RT::BuildWideGpu(static_cast<const float*>(d_verts), nv, static_cast<const uint32_t*>(d_idx), nt, gp, go,
                          ctx->stream);
         CUDA_CHECK(cudaFree(d_verts));
@@ -323,8 +325,17 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         CHECK_CODE(bp.max_leaf >= 1 && bp.max_leaf <= 4, FND_ERR_INVALID_ARG, "max_leaf_tris %u not in [1, 4]",
                    bp.max_leaf);
         CHECK_CODE(!bvh || (bvh->flags & ~(uint32_t)(FND_BVH_SPATIAL_SPLITS | FND_BVH_GPU_BUILD |
-                                                     FND_BVH_SAH_COLLAPSE)) == 0,
+                                                     FND_BVH_SAH_COLLAPSE | FND_BVH_GPU_CLUSTER |
+                                                     FND_BVH_CLUSTER_RADIUS(255))) == 0,
                    FND_ERR_INVALID_ARG, "unknown BVH flags 0x%x", bvh ? bvh->flags : 0u);
+        const uint32_t radius_bits = bvh ? (bvh->flags >> 8) & 255u : 0u;
+        CHECK_CODE(radius_bits <= 64, FND_ERR_INVALID_ARG, "clustering radius %u not in 1..64", radius_bits);
+        CHECK_CODE(!bvh || (bvh->flags & FND_BVH_GPU_CLUSTER) || radius_bits == 0, FND_ERR_INVALID_ARG,
+                   "FND_BVH_CLUSTER_RADIUS without FND_BVH_GPU_CLUSTER");
+        CHECK_CODE(!bvh || !(bvh->flags & FND_BVH_GPU_CLUSTER) || (bvh->flags & FND_BVH_GPU_BUILD),
+                   FND_ERR_INVALID_ARG, "FND_BVH_GPU_CLUSTER without FND_BVH_GPU_BUILD");
+        const uint32_t cluster_radius =
+            bvh && (bvh->flags & FND_BVH_GPU_CLUSTER) ? (radius_bits ? radius_bits : 2u) : 0u;
         RT::CollapseOptions copt;
         copt.sah = bvh && (bvh->flags & FND_BVH_SAH_COLLAPSE);
         copt.threads = bvh ? bvh->build_threads : 0u;
@@ -344,7 +355,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
             return;
         }
         if (gpu_build) {
-            UploadGpuBuilt(ctx, scene.get(), verts, nv, idx, nt, bp, margin_scale, copt);
+            UploadGpuBuilt(ctx, scene.get(), verts, nv, idx, nt, bp, margin_scale, copt, cluster_radius);
             *out_scene = scene.release();
             ctx->live_scenes++;
             return;

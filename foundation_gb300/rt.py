@@ -44,12 +44,18 @@ RENDER_ACCUMULATE = 1
 BVH_SPATIAL_SPLITS = 1
 BVH_GPU_BUILD = 2
 BVH_SAH_COLLAPSE = 4
+BVH_GPU_CLUSTER = 8
 RENDER_CACHE = 2
 RENDER_WAVEFRONT = 4
 RENDER_TRAIN_ONLY = 8
 TONEMAP_CLAMP, TONEMAP_REINHARD, TONEMAP_ACES = 0, 1, 2
 CACHE_NUM_PARAMS = 22720
 CACHE_NUM_FEATURES = 96
+
+
+def BVH_CLUSTER_RADIUS(r: int) -> int:
+    """FND_BVH_CLUSTER_RADIUS: the clustering search radius in bits 8..15 of the BVH flags."""
+    return (int(r) & 255) << 8
 
 
 class FndError(RuntimeError):
@@ -291,9 +297,12 @@ class Context:
     def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0,
                spatial_splits: bool = False, traversal_cost: float = 0.0, gpu_build: bool = False,
                split_budget: float = 0.0, margin_scale: float = 0.0, sah_collapse: bool = False,
-               collapse_tri_cost: float = 0.0) -> "Scene":
+               collapse_tri_cost: float = 0.0, cluster: bool = False, cluster_radius: int = 0) -> "Scene":
+        """cluster (with gpu_build): the binary tree by locally-ordered clustering
+        with search radius cluster_radius (1..64; 0: 2) instead of the Karras
+        hierarchy."""
         return Scene(self, verts, idx, bins, max_leaf, threads, spatial_splits, traversal_cost, gpu_build,
-                     split_budget, margin_scale, sah_collapse, collapse_tri_cost)
+                     split_budget, margin_scale, sah_collapse, collapse_tri_cost, cluster, cluster_radius)
 
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
@@ -442,13 +451,14 @@ class Context:
 class Scene:
     def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0, spatial_splits=False,
                  traversal_cost=0.0, gpu_build=False, split_budget=0.0, margin_scale=0.0, sah_collapse=False,
-                 collapse_tri_cost=0.0):
+                 collapse_tri_cost=0.0, cluster=False, cluster_radius=0):
         self._h = None
         self.ctx = ctx
         v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
         flags = ((BVH_SPATIAL_SPLITS if spatial_splits else 0) | (BVH_GPU_BUILD if gpu_build else 0) |
-                 (BVH_SAH_COLLAPSE if sah_collapse else 0))
+                 (BVH_SAH_COLLAPSE if sah_collapse else 0) | (BVH_GPU_CLUSTER if cluster else 0) |
+                 BVH_CLUSTER_RADIUS(cluster_radius))
         bd = _BvhDesc(bins, max_leaf, threads, flags, traversal_cost, split_budget, margin_scale, collapse_tri_cost)
         h = C.c_void_p()
         _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),

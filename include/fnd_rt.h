@@ -90,7 +90,8 @@ typedef struct fnd_rt_bvh_desc {
     uint32_t build_threads; /* host threads of the build and the collapse; 0: all
                                host cores. The tree does not depend on it, except
                                when a spatial-split budget runs out (split_budget) */
-    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD, FND_BVH_SAH_COLLAPSE or 0 */
+    uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD, FND_BVH_SAH_COLLAPSE,
+                               FND_BVH_GPU_CLUSTER (+ FND_BVH_CLUSTER_RADIUS(r)) or 0 */
     float traversal_cost;   /* SAH cost of a traversal step relative to a triangle
                                test, (0, 64]; 0: default 1 (the reference tree) */
     float split_budget;     /* FND_BVH_SPATIAL_SPLITS: references the splits may add,
@@ -127,6 +128,15 @@ enum { FND_BVH_GPU_BUILD = 2u };
  * the host build and on FND_BVH_GPU_BUILD alike; hits are identical either
  * way. */
 enum { FND_BVH_SAH_COLLAPSE = 4u };
+/* With FND_BVH_GPU_BUILD: the binary tree by parallel locally-ordered
+ * clustering over the Morton order (Meister & Bittner 2018) instead of the
+ * Karras hierarchy: each round merges the clusters that are each other's
+ * nearest neighbour (least merged box area) among the r clusters on either
+ * side. A slower build, a faster tree; hits are identical. */
+enum { FND_BVH_GPU_CLUSTER = 8u };
+/* The clustering's search radius r, 1..64, in bits 8..15 of flags; 0: 2 (the fastest
+ * trees of 1 - 64 on the traversal kernel). */
+#define FND_BVH_CLUSTER_RADIUS(r) ((uint32_t)(r) << 8)
 
 typedef struct fnd_rt_scene_info {
     uint32_t num_tris;

@@ -35,6 +35,18 @@ def test_library_exports_every_declared_symbol(built):
     assert set(names) <= set(rt.SIGNATURES)
 
 
+def test_binding_constants_match_the_header():
+    """The BVH flags (and the clustering radius field) of the Python binding
+    are the header's."""
+    from foundation_gb300 import rt
+    src = open(os.path.join(ROOT, "include", "fnd_rt.h")).read()
+    enums = {k: int(v) for k, v in re.findall(r"enum \{ (FND_\w+) = (\d+)u \};", src)}
+    for name in ("BVH_SPATIAL_SPLITS", "BVH_GPU_BUILD", "BVH_SAH_COLLAPSE", "BVH_GPU_CLUSTER"):
+        assert enums["FND_" + name] == getattr(rt, name), name
+    shift = int(re.search(r"#define FND_BVH_CLUSTER_RADIUS\(r\) \(\(uint32_t\)\(r\) << (\d+)\)", src).group(1))
+    assert rt.BVH_CLUSTER_RADIUS(5) == 5 << shift
+
+
 def test_null_arguments_return_status(built):
     from foundation_gb300 import rt
     lib = rt.load()

@@ -1,4 +1,5 @@
-"""BVH built on the GPU (FND_BVH_GPU_BUILD: linear BVH + SAH leaf merging +
+"""BVH built on the GPU (FND_BVH_GPU_BUILD: linear BVH or, with
+FND_BVH_GPU_CLUSTER, locally-ordered clustering, then SAH leaf merging and the
 device collapse to the 8-wide format): every hit equals the CPU oracle's
 (ids exact, t bit-identical), for tiny, degenerate and large scenes; bad
 input fails cleanly; a path-traced image equals the host-built scene's."""
@@ -40,24 +41,46 @@ def test_gpu_built_scene_matches_oracle(ctx, case):
         sc = S.soup_scene(1 << 20)
         rays = S.incoherent_rays(1 << 18, (0, 0, 0), (1, 1, 1), seed=2)
     b = O.OracleBVH(sc.verts, sc.idx)
-    g = ctx.upload(sc.verts, sc.idx, gpu_build=True)
-    info = g.info()
-    assert info["num_refs"] == sc.num_tris and 1 <= info["wide_depth"] <= 32
-    assert info["num_wide_nodes"] >= 1 and info["num_leaves"] >= 1
+    ref_closest, ref_any = b.closest(rays), b.any(rays)
     lo, hi = sc.verts[sc.idx.ravel()].min(0), sc.verts[sc.idx.ravel()].max(0)
-    assert np.array_equal(np.array(info["bounds_lo"], np.float32), lo)
-    assert np.array_equal(np.array(info["bounds_hi"], np.float32), hi)
-    assert_same(g.closest(rays), b.closest(rays))
-    assert np.array_equal(g.any(rays), b.any(rays))
-    # the SAH-optimal collapse on the device: fuller nodes, the same hits
-    gs = ctx.upload(sc.verts, sc.idx, gpu_build=True, sah_collapse=True)
-    si = gs.info()
-    assert 1 <= si["wide_depth"] <= 32 and si["num_refs"] == sc.num_tris
-    assert si["num_wide_nodes"] < info["num_wide_nodes"]
-    assert_same(gs.closest(rays), b.closest(rays))
-    assert np.array_equal(gs.any(rays), b.any(rays))
-    gs.close()
-    g.close()
+    sah = {}
+    for cluster in (False, True):
+        g = ctx.upload(sc.verts, sc.idx, gpu_build=True, cluster=cluster)
+        info = g.info()
+        sah[cluster] = info["sah_cost"]
+        assert info["num_refs"] == sc.num_tris and 1 <= info["wide_depth"] <= 32
+        assert info["num_wide_nodes"] >= 1 and info["num_leaves"] >= 1
+        assert np.array_equal(np.array(info["bounds_lo"], np.float32), lo)
+        assert np.array_equal(np.array(info["bounds_hi"], np.float32), hi)
+        assert_same(g.closest(rays), ref_closest)
+        assert np.array_equal(g.any(rays), ref_any)
+        # the SAH-optimal collapse on the device: fuller nodes, the same hits
+        gs = ctx.upload(sc.verts, sc.idx, gpu_build=True, sah_collapse=True, cluster=cluster)
+        si = gs.info()
+        assert 1 <= si["wide_depth"] <= 32 and si["num_refs"] == sc.num_tris
+        assert si["num_wide_nodes"] < info["num_wide_nodes"]
+        assert_same(gs.closest(rays), ref_closest)
+        assert np.array_equal(gs.any(rays), ref_any)
+        gs.close()
+        g.close()
+    # clustering gives the lower-cost binary tree
+    assert sah[True] < sah[False], sah
+
+
+@pytest.mark.parametrize("radius", [1, 2, 64])
+def test_clustered_build_at_radius_limits(ctx, radius):
+    """Radius 1 merges only neighbours in the array (the slowest progress),
+    64 is the widest window; the tree is deterministic, hits exact."""
+    sc = S.soup_scene(1 << 16)
+    rays = S.incoherent_rays(1 << 16, (0, 0, 0), (1, 1, 1), seed=5)
+    ref = O.OracleBVH(sc.verts, sc.idx).closest(rays)
+    infos = []
+    for _ in range(2):
+        g = ctx.upload(sc.verts, sc.idx, gpu_build=True, sah_collapse=True, cluster=True, cluster_radius=radius)
+        assert_same(g.closest(rays), ref)
+        infos.append({k: v for k, v in g.info().items() if not k.endswith("_ms")})
+        g.close()
+    assert infos[0] == infos[1]
 
 
 def test_gpu_build_tiny_and_degenerate(ctx):
@@ -68,18 +91,20 @@ def test_gpu_build_tiny_and_degenerate(ctx):
         rays = S.incoherent_rays(4096, (-1, -1, -1), (1, 1, 1), seed=n)
         ref = O.OracleBVH(v, f).closest(rays)
         for sah in (False, True):
-            g = ctx.upload(v, f, gpu_build=True, sah_collapse=sah)
-            assert_same(g.closest(rays), ref)
-            g.close()
+            for cluster in (False, True):
+                g = ctx.upload(v, f, gpu_build=True, sah_collapse=sah, cluster=cluster)
+                assert_same(g.closest(rays), ref)
+                g.close()
     # duplicates, a degenerate (zero-area) triangle, all centroids equal
     v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.5, 0.5, 0], [0.5, 0.5, 0], [0.5, 0.5, 0]], np.float32)
     f = np.array([[0, 1, 2]] * 40 + [[3, 4, 5]] * 3, np.uint32)
     rays = S.camera_rays(64, 64, eye=(0.3, 0.3, 2.0), target=(0.3, 0.3, 0.0))
     ref = O.OracleBVH(v, f).closest(rays)
     for sah in (False, True):
-        g = ctx.upload(v, f, gpu_build=True, sah_collapse=sah)
-        assert_same(g.closest(rays), ref)
-        g.close()
+        for cluster in (False, True):
+            g = ctx.upload(v, f, gpu_build=True, sah_collapse=sah, cluster=cluster, cluster_radius=3 if cluster else 0)
+            assert_same(g.closest(rays), ref)
+            g.close()
 
 
 def test_gpu_build_rejects_bad_input(ctx):
@@ -93,6 +118,12 @@ def test_gpu_build_rejects_bad_input(ctx):
         ctx.upload(v2, np.array([[0, 1, 2]], np.uint32), gpu_build=True)
     with pytest.raises(fg.FndError):
         ctx.upload(v, np.array([[0, 1, 2]], np.uint32), gpu_build=True, spatial_splits=True)
+    with pytest.raises(fg.FndError):  # clustering on the host build
+        ctx.upload(v, np.array([[0, 1, 2]], np.uint32), cluster=True)
+    with pytest.raises(fg.FndError):  # radius above 64
+        ctx.upload(v, np.array([[0, 1, 2]], np.uint32), gpu_build=True, cluster=True, cluster_radius=65)
+    with pytest.raises(fg.FndError):  # a radius without clustering
+        ctx.upload(v, np.array([[0, 1, 2]], np.uint32), gpu_build=True, cluster_radius=8)
     g = ctx.upload(v, np.zeros((0, 3), np.uint32), gpu_build=True)  # empty scene still works
     assert (g.closest(S.cube_camera_rays(10))["prim"] == fg.INVALID_ID).all()
     g.close()
