@@ -13,6 +13,10 @@ where the size bucket is floor(log2(triangles)), coherence is "coherent"
 (camera rays) or "incoherent", and the kind is "closest" or "any".
 `apply` selects the entry of the nearest size bucket for a workload.
 
+`tune_node_width` adds the node-width dimension: the scene is built with
+nodes of at most 4, 6 and 8 children, the launch shapes are tuned on each,
+and the entry keeps the fastest width (read back by `upload_options`).
+
 The path tracer's queue widths — paths in flight per wave and the queue
 length below which the tail megakernel finishes a wave — are tuned per image
 size and mode by `tune_render` (key "render:<w>x<h>:<plain|cache>") and read
@@ -83,6 +87,37 @@ def tune_workload(ctx: "rt.Context", table: TuneTable, scene: "rt.Scene", rays_d
                   kind: int = rt.QUERY_CLOSEST, reps: int = 3) -> dict:
     best, entries = ctx.tune(scene, rays_dev, kind=kind, reps=reps)
     return table.record(scene.info()["num_tris"], coherence, kind, best, entries)
+
+
+def tune_node_width(ctx: "rt.Context", table: TuneTable, verts, idx, rays_dev, coherence: str,
+                    kind: int = rt.QUERY_CLOSEST, widths=(4, 6, 8), reps: int = 3, **upload_kw) -> dict:
+    """The node-width dimension: builds the scene with nodes of at most w
+    children for every w in `widths` (upload_kw as for Context.upload), runs
+    the launch-shape tuner on each and records the width whose best shape is
+    the fastest, with that shape, under the workload's key. The entry's
+    "width_ms" holds every width's best time."""
+    results = []
+    num_tris = 0
+    for w in widths:
+        s = ctx.upload(verts, idx, node_width=w, **upload_kw)
+        try:
+            num_tris = s.info()["num_tris"]
+            best, entries = ctx.tune(s, rays_dev, kind=kind, reps=reps)
+        finally:
+            s.close()
+        results.append(dict(node_width=w, ms=min(e["ms"] for e in entries), best=best, entries=entries))
+    win = min(results, key=lambda r: r["ms"])
+    entry = table.record(num_tris, coherence, kind, win["best"], win["entries"])
+    entry["node_width"] = win["node_width"]
+    entry["width_ms"] = {str(r["node_width"]): r["ms"] for r in results}
+    return entry
+
+
+def upload_options(table: TuneTable, num_tris: int, coherence: str, kind: int = rt.QUERY_CLOSEST) -> dict:
+    """Keyword arguments for Context.upload from the nearest tuned entry: the
+    node width, if the entry was tuned over widths ({} otherwise)."""
+    e = table.lookup(num_tris, coherence, kind)
+    return {} if e is None or "node_width" not in e else dict(node_width=e["node_width"])
 
 
 def render_key(width: int, height: int, cache: bool) -> str:

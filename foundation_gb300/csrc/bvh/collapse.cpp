@@ -113,8 +113,8 @@ public:
     // below a breadth-first top part in parallel, each in reverse pre-order,
     // then the top part in reverse breadth-first order, so every node's
     // children are solved before it.
-    SahCollapse(const BinaryBvh& bin, double c_node, double c_tri, uint32_t threads)
-        : m_bin(bin), m_c_node(c_node), m_c_tri(c_tri) {
+    SahCollapse(const BinaryBvh& bin, double c_node, double c_tri, uint32_t threads, int width)
+        : m_bin(bin), m_c_node(c_node), m_c_tri(c_tri), m_width(width) {
         const size_t n = bin.nodes.size();
         m_cost.assign(8 * n, 0.0f);
         m_choice.assign(8 * n, 0);
@@ -150,7 +150,7 @@ public:
             return;
         }
         Gather(b.a, m_node_j[n], kids, nk);
-        Gather(b.a + 1, 8 - m_node_j[n], kids, nk);
+        Gather(b.a + 1, m_width - m_node_j[n], kids, nk);
     }
 
 private:
@@ -204,8 +204,9 @@ private:
                 }
             }
         }
-        const float node_cost = (float)(area * m_c_node) + split[8];
-        m_node_j[k] = split_j[8];
+        // a wide node: its children are the best split of m_width roots
+        const float node_cost = (float)(area * m_c_node) + split[m_width];
+        m_node_j[k] = split_j[m_width];
         c[0] = node_cost;
         if (m_tris[k] <= (uint32_t)kMaxLeafTris) {
             const float leaf_cost = (float)(area * m_c_tri * m_tris[k]);
@@ -239,6 +240,7 @@ private:
 
     const BinaryBvh& m_bin;
     const double m_c_node, m_c_tri;
+    const int m_width;               // children per wide node
     std::vector<uint32_t> m_tris;    // triangles (leaf slots) under n
     std::vector<float> m_cost;       // [8 n + i - 1]: C(n, i)
     std::vector<uint8_t> m_choice;   // [8 n + i - 1], i >= 2: 0 = C(n, i - 1), else roots given to the left child
@@ -269,13 +271,14 @@ void SubtreePrims(const BinaryBvh& bin, uint32_t n, uint32_t* out, uint32_t& cnt
 // The wide node made of binary node `bnode`: its children (SAH-optimal or
 // greedy), inflated child boxes, octant slots, quantised boxes and leaf
 // triangles. Depends on nothing outside the subtree of `bnode`.
-void PlanNode(const BinaryBvh& bin, const SahCollapse* sah, float margin, uint32_t bnode, NodePlan& plan) {
+void PlanNode(const BinaryBvh& bin, const SahCollapse* sah, float margin, int width, uint32_t bnode,
+              NodePlan& plan) {
     Kid kids[kWidth];
     int nk = 0;
     if (sah) {
         sah->NodeKids(bnode, kids, nk);
     } else {
-        // gather up to 8 children by expanding the largest internal child
+        // gather up to `width` children by expanding the largest internal child
         nk = 1;
         kids[0] = {bnode, bin.nodes[bnode].count > 0};
         for (;;) {
@@ -290,7 +293,7 @@ void PlanNode(const BinaryBvh& bin, const SahCollapse* sah, float margin, uint32
                     pick = k;
                 }
             }
-            if (pick < 0 || nk == kWidth) break;
+            if (pick < 0 || nk == width) break;
             const uint32_t l = bin.nodes[kids[pick].bnode].a;
             kids[pick] = {l, bin.nodes[l].count > 0};
             kids[nk++] = {l + 1, bin.nodes[l + 1].count > 0};
@@ -409,7 +412,9 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
     const uint32_t threads =
         opt.threads ? opt.threads : std::max(1u, (uint32_t)std::thread::hardware_concurrency());
     std::unique_ptr<SahCollapse> sah;
-    if (opt.sah) sah = std::make_unique<SahCollapse>(bin, opt.c_node, opt.c_tri, threads);
+    CHECK_CODE(opt.width >= 2 && opt.width <= (uint32_t)kWidth, FND_ERR_INVALID_ARG, "node width %u not in 2..%d",
+               opt.width, kWidth);
+    if (opt.sah) sah = std::make_unique<SahCollapse>(bin, opt.c_node, opt.c_tri, threads, (int)opt.width);
     const BinaryNode& root = bin.nodes[0];
     for (int i = 0; i < 3; ++i) {
         out.lo[i] = root.lo[i];
@@ -439,7 +444,7 @@ void CollapseToWide(const BinaryBvh& bin, const float* tri, uint32_t nt, WideBvh
     while (!level.empty()) {
         plans.resize(level.size());
         ParallelFor(level.size(), threads, kLevelChunk,
-                    [&](size_t i) { PlanNode(bin, sah.get(), margin, level[i].bnode, plans[i]); });
+                    [&](size_t i) { PlanNode(bin, sah.get(), margin, (int)opt.width, level[i].bnode, plans[i]); });
         next.clear();
         uint64_t child = out.nodes.size();
         for (size_t i = 0; i < level.size(); ++i) {

@@ -55,10 +55,11 @@ struct CollapseOptions {
     double c_node = 1.0;    // its cost of a wide-node visit per unit of half area
     double c_tri = 0.3;     // and of a triangle test (the kernel's best of 0.05 - 1)
     uint32_t threads = 0;   // host threads; 0: all cores. The output does not depend on it
+    uint32_t width = 8;     // children per wide node, 2..8 (the record always has 8 slots)
 };
 
-// Greedy collapse (largest-surface-area internal child expanded first until 8
-// children) or SAH-optimal collapse (opt.sah), octant-ordered slot assignment,
+// Greedy collapse (largest-surface-area internal child expanded first until
+// opt.width children) or SAH-optimal collapse (opt.sah), octant-ordered slot assignment,
 // 8-bit outward quantisation; wide nodes in breadth-first order, computed a
 // level at a time on opt.threads threads. margin_scale multiplies SceneMargin (a
 // bottom-level scene whose instances shrink it far below the world's size

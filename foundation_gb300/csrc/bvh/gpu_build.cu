@@ -77,6 +77,7 @@ struct Buffers {
     uint8_t* dpj;                 // roots given to the left child when k is a wide node
     uint8_t* dpleaf;              // C(k, 1) is one leaf slot
     float c_tri;                  // cost of a triangle test relative to a wide-node visit
+    uint32_t width;               // children per wide node (2..8)
 };
 
 __device__ __forceinline__ void atomic_min_f(float* a, float v) {
@@ -635,7 +636,7 @@ __global__ void __launch_bounds__(256) refit_kernel(uint32_t n, Buffers B, uint3
                 }
             }
             float c[8];
-            const float node_cost = a + sp[8];
+            const float node_cost = a + sp[B.width];
             c[0] = node_cost;
             uint8_t as_leaf = 0;
             if (cnt <= (uint32_t)kMaxLeafTris) {
@@ -658,7 +659,7 @@ __global__ void __launch_bounds__(256) refit_kernel(uint32_t n, Buffers B, uint3
             dc[0] = make_float4(c[0], c[1], c[2], c[3]);
             dc[1] = make_float4(c[4], c[5], c[6], c[7]);
             for (int i = 0; i < 8; ++i) B.dpch[8 * (size_t)p + i] = ch[i];
-            B.dpj[p] = sj[8];
+            B.dpj[p] = sj[B.width];
             B.dpleaf[p] = as_leaf;
         }
         p = B.parent_i[p];
@@ -693,7 +694,7 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
             uint2 st[16];
             int sp = 0;
             const uint32_t j = B.dpj[item.x];
-            st[sp++] = make_uint2(B.right[item.x], 8u - j);
+            st[sp++] = make_uint2(B.right[item.x], B.width - j);
             st[sp++] = make_uint2(B.left[item.x], j);
             nk = 0;
             while (sp > 0) {
@@ -728,7 +729,7 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
                     pick = c;
                 }
             }
-            if (pick < 0 || nk == kWidth) break;
+            if (pick < 0 || nk == (int)B.width) break;
             const uint32_t p = kids[pick];
             kids[pick] = B.left[p];
             kids[nk++] = B.right[p];
@@ -1023,6 +1024,8 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
                kGpuBuildMaxTris, nt);
     CHECK_CODE(p.max_leaf >= 1 && p.max_leaf <= (uint32_t)kMaxLeafTris, FND_ERR_INVALID_ARG, "max_leaf %u",
                p.max_leaf);
+    CHECK_CODE(p.width >= 2 && p.width <= (uint32_t)kWidth, FND_ERR_INVALID_ARG, "node width %u not in 2..%d",
+               p.width, kWidth);
     CHECK_CODE(p.ploc_radius <= (uint32_t)kPlocMaxRadius, FND_ERR_INVALID_ARG, "clustering radius %u above %d",
                p.ploc_radius, kPlocMaxRadius);
     int dev = 0, sms = 0;
@@ -1053,6 +1056,7 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     B.bounds = S.get<float>(12);
     B.status = S.get<uint32_t>(1);
     B.counters = S.get<uint32_t>(4 + kMaxLevels + 2);
+    B.width = p.width;
     B.qa = S.get<uint2>(n);
     B.qb = S.get<uint2>(n);
     if (p.sah_collapse && n >= 2) {

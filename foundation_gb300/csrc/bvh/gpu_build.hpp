@@ -26,6 +26,7 @@ struct GpuBuildParams {
     float margin_scale = 1.0f;
     bool sah_collapse = false;  // SAH-optimal collapse (collapse.hpp) instead of the greedy one
     float c_tri = 0.3f;         // its cost of a triangle test relative to a wide-node visit
+    uint32_t width = 8;         // children per wide node, 2..8
     uint32_t ploc_radius = 0;   // binary tree by locally-ordered clustering with this search radius
                                 // (1..64); 0: Karras hierarchy
 };

@@ -144,6 +144,7 @@ void UploadGpuBuilt(fnd_rt_ctx* ctx, fnd_rt_scene* scene, const float* verts, ui
         gp.sah_collapse = copt.sah;
         gp.c_tri = (float)copt.c_tri;
         gp.ploc_radius = cluster_radius;
+        gp.width = copt.width;
         RT::BuildWideGpu(static_cast<const float*>(d_verts), nv, static_cast<const uint32_t*>(d_idx), nt, gp, go,
                          ctx->stream);
         CUDA_CHECK(cudaFree(d_verts));
@@ -326,9 +327,12 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
                    bp.max_leaf);
         CHECK_CODE(!bvh || (bvh->flags & ~(uint32_t)(FND_BVH_SPATIAL_SPLITS | FND_BVH_GPU_BUILD |
                                                      FND_BVH_SAH_COLLAPSE | FND_BVH_GPU_CLUSTER |
-                                                     FND_BVH_CLUSTER_RADIUS(255))) == 0,
+                                                     FND_BVH_CLUSTER_RADIUS(255) | FND_BVH_NODE_WIDTH(15))) == 0,
                    FND_ERR_INVALID_ARG, "unknown BVH flags 0x%x", bvh ? bvh->flags : 0u);
         const uint32_t radius_bits = bvh ? (bvh->flags >> 8) & 255u : 0u;
+        const uint32_t width_bits = bvh ? (bvh->flags >> 16) & 15u : 0u;
+        CHECK_CODE(width_bits == 0 || (width_bits >= 2 && width_bits <= 8), FND_ERR_INVALID_ARG,
+                   "node width %u not in 2..8", width_bits);
         CHECK_CODE(radius_bits <= 64, FND_ERR_INVALID_ARG, "clustering radius %u not in 1..64", radius_bits);
         CHECK_CODE(!bvh || (bvh->flags & FND_BVH_GPU_CLUSTER) || radius_bits == 0, FND_ERR_INVALID_ARG,
                    "FND_BVH_CLUSTER_RADIUS without FND_BVH_GPU_CLUSTER");
@@ -339,6 +343,7 @@ int fnd_rt_scene_upload(fnd_rt_ctx* ctx, const float* verts, uint32_t nv, const 
         RT::CollapseOptions copt;
         copt.sah = bvh && (bvh->flags & FND_BVH_SAH_COLLAPSE);
         copt.threads = bvh ? bvh->build_threads : 0u;
+        copt.width = width_bits ? width_bits : 8u;
         copt.c_tri = bvh && bvh->collapse_tri_cost != 0.0f ? bvh->collapse_tri_cost : 0.3;
         CHECK_CODE(copt.c_tri > 0.0 && copt.c_tri <= 16.0, FND_ERR_INVALID_ARG, "collapse_tri_cost %g not in (0, 16]",
                    copt.c_tri);

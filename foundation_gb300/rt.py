@@ -58,6 +58,11 @@ def BVH_CLUSTER_RADIUS(r: int) -> int:
     return (int(r) & 255) << 8
 
 
+def BVH_NODE_WIDTH(w: int) -> int:
+    """FND_BVH_NODE_WIDTH: children per wide node (2..8) in bits 16..19 of the BVH flags."""
+    return (int(w) & 15) << 16
+
+
 class FndError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
@@ -297,12 +302,14 @@ class Context:
     def upload(self, verts, idx, bins: int = 32, max_leaf: int = 4, threads: int = 0,
                spatial_splits: bool = False, traversal_cost: float = 0.0, gpu_build: bool = False,
                split_budget: float = 0.0, margin_scale: float = 0.0, sah_collapse: bool = False,
-               collapse_tri_cost: float = 0.0, cluster: bool = False, cluster_radius: int = 0) -> "Scene":
+               collapse_tri_cost: float = 0.0, cluster: bool = False, cluster_radius: int = 0,
+               node_width: int = 0) -> "Scene":
         """cluster (with gpu_build): the binary tree by locally-ordered clustering
         with search radius cluster_radius (1..64; 0: 2) instead of the Karras
-        hierarchy."""
+        hierarchy. node_width: children per wide node (2..8; 0: 8)."""
         return Scene(self, verts, idx, bins, max_leaf, threads, spatial_splits, traversal_cost, gpu_build,
-                     split_budget, margin_scale, sah_collapse, collapse_tri_cost, cluster, cluster_radius)
+                     split_budget, margin_scale, sah_collapse, collapse_tri_cost, cluster, cluster_radius,
+                     node_width)
 
     def render(self, scene: "Scene", width: int, height: int, spp: int, camera: dict, *, max_depth: int = 8,
                rr_start: int = 3, seed: int = 1, sky=(0.0, 0.0, 0.0), sun_dir=(0.0, 0.0, 0.0),
@@ -451,14 +458,14 @@ class Context:
 class Scene:
     def __init__(self, ctx: Context, verts, idx, bins=32, max_leaf=4, threads=0, spatial_splits=False,
                  traversal_cost=0.0, gpu_build=False, split_budget=0.0, margin_scale=0.0, sah_collapse=False,
-                 collapse_tri_cost=0.0, cluster=False, cluster_radius=0):
+                 collapse_tri_cost=0.0, cluster=False, cluster_radius=0, node_width=0):
         self._h = None
         self.ctx = ctx
         v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
         f = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
         flags = ((BVH_SPATIAL_SPLITS if spatial_splits else 0) | (BVH_GPU_BUILD if gpu_build else 0) |
                  (BVH_SAH_COLLAPSE if sah_collapse else 0) | (BVH_GPU_CLUSTER if cluster else 0) |
-                 BVH_CLUSTER_RADIUS(cluster_radius))
+                 BVH_CLUSTER_RADIUS(cluster_radius) | BVH_NODE_WIDTH(node_width))
         bd = _BvhDesc(bins, max_leaf, threads, flags, traversal_cost, split_budget, margin_scale, collapse_tri_cost)
         h = C.c_void_p()
         _check(load().fnd_rt_scene_upload(ctx.handle, _ptr(v), len(v), _ptr(f), len(f), C.byref(bd), C.byref(h)),

@@ -91,7 +91,8 @@ typedef struct fnd_rt_bvh_desc {
                                host cores. The tree does not depend on it, except
                                when a spatial-split budget runs out (split_budget) */
     uint32_t flags;         /* FND_BVH_SPATIAL_SPLITS, FND_BVH_GPU_BUILD, FND_BVH_SAH_COLLAPSE,
-                               FND_BVH_GPU_CLUSTER (+ FND_BVH_CLUSTER_RADIUS(r)) or 0 */
+                               FND_BVH_GPU_CLUSTER (+ FND_BVH_CLUSTER_RADIUS(r)),
+                               FND_BVH_NODE_WIDTH(w) or 0 */
     float traversal_cost;   /* SAH cost of a traversal step relative to a triangle
                                test, (0, 64]; 0: default 1 (the reference tree) */
     float split_budget;     /* FND_BVH_SPATIAL_SPLITS: references the splits may add,
@@ -137,6 +138,10 @@ enum { FND_BVH_GPU_CLUSTER = 8u };
 /* The clustering's search radius r, 1..64, in bits 8..15 of flags; 0: 2 (the fastest
  * trees of 1 - 64 on the traversal kernel). */
 #define FND_BVH_CLUSTER_RADIUS(r) ((uint32_t)(r) << 8)
+/* Children per wide node, 2..8, in bits 16..19 of flags; 0: 8. The node
+ * record and its test keep 8 slots whatever the width (a narrower tree has
+ * more, emptier nodes): the autotuner's node-width dimension. Any build. */
+#define FND_BVH_NODE_WIDTH(w) ((uint32_t)(w) << 16)
 
 typedef struct fnd_rt_scene_info {
     uint32_t num_tris;

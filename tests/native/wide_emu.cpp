@@ -174,6 +174,38 @@ emu_bvh* emu_build_sah_collapse(const float* verts, uint32_t nv, const uint32_t*
     return e;
 }
 
+// Binned SAH collapsed to nodes of at most `width` children (greedy, or the
+// SAH-optimal rule with sah != 0).
+emu_bvh* emu_build_width(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, int sah,
+                         uint32_t width) {
+    auto* e = new emu_bvh();
+    std::vector<float> tri(9 * (size_t)nt);
+    for (uint32_t t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) tri[9 * (size_t)t + 3 * k + c] = verts[3 * (size_t)idx[3 * (size_t)t + k] + c];
+    BuildParams p;
+    BuildBinaryBvh(tri.data(), nt, p, e->bin);
+    CollapseOptions o;
+    o.sah = sah != 0;
+    o.width = width;
+    CollapseToWide(e->bin, tri.data(), nt, e->wide, 1.0f, o);
+    e->view.nodes = reinterpret_cast<const uint4*>(e->wide.nodes.data());
+    e->view.v0 = reinterpret_cast<const float4*>(e->wide.v0.data());
+    e->view.v1 = reinterpret_cast<const float4*>(e->wide.v1.data());
+    e->view.v2 = reinterpret_cast<const float4*>(e->wide.v2.data());
+    e->view.num_nodes = (uint32_t)e->wide.nodes.size();
+    e->view.num_tris = (uint32_t)e->bin.prims.size();
+    (void)nv;
+    return e;
+}
+
+// The wide tree's node records (80 bytes each), copied to out (nodes x 80
+// bytes); returns the node count.
+uint32_t emu_nodes(const emu_bvh* e, void* out) {
+    if (out) std::memcpy(out, e->wide.nodes.data(), e->wide.nodes.size() * sizeof(WideNode));
+    return (uint32_t)e->wide.nodes.size();
+}
+
 // FNV-1a hash of the bytes of the wide tree (nodes, then the three plane
 // arrays) that e's binary tree collapses to on `threads` threads, by the
 // SAH-optimal rule (sah != 0) or the greedy one.

@@ -40,6 +40,31 @@ def test_tune_pass_on_gpu(built, tmp_path):
 
 
 @pytest.mark.gpu
+def test_node_width_tuned(built, tmp_path):
+    """The tuner's node-width dimension: every width is built and tuned, the
+    recorded width is the fastest, and upload_options gives it back."""
+    import torch
+    import foundation_gb300 as fg
+    from foundation_gb300 import scenes as S
+    cs = S.cornell_scene(num_spheres=50)
+    with fg.Context(0) as ctx:
+        rays = torch.from_numpy(S.incoherent_rays(1 << 17, *cs.bounds, seed=6)).cuda()
+        t = AT.TuneTable()
+        e = AT.tune_node_width(ctx, t, cs.verts, cs.idx, rays, "incoherent", widths=(4, 8), reps=1,
+                               sah_collapse=True)
+        assert set(e["width_ms"]) == {"4", "8"}
+        assert e["width_ms"][str(e["node_width"])] == min(e["width_ms"].values())
+        opts = AT.upload_options(t, cs.num_tris, "incoherent")
+        assert opts == dict(node_width=e["node_width"])
+        s = ctx.upload(cs.verts, cs.idx, sah_collapse=True, **opts)
+        assert s.info()["num_tris"] == cs.num_tris
+        s.close()
+        p = str(tmp_path / "t.json")
+        t.save(p)
+        assert AT.TuneTable.load(p).entries == t.entries
+
+
+@pytest.mark.gpu
 def test_render_queue_widths_tuned(built, tmp_path):
     import foundation_gb300 as fg
     from foundation_gb300 import scenes as S

@@ -29,6 +29,10 @@ def emu(built):
     L.emu_num_refs.argtypes = [P]
     L.emu_build_sah_collapse.restype = P
     L.emu_build_sah_collapse.argtypes = [P, C.c_uint32, P, C.c_uint32, C.c_int, C.c_double]
+    L.emu_build_width.restype = P
+    L.emu_build_width.argtypes = [P, C.c_uint32, P, C.c_uint32, C.c_int, C.c_uint32]
+    L.emu_nodes.restype = C.c_uint32
+    L.emu_nodes.argtypes = [P, P]
     L.emu_collapse_hash.restype = C.c_uint64
     L.emu_collapse_hash.argtypes = [P, P, P, C.c_uint32, C.c_int, C.c_uint32]
     return L
@@ -234,3 +238,43 @@ def test_collapse_independent_of_threads(emu, scene):
                 assert len(hashes) == 1, (scene, spatial, sah)
         finally:
             emu.emu_free(h)
+
+
+@pytest.mark.parametrize("sah", [0, 1])
+def test_emulated_node_width(emu, sah):
+    """Nodes of at most 2, 4 and 6 children (the autotuner's node-width
+    dimension; the record keeps its 8 slots): no node uses more slots than
+    the width, narrower trees have more nodes, and the hits are the oracle's,
+    on Cornell rays and on the small and degenerate trees."""
+    sc, rays = CASES["cornell_incoherent"]()
+    v = np.ascontiguousarray(sc.verts, np.float32)
+    f = np.ascontiguousarray(sc.idx, np.uint32)
+    ref = O.OracleBVH(sc.verts, sc.idx).closest(rays)
+    counts = {}
+    for width in (2, 4, 6, 8):
+        e = Emu.__new__(Emu)
+        e.L, e.v, e.f = emu, v, f
+        e.h = emu.emu_build_width(_p(v), len(v), _p(f), len(f), sah, width)
+        n = emu.emu_nodes(e.h, None)
+        raw = np.zeros((n, 80), np.uint8)
+        emu.emu_nodes(e.h, _p(raw))
+        used = (raw[:, 24:32] != 0).sum(1)
+        assert used.max() <= width and used.min() >= 1
+        counts[width] = n
+        prim, tbits, _ = e.trace(rays)
+        assert np.array_equal(prim, ref["prim"]), width
+        assert np.array_equal(tbits, ref["t"].view(np.uint32))
+    assert counts[2] > counts[4] > counts[6] > counts[8]
+    rng = np.random.default_rng(11)
+    for n in (1, 2, 3, 5, 9, 33):
+        vv = rng.uniform(-1, 1, (3 * n, 3)).astype(np.float32)
+        ff = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+        rr = S.incoherent_rays(2048, (-1, -1, -1), (1, 1, 1), seed=n)
+        want = O.brute_closest(vv, ff, rr)
+        for width in (2, 3):
+            e = Emu.__new__(Emu)
+            e.L, e.v, e.f = emu, vv, ff
+            e.h = emu.emu_build_width(_p(vv), len(vv), _p(ff), len(ff), sah, width)
+            prim, tbits, _ = e.trace(rr)
+            assert np.array_equal(prim, want["prim"]), (n, width)
+            assert np.array_equal(tbits, want["t"].view(np.uint32))

@@ -142,3 +142,25 @@ def test_gpu_built_scene_renders_like_host_built(ctx):
         s.close()
     assert stats[0] == stats[1]
     np.testing.assert_allclose(imgs[1], imgs[0], rtol=1e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("gpu", [False, True], ids=["host_build", "gpu_build"])
+def test_node_width(ctx, gpu):
+    """Nodes of at most 2, 4 and 6 children (FND_BVH_NODE_WIDTH), greedy and
+    SAH-optimal collapse, host and GPU builds: the oracle's hits, and more
+    wide nodes the narrower they are."""
+    import foundation_gb300 as fg
+    sc = S.cornell_scene(num_spheres=40)
+    rays = S.incoherent_rays(1 << 17, *sc.bounds, seed=4)
+    ref = O.OracleBVH(sc.verts, sc.idx).closest(rays)
+    for sah in (False, True):
+        nodes = []
+        for width in (2, 4, 6, 8):
+            g = ctx.upload(sc.verts, sc.idx, gpu_build=gpu, cluster=gpu, sah_collapse=sah, node_width=width)
+            assert_same(g.closest(rays), ref)
+            nodes.append(g.info()["num_wide_nodes"])
+            g.close()
+        assert nodes == sorted(nodes, reverse=True) and nodes[0] > nodes[-1], nodes
+    for bad in (1, 9):
+        with pytest.raises(fg.FndError):
+            ctx.upload(sc.verts[:3], sc.idx[:1] * 0 + np.arange(3, dtype=np.uint32), node_width=bad)
