@@ -14,11 +14,36 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
+#include <new>
+#include <utility>
 #include <vector>
 
 namespace Foundation {
 namespace RT {
 
+// Allocator whose value-initialisation (vector(n), resize(n)) leaves the
+// elements uninitialised: the builders and the collapse write every element
+// themselves, on several threads, instead of one thread zero-filling
+// gigabytes first.
+template <class T>
+struct NoInitAllocator : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInitAllocator<U>;
+    };
+    NoInitAllocator() = default;
+    template <class U>
+    NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
+    template <class U>
+    void construct(U* p) noexcept {
+        ::new (static_cast<void*>(p)) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) {
+        ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+    }
+};
 struct Aabb {
     float lo[3], hi[3];
 };
@@ -30,8 +55,8 @@ struct BinaryNode {
 };
 
 struct BinaryBvh {
-    std::vector<BinaryNode> nodes;  // nodes[0] is the root
-    std::vector<uint32_t> prims;    // leaf slots -> original triangle index
+    std::vector<BinaryNode, NoInitAllocator<BinaryNode>> nodes;  // nodes[0] is the root
+    std::vector<uint32_t, NoInitAllocator<uint32_t>> prims;      // leaf slots -> original triangle index
     uint32_t depth = 0;
     uint32_t leaves = 0;
     double sah_cost = 0.0;  // normalised by the root half-area

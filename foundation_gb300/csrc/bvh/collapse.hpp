@@ -13,27 +13,6 @@
 namespace Foundation {
 namespace RT {
 
-// Allocator whose value-initialisation (vector(n), resize(n)) leaves the
-// elements uninitialised: the collapse writes every plane element itself, on
-// several threads, instead of one thread zero-filling gigabytes first.
-template <class T>
-struct NoInitAllocator : std::allocator<T> {
-    template <class U>
-    struct rebind {
-        using other = NoInitAllocator<U>;
-    };
-    NoInitAllocator() = default;
-    template <class U>
-    NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
-    template <class U>
-    void construct(U* p) noexcept {
-        ::new (static_cast<void*>(p)) U;
-    }
-    template <class U, class... A>
-    void construct(U* p, A&&... a) {
-        ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
-    }
-};
 using PlaneVector = std::vector<float, NoInitAllocator<float>>;
 
 struct WideBvh {

@@ -101,8 +101,8 @@ struct Split {
 };
 
 struct Out {
-    std::vector<BinaryNode> nodes;
-    std::vector<uint32_t> prims;
+    std::vector<BinaryNode, NoInitAllocator<BinaryNode>> nodes;
+    std::vector<uint32_t, NoInitAllocator<uint32_t>> prims;
     uint32_t depth = 0, leaves = 0;
     double sah = 0.0;
 };

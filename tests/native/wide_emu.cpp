@@ -206,6 +206,44 @@ uint32_t emu_nodes(const emu_bvh* e, void* out) {
     return (uint32_t)e->wide.nodes.size();
 }
 
+// FNV-1a hash of the binary tree the binned-SAH builder makes on `threads`
+// threads, in depth-first order: every node's box and triangle count and
+// every leaf's triangle indices (the node numbering is left out: it follows
+// the order the threads take the nodes in).
+uint64_t emu_binary_hash(const float* verts, const uint32_t* idx, uint32_t nt, uint32_t threads) {
+    std::vector<float> tri(9 * (size_t)nt);
+    for (uint32_t t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) tri[9 * (size_t)t + 3 * k + c] = verts[3 * (size_t)idx[3 * (size_t)t + k] + c];
+    BuildParams p;
+    p.threads = threads;
+    BinaryBvh b;
+    BuildBinaryBvh(tri.data(), nt, p, b);
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void* q, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(q);
+        for (size_t i = 0; i < n; ++i) {
+            h ^= c[i];
+            h *= 1099511628211ull;
+        }
+    };
+    std::vector<uint32_t> stack{0u};
+    while (!stack.empty()) {
+        const BinaryNode& nd = b.nodes[stack.back()];
+        stack.pop_back();
+        mix(nd.lo, sizeof(nd.lo));
+        mix(nd.hi, sizeof(nd.hi));
+        mix(&nd.count, sizeof(nd.count));
+        if (nd.count) {
+            mix(&b.prims[nd.a], sizeof(uint32_t) * nd.count);
+        } else {
+            stack.push_back(nd.a + 1);
+            stack.push_back(nd.a);
+        }
+    }
+    return h;
+}
+
 // FNV-1a hash of the bytes of the wide tree (nodes, then the three plane
 // arrays) that e's binary tree collapses to on `threads` threads, by the
 // SAH-optimal rule (sah != 0) or the greedy one.

@@ -33,6 +33,8 @@ def emu(built):
     L.emu_build_width.argtypes = [P, C.c_uint32, P, C.c_uint32, C.c_int, C.c_uint32]
     L.emu_nodes.restype = C.c_uint32
     L.emu_nodes.argtypes = [P, P]
+    L.emu_binary_hash.restype = C.c_uint64
+    L.emu_binary_hash.argtypes = [P, P, C.c_uint32, C.c_uint32]
     L.emu_collapse_hash.restype = C.c_uint64
     L.emu_collapse_hash.argtypes = [P, P, P, C.c_uint32, C.c_int, C.c_uint32]
     return L
@@ -278,3 +280,20 @@ def test_emulated_node_width(emu, sah):
             prim, tbits, _ = e.trace(rr)
             assert np.array_equal(prim, want["prim"]), (n, width)
             assert np.array_equal(tbits, want["t"].view(np.uint32))
+
+
+@pytest.mark.parametrize("scene", ["soup", "identical"])
+def test_binary_build_independent_of_threads(emu, scene):
+    """The binned-SAH tree (boxes, counts, leaf triangles in depth-first
+    order) is the same on 1, 2, 3 and 8 build threads: large nodes are split
+    with every thread (bins merged, stable partition through per-chunk
+    offsets), the rest one node per thread. The identical-triangles case
+    takes the index-median split in both phases."""
+    if scene == "soup":
+        sc = S.soup_scene(300000, seed=6)
+        v, f = np.ascontiguousarray(sc.verts, np.float32), np.ascontiguousarray(sc.idx, np.uint32)
+    else:
+        v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+        f = np.zeros((150000, 3), np.uint32) + np.arange(3, dtype=np.uint32)
+    hashes = {emu.emu_binary_hash(_p(v), _p(f), len(f), t) for t in (1, 2, 3, 8)}
+    assert len(hashes) == 1
