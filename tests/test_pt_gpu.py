@@ -159,15 +159,15 @@ def test_render_does_not_depend_on_the_tree(ctx):
         np.testing.assert_allclose(img, imgs[0], rtol=1e-4, atol=1e-6)
 
 
-def test_time_to_relmse_judge_matches_fp64_oracle_on_1080p_crops(ctx):
+def test_time_to_relmse_reference_matches_fp64_oracle_on_1080p_crops(ctx):
     """The time-to-relMSE reference is the GPU's own plain render
     (convergence.render_reference, 8192 spp in the bench). Checked here at
-    its full 1920x1080 geometry: three 24x24 crops of a 1024-spp judge render
-    (centre, the brightest block, a block of median brightness) against the FP64 oracle's
-    path tracer at 4096 spp over the same crops. Without bias the judge's
-    relMSE against the oracle is about 0.6x the relMSE between two judge
-    renders of different seeds; the bar is 1.5x, and the crop means agree
-    within 2%."""
+    its full 1920x1080 geometry: three 24x24 crops of a 1024-spp reference
+    render (centre, the brightest block, a block of median brightness)
+    against the FP64 oracle's path tracer at 4096 spp over the same crops.
+    Without bias the reference render's relMSE against the oracle is about
+    0.6x the relMSE between two reference renders of different seeds; the bar
+    is 1.5x, and the crop means agree within 2%."""
     from foundation_gb300 import convergence as CV
     cs = S.cornell_scene()
     s = upload(ctx, cs)
