@@ -12,6 +12,11 @@
 //  * one thread per ray; the traversal state is a "node group" (base index of
 //    a node's internal children + the ordered bit mask of children still to
 //    visit) and a "triangle group" (base + bit mask of triangles to test);
+//  * a node's hit mask goes to the ray's traversal order (bit i: slot
+//    i ^ oct) through a shared 8 x 256-byte table in the single-scene and
+//    batched kernels (one load in place of three conditional bit swaps:
+//    +1.6% on the issue-bound kernel; the two-level kernel, whose shared
+//    memory already holds the world rays, keeps the swaps);
 //  * the stack holds node groups; its top kShort entries live in shared
 //    memory (one column per thread, bank-conflict free), deeper entries spill
 //    to a thread-local array; the depth bound kMaxStack is checked on the
@@ -303,7 +308,7 @@ template <class Src, int kKind, bool kStats, int kShort, int kBlock, bool kTwoLe
           bool kMulti = false>
 __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C, uint2* s_stack,
                                                  CoopShared<kBlock, kMulti>* s_coop = nullptr,
-                                                 RayState* s_world = nullptr) {
+                                                 RayState* s_world = nullptr, const uint8_t* s_perm = nullptr) {
     // two-level cooperative rounds: each lane's planes and hit-id offset
     // come from its own slot (the lanes of a warp sit in different instances)
     static_assert(!(kCoop && kTwoLevel) || kMulti, "two-level cooperative rounds need per-lane scenes");
@@ -415,7 +420,7 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
             if (ng_group & 0xFFu) overflow = !push(make_uint2(ng_base, ng_group));
             if (overflow) {
             } else if (child < sc.num_nodes) {
-                const NodeHits h = intersect_node(r, sc.nodes, child, best_t);
+                const NodeHits h = intersect_node(r, sc.nodes, child, best_t, s_perm);
                 if (kStats) {
                     st_nodes++;
                     if (lane == (uint32_t)__ffs(__activemask()) - 1u) st_wnode++;
@@ -582,10 +587,18 @@ __device__ __forceinline__ void persistent_trace(const Src& src, const Common& C
 // unless the block is 256 threads wide.
 constexpr int MinBlocks(int block) { return block == 256 ? 4 : 1152 / block; }
 
+// Fills the 8 x 256 byte table of xor_permute8 (all threads of the block).
+__device__ __forceinline__ void fill_perm(uint8_t* t) {
+    for (uint32_t i = threadIdx.x; i < 2048u; i += blockDim.x) t[i] = (uint8_t)xor_permute8(i & 255u, i >> 8);
+    __syncthreads();
+}
+
 template <bool kAny, bool kStats, int kShort, int kBlock>
 __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const TraceLaunch L) {
     __shared__ uint2 s_stack[kShort * kBlock];
     __shared__ CoopShared<kBlock, false> s_coop;
+    __shared__ uint8_t s_perm[2048];
+    fill_perm(s_perm);
     SingleSource src;
     src.scene = L.scene;
     src.rays = L.rays;
@@ -595,20 +608,24 @@ __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const 
     src.n = L.n_dev ? min(*L.n_dev, L.n) : L.n;
     if (L.ray_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(L.ray_total, (unsigned long long)src.n);
     const Common C{L.counter, L.status, L.stats, L.refill_min, L.postpone_min};
-    persistent_trace<SingleSource, kAny ? 1 : 0, kStats, kShort, kBlock, false, true>(src, C, s_stack, &s_coop);
+    persistent_trace<SingleSource, kAny ? 1 : 0, kStats, kShort, kBlock, false, true>(src, C, s_stack, &s_coop, nullptr,
+                                                                                     s_perm);
 }
 
 template <int kShort, int kBlock>
 __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) batch_kernel(const BatchLaunch B) {
     __shared__ uint2 s_stack[kShort * kBlock];
     __shared__ CoopShared<kBlock, true> s_coop;
+    __shared__ uint8_t s_perm[2048];
+    fill_perm(s_perm);
     BatchSource src;
     src.jobs = B.jobs;
     src.prefix = B.prefix;
     src.njobs = B.njobs;
     src.n = B.total;
     const Common C{B.counter, B.status, nullptr, B.refill_min, B.postpone_min};
-    persistent_trace<BatchSource, 2, false, kShort, kBlock, false, true, true>(src, C, s_stack, &s_coop);
+    persistent_trace<BatchSource, 2, false, kShort, kBlock, false, true, true>(src, C, s_stack, &s_coop, nullptr,
+                                                                             s_perm);
 }
 
 template <bool kAny>

@@ -207,8 +207,10 @@ struct NodeHits {
     uint32_t tris;
 };
 
+// perm (optional): a table of 8 x 256 bytes, perm[oct * 256 + m] =
+// xor_permute8(m, oct), in place of the bit swaps.
 __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint4* __restrict__ nodes, uint32_t idx,
-                                                   float tfar) {
+                                                   float tfar, const uint8_t* perm = nullptr) {
     const uint4* n = nodes + 5 * (size_t)idx;
     const uint4 w0 = __ldg(n + 0);
     const uint4 w1 = __ldg(n + 1);
@@ -283,7 +285,7 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
     NodeHits out;
     out.child_base = w1.x;
     out.tri_base = w1.y;
-    out.group = (imask << 8) | xor_permute8(hitm & imask, r.oct);
+    out.group = (imask << 8) | (perm ? (uint32_t)perm[(r.oct << 8) | (hitm & imask)] : xor_permute8(hitm & imask, r.oct));
     out.tris = tris;
     return out;
 }
