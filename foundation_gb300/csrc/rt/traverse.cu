@@ -590,6 +590,8 @@ constexpr int MinBlocks(int block) { return block == 256 ? 4 : 1152 / block; }
 // Fills the 8 x 256 byte table of xor_permute8 (all threads of the block).
 __device__ __forceinline__ void fill_perm(uint8_t* t) {
     for (uint32_t i = threadIdx.x; i < 2048u; i += blockDim.x) t[i] = (uint8_t)xor_permute8(i & 255u, i >> 8);
+    uint32_t* m = reinterpret_cast<uint32_t*>(t + 2048);
+    for (uint32_t i = threadIdx.x; i < 256u; i += blockDim.x) m[i] = ((2u << ((i >> 5) & 3u)) - 1u) << (i & 31u);
     __syncthreads();
 }
 
@@ -597,7 +599,7 @@ template <bool kAny, bool kStats, int kShort, int kBlock>
 __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) trace_kernel(const TraceLaunch L) {
     __shared__ uint2 s_stack[kShort * kBlock];
     __shared__ CoopShared<kBlock, false> s_coop;
-    __shared__ uint8_t s_perm[2048];
+    __shared__ __align__(16) uint8_t s_perm[2048 + 1024];
     fill_perm(s_perm);
     SingleSource src;
     src.scene = L.scene;
@@ -616,7 +618,7 @@ template <int kShort, int kBlock>
 __global__ void __launch_bounds__(kBlock, MinBlocks(kBlock)) batch_kernel(const BatchLaunch B) {
     __shared__ uint2 s_stack[kShort * kBlock];
     __shared__ CoopShared<kBlock, true> s_coop;
-    __shared__ uint8_t s_perm[2048];
+    __shared__ __align__(16) uint8_t s_perm[2048 + 1024];
     fill_perm(s_perm);
     BatchSource src;
     src.jobs = B.jobs;

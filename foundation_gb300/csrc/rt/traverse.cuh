@@ -208,7 +208,8 @@ struct NodeHits {
 };
 
 // perm (optional): a table of 8 x 256 bytes, perm[oct * 256 + m] =
-// xor_permute8(m, oct), in place of the bit swaps.
+// xor_permute8(m, oct), in place of the bit swaps, followed by 256 words:
+// the triangle mask of a leaf slot by its meta byte.
 __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint4* __restrict__ nodes, uint32_t idx,
                                                    float tfar, const uint8_t* perm = nullptr) {
     const uint4* n = nodes + 5 * (size_t)idx;
@@ -280,7 +281,8 @@ __device__ __forceinline__ NodeHits intersect_node(const RayState& r, const uint
         const uint32_t s = (uint32_t)__ffs(lh) - 1u;
         lh &= lh - 1u;
         const uint32_t meta = __byte_perm(s < 4u ? w1.z : w1.w, 0u, 0x4440u | (s & 3u));
-        tris |= ((2u << ((meta >> 5) & 3u)) - 1u) << (meta & 31u);
+        tris |= perm ? reinterpret_cast<const uint32_t*>(perm + 2048)[meta]
+                     : ((2u << ((meta >> 5) & 3u)) - 1u) << (meta & 31u);
     }
     NodeHits out;
     out.child_base = w1.x;
