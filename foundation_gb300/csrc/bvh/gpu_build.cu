@@ -26,8 +26,9 @@
 //  6. collapse to 8-wide nodes, one wide level per launch: the children by
 //     the greedy rule of collapse.cpp (expand the largest-area internal child
 //     until 8) or by those decisions, octant slots, margin inflation and
-//     outward quantisation in double precision as on the host, children and
-//     leaf triangles allocated with atomics.
+//     outward quantisation in FP32 with directed rounding (conservative by
+//     construction; the host collapse uses FP64), children and leaf
+//     triangles allocated with atomics.
 #include "gpu_build.hpp"
 
 #include <algorithm>
@@ -98,17 +99,20 @@ __global__ void init_bounds_kernel(float* b) {
     if (i < 12) b[i] = (i % 6) < 3 ? __int_as_float(0x7F800000) : __int_as_float(0xFF800000);
 }
 
+// Grid-stride over the triangles: each thread folds its triangles' boxes and
+// centroids into its own bounds, the block reduces them, and one thread per
+// block updates the scene bounds (a few thousand atomics in all, not one set
+// per warp).
 __global__ void __launch_bounds__(256) prep_kernel(const float* __restrict__ verts, uint32_t nv,
                                                    const uint32_t* __restrict__ idx, uint32_t nt, Buffers B,
                                                    float4* __restrict__ shade) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    float lo[3], hi[3], c[3];
+    __shared__ float s_red[8][12];
+    float lo[3], hi[3], c[3], cmax[3];
     for (int a = 0; a < 3; ++a) {
         lo[a] = c[a] = __int_as_float(0x7F800000);
-        hi[a] = __int_as_float(0xFF800000);
+        hi[a] = cmax[a] = __int_as_float(0xFF800000);
     }
-    float cmax[3] = {hi[0], hi[1], hi[2]};
-    if (t < nt) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
         uint32_t vi[3];
         bool ok = true;
         for (int k = 0; k < 3; ++k) {
@@ -117,39 +121,44 @@ __global__ void __launch_bounds__(256) prep_kernel(const float* __restrict__ ver
         }
         if (!ok) {
             atomicOr(B.status, kPrepBadIndex);
-        } else {
-            float v[9];
-            bool finite = true;
-            for (int k = 0; k < 3; ++k)
-                for (int a = 0; a < 3; ++a) {
-                    v[3 * k + a] = verts[3 * (size_t)vi[k] + a];
-                    finite = finite && isfinite(v[3 * k + a]);
-                }
-            if (!finite) atomicOr(B.status, kPrepNonFinite);
-            for (int a = 0; a < 3; ++a) {
-                lo[a] = fminf(fminf(v[a], v[3 + a]), v[6 + a]);
-                hi[a] = fmaxf(fmaxf(v[a], v[3 + a]), v[6 + a]);
-                c[a] = cmax[a] = __fmul_rn(0.5f, __fadd_rn(lo[a], hi[a]));
-            }
-            B.blo[t] = make_float4(lo[0], lo[1], lo[2], 0.0f);
-            B.bhi[t] = make_float4(hi[0], hi[1], hi[2], 0.0f);
-            // geometric normal (winding order), the host's expression tree
-            const float e1x = __fsub_rn(v[3], v[0]), e1y = __fsub_rn(v[4], v[1]), e1z = __fsub_rn(v[5], v[2]);
-            const float e2x = __fsub_rn(v[6], v[0]), e2y = __fsub_rn(v[7], v[1]), e2z = __fsub_rn(v[8], v[2]);
-            float nx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
-            float ny = __fsub_rn(__fmul_rn(e1z, e2x), __fmul_rn(e1x, e2z));
-            float nz = __fsub_rn(__fmul_rn(e1x, e2y), __fmul_rn(e1y, e2x));
-            const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz)));
-            if (l > 0.0f) {
-                nx = __fdiv_rn(nx, l);
-                ny = __fdiv_rn(ny, l);
-                nz = __fdiv_rn(nz, l);
-            } else {
-                nx = ny = 0.0f;
-                nz = 1.0f;
-            }
-            shade[t] = make_float4(nx, ny, nz, 0.0f);
+            continue;
         }
+        float v[9];
+        bool finite = true;
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) {
+                v[3 * k + a] = verts[3 * (size_t)vi[k] + a];
+                finite = finite && isfinite(v[3 * k + a]);
+            }
+        if (!finite) atomicOr(B.status, kPrepNonFinite);
+        float tlo[3], thi[3];
+        for (int a = 0; a < 3; ++a) {
+            tlo[a] = fminf(fminf(v[a], v[3 + a]), v[6 + a]);
+            thi[a] = fmaxf(fmaxf(v[a], v[3 + a]), v[6 + a]);
+            const float cc = __fmul_rn(0.5f, __fadd_rn(tlo[a], thi[a]));
+            lo[a] = fminf(lo[a], tlo[a]);
+            hi[a] = fmaxf(hi[a], thi[a]);
+            c[a] = fminf(c[a], cc);
+            cmax[a] = fmaxf(cmax[a], cc);
+        }
+        B.blo[t] = make_float4(tlo[0], tlo[1], tlo[2], 0.0f);
+        B.bhi[t] = make_float4(thi[0], thi[1], thi[2], 0.0f);
+        // geometric normal (winding order), the host's expression tree
+        const float e1x = __fsub_rn(v[3], v[0]), e1y = __fsub_rn(v[4], v[1]), e1z = __fsub_rn(v[5], v[2]);
+        const float e2x = __fsub_rn(v[6], v[0]), e2y = __fsub_rn(v[7], v[1]), e2z = __fsub_rn(v[8], v[2]);
+        float nx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
+        float ny = __fsub_rn(__fmul_rn(e1z, e2x), __fmul_rn(e1x, e2z));
+        float nz = __fsub_rn(__fmul_rn(e1x, e2y), __fmul_rn(e1y, e2x));
+        const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz)));
+        if (l > 0.0f) {
+            nx = __fdiv_rn(nx, l);
+            ny = __fdiv_rn(ny, l);
+            nz = __fdiv_rn(nz, l);
+        } else {
+            nx = ny = 0.0f;
+            nz = 1.0f;
+        }
+        shade[t] = make_float4(nx, ny, nz, 0.0f);
     }
     for (int o = 16; o > 0; o >>= 1)
         for (int a = 0; a < 3; ++a) {
@@ -158,13 +167,30 @@ __global__ void __launch_bounds__(256) prep_kernel(const float* __restrict__ ver
             c[a] = fminf(c[a], __shfl_xor_sync(kFull, c[a], o));
             cmax[a] = fmaxf(cmax[a], __shfl_xor_sync(kFull, cmax[a], o));
         }
-    if ((threadIdx.x & 31u) == 0 && lo[0] <= hi[0]) {
+    const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31u) == 0)
         for (int a = 0; a < 3; ++a) {
-            atomic_min_f(B.bounds + a, lo[a]);
-            atomic_max_f(B.bounds + 3 + a, hi[a]);
-            atomic_min_f(B.bounds + 6 + a, c[a]);
-            atomic_max_f(B.bounds + 9 + a, cmax[a]);
+            s_red[warp][a] = lo[a];
+            s_red[warp][3 + a] = hi[a];
+            s_red[warp][6 + a] = c[a];
+            s_red[warp][9 + a] = cmax[a];
         }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (uint32_t w = 1; w < nw; ++w)
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fminf(lo[a], s_red[w][a]);
+                hi[a] = fmaxf(hi[a], s_red[w][3 + a]);
+                c[a] = fminf(c[a], s_red[w][6 + a]);
+                cmax[a] = fmaxf(cmax[a], s_red[w][9 + a]);
+            }
+        if (lo[0] <= hi[0])
+            for (int a = 0; a < 3; ++a) {
+                atomic_min_f(B.bounds + a, lo[a]);
+                atomic_max_f(B.bounds + 3 + a, hi[a]);
+                atomic_min_f(B.bounds + 6 + a, c[a]);
+                atomic_max_f(B.bounds + 9 + a, cmax[a]);
+            }
     }
 }
 
@@ -803,17 +829,19 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
         WideNode nd;
         uint32_t* ndw = reinterpret_cast<uint32_t*>(&nd);
         for (int w = 0; w < 20; ++w) ndw[w] = 0u;
-        double step[3];
+        // grid step 2^e per axis: the least e with 255 2^e >= the node's
+        // extent rounded up (all in FP32; 255 2^e and 2^-e are exact)
+        float inv_step[3];
         bool bad = false;
         for (int a = 0; a < 3; ++a) {
             nd.p[a] = nlo[a];
-            const double ext = (double)nhi[a] - (double)nlo[a];
-            int e = ext > 0.0 ? (int)ceil(log2(ext / 255.0)) : -100;
-            while (ldexp(255.0, e) < ext) e++;
-            while (e > -100 && ldexp(255.0, e - 1) >= ext) e--;
+            const float ext = __fsub_ru(nhi[a], nlo[a]);
+            int e = ext > 0.0f ? ilogbf(ext) - 8 : -100;
+            while (e <= 100 && ldexpf(255.0f, e) < ext) e++;
+            while (e > -100 && ldexpf(255.0f, e - 1) >= ext) e--;
             if (e < -100 || e > 100) bad = true;
             nd.e[a] = (uint8_t)(e + 127);
-            step[a] = ldexp(1.0, e);
+            inv_step[a] = ldexpf(1.0f, -e);
         }
         uint32_t n_int = 0, n_tri = 0;
         bool bad_tree = false;
@@ -831,17 +859,15 @@ __global__ void __launch_bounds__(128) collapse_kernel(const CollapseArgs A) {
         for (int s = 0; s < kWidth; ++s) {
             const int c = child_in_slot[s];
             if (c < 0) continue;
+            // outward: the offsets from p rounded down / up before the
+            // exact scaling by 2^-e, so p + ql 2^e <= lo and p + qh 2^e >= hi
+            // hold exactly; qh <= 255 since hi - p <= the node's extent
             for (int a = 0; a < 3; ++a) {
-                const double p = nd.p[a];
-                double ql = floor(((double)clo[c][a] - p) / step[a]);
-                double qh = ceil(((double)chi[c][a] - p) / step[a]);
-                ql = fmin(fmax(ql, 0.0), 255.0);
-                qh = fmin(fmax(qh, 0.0), 255.0);
-                while (ql > 0.0 && p + ql * step[a] > (double)clo[c][a]) ql -= 1.0;
-                while (qh < 255.0 && p + qh * step[a] < (double)chi[c][a]) qh += 1.0;
-                if (!(p + ql * step[a] <= (double)clo[c][a] && p + qh * step[a] >= (double)chi[c][a])) bad = true;
-                nd.qlo[a][s] = (uint8_t)ql;
-                nd.qhi[a][s] = (uint8_t)qh;
+                const float p = nd.p[a];
+                const float ql = floorf(__fmul_rd(__fsub_rd(clo[c][a], p), inv_step[a]));
+                const float qh = ceilf(__fmul_ru(__fsub_ru(chi[c][a], p), inv_step[a]));
+                nd.qlo[a][s] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
+                nd.qhi[a][s] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
             }
             if (is_leaf[c]) {
                 nd.meta[s] = (uint8_t)(kMetaLeafFlag | ((cnt[c] - 1u) << 5) | tri_off);
@@ -1076,7 +1102,7 @@ void BuildWideGpu(const float* d_verts, uint32_t nv, const uint32_t* d_idx, uint
     Check(cudaMemsetAsync(B.counters, 0, 4ull * (4 + kMaxLevels + 2), s), "memset");
     init_bounds_kernel<<<1, 32, 0, s>>>(B.bounds);
     const uint32_t g256 = (n + 255) / 256;
-    prep_kernel<<<g256, 256, 0, s>>>(d_verts, nv, d_idx, n, B, shade);
+    prep_kernel<<<std::max(1u, std::min(g256, 8u * (uint32_t)sms)), 256, 0, s>>>(d_verts, nv, d_idx, n, B, shade);
     uint32_t h_status = 0;
     float h_bounds[12];
     Check(cudaMemcpyAsync(&h_status, B.status, 4, cudaMemcpyDeviceToHost, s), "status readback");
