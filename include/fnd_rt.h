@@ -117,11 +117,13 @@ typedef struct fnd_rt_bvh_desc {
  * which tightens the tree of scenes with long, overlapping triangles. Hits
  * are identical either way. */
 enum { FND_BVH_SPATIAL_SPLITS = 1u };
-/* Build on the GPU: linear BVH over 63-bit Morton codes (Karras 2012) with
- * SAH leaf merging, collapsed to the same 8-wide format on the device. Much
- * faster to build, somewhat slower to trace than the binned-SAH tree; hits
- * are identical. Up to 2^27 triangles; not combined with spatial splits;
- * build_threads is ignored. */
+/* Build on the GPU: linear BVH over 63-bit Morton codes of the triangle
+ * centroids on cubic cells (Karras 2012), or FND_BVH_GPU_CLUSTER, with SAH
+ * leaf merging, collapsed to the same 8-wide format on the device. Much
+ * faster to build (31M triangles in tens of ms), a few per cent slower to
+ * trace than the binned-SAH tree on large flat scenes; hits are identical.
+ * Up to 2^27 triangles; not combined with spatial splits; build_threads is
+ * ignored. */
 enum { FND_BVH_GPU_BUILD = 2u };
 /* Collapse the binary tree into 8-wide nodes by the SAH-optimal dynamic
  * programme (Ylitie, Karras & Laine 2017) instead of the greedy rule: fuller
